@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""Benchmark of the mag2d PIC-MCC step on GB300: particle-steps/s.
+
+Workload (default): the 22-pole RF ion trap with null-collision MCC — 1e6 ions
+of 3 amu on a 257x257 x-y grid over a 10 mm square, uRF = (r/r0)^11 cos(11 phi)
+(r0 = 5 mm, 50 V at 17 MHz) loaded as a field table, He at 1e-2 Pa with an
+elastic cross section sigma ~ E^-1/2 (constant sigma v), dt = 2 ns.  Inputs are
+synthetic and seeded.  One bench step = one Pic::advance of all particles.
+
+Timing: W untimed warm-up steps, then K timed steps.  Between timed steps L2 is
+flushed by writing a 512 MB buffer on the simulation's stream (the particle
+state, 24 MB, would otherwise stay in the 129 MB L2); each step is bracketed by
+CUDA events on that stream and the step times are summed.  value = sum of live
+particles over the timed steps / summed step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU implementation of the step (the oracle port of
+the reference algorithm, FP64, the reference's SHR3/ziggurat random numbers)
+on all host cores, one independent sample per core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+METRIC = "PIC particle-steps/s"
+UNIT = "particle-steps/s"
+N_IONS = 1_000_000
+GRID = 257
+FLUSH_BYTES = 512 << 20
+BYTES_PER_PARTICLE_STEP = 44  # read x,z,vx,vy,vz,id (24 B) + write x,z,vx,vy,vz (20 B), FP32/uint32 SoA
+
+
+def _env_rank():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", str(r)))
+    return r, w, lr
+
+
+def _config(n_gpus: int, n_ions: int = N_IONS) -> dict:
+    return {"workload": "multipole_xy: 22-pole RF ion trap, 257x257 x-y grid, 1e6 ions (3 amu, 0.1 eV), "
+                        "He 1e-2 Pa elastic MCC, dt 2 ns", "grid": [GRID, GRID], "particles_per_gpu": n_ions,
+            "species": 2, "l2": "flushed between timed steps (512 MB write)",
+            "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"}
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline: the oracle port on the host cores
+def _cpu_worker(args):
+    """One core: the oracle port on a sample of the workload; returns (particle_steps, seconds)."""
+    n, steps, seed = args
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np  # noqa: F401
+
+    from cases import multipole_xy
+    from mag2d_cases import Port, load_port  # noqa: F401
+
+    with tempfile.TemporaryDirectory() as d:
+        tmp = Path(d)
+        cfg, species, inter, cpath, spath, parts, loaded = multipole_xy(tmp, n=n, n_nodes=GRID, seed=seed)
+        import numpy as np
+
+        mask = np.zeros((3, 3), dtype=np.int8)
+        volt = np.zeros((3, 3))
+        port = Port(cfg, species, inter, mask, volt, seed=seed, loaded_fields=loaded)
+        port.set_particles(1, *parts)
+        port.advance_init()
+        port.advance(2)
+        live0 = port.n_live(1)
+        t = port.time_advance(steps)
+        live1 = port.n_live(1)
+    return 0.5 * (live0 + live1) * steps, t
+
+
+def cpu_baseline(sample_particles: int = 20_000, sample_steps: int = 100, cores: int | None = None) -> dict:
+    import multiprocessing as mp
+
+    cores = cores or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(sample_particles, sample_steps, 100 + i) for i in range(cores)])
+    wall = time.perf_counter() - t0
+    ps = sum(r[0] for r in res)
+    per_core = sum(r[0] / r[1] for r in res) / len(res)
+    busy = max(r[1] for r in res)
+    return {"value": ps / busy, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cores} independent processes x ({sample_particles} ions x {sample_steps} steps) of the "
+                      f"same workload, FP64 oracle port with SHR3/ziggurat RNG; per-core {per_core:.3e} {UNIT}; "
+                      f"wall {wall:.1f} s incl. set-up",
+            "per_core": per_core}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return
+    base = cpu_baseline(sample_particles=20_000, sample_steps=50)
+    v = base["value"]
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": N_IONS / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": _config(args.gpus), "impl": "reference",
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self) -> dict:
+        self.out.flush()
+        rows = []
+        for line in Path(self.out.name).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(r[0] for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[2 + k].lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": rows[0][1], "reasons": reasons, "samples": len(rows)}
+
+
+def _load_profile_traffic():
+    p = ROOT / "profiles" / "push_multipole.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return d.get("dram_bytes_per_particle_step")
+        except Exception:
+            return None
+    return None
+
+
+def run_ours(args) -> None:
+    rank, world, local = _env_rank()
+    import numpy as np
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import __graft_entry__
+
+    if rank == 0 or not (ROOT / "mag2d_gb300" / "lib" / "libmag2d_gpu.so").exists():
+        __graft_entry__.build()
+    if world > 1:
+        dist.barrier()
+    import mag2d_gb300 as m
+    from cases import multipole_xy
+
+    tmp = Path(tempfile.mkdtemp(prefix=f"mag2d_bench_{rank}_"))
+    cfg, species, inter, cpath, spath, parts, loaded = multipole_xy(tmp, n=args.particles, n_nodes=GRID,
+                                                                    seed=2 + rank)
+    pic = m.Pic(cpath, spath, seed=1000 + rank, device=local, capacity_hint=args.particles)
+    ion = pic.speclist[1]
+    ion.set_particles(*parts)
+    pic.advance_init()
+    pic.sync()
+
+    stream = torch.cuda.ExternalStream(pic.stream, device=local)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(args.warmup):
+        flush_l2()
+        pic.advance(1)
+    pic.sync()
+    d0 = ion.diag()
+    launches0 = pic.kernel_launches
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush_l2()
+            starts[k].record(stream)
+            pic.advance(1)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) * 1e-3
+    d1 = ion.diag()
+    launches = pic.kernel_launches - launches0
+    psteps = d1["particle_steps"] - d0["particle_steps"]
+
+    # per-kernel device time (events between the kernels of each step), L2 flushed
+    kern = np.zeros(3)
+    nk = max(3, min(args.steps, 20))
+    for _ in range(nk):
+        flush_l2()
+        kern += np.array(pic.advance_timed(1))
+    push_ms = kern[1] / nk
+    live_now = ion.diag()["n_live"]
+    alg_bytes = BYTES_PER_PARTICLE_STEP * live_now
+    achieved = alg_bytes / (push_ms * 1e-3) / 1e9
+
+    # e2e through the C ABI with host buffers: upload the state from host arrays,
+    # advance a print interval of steps, read the diagnostics back
+    e2e_chunk = 50
+    hst = ion.particles()
+    host = [np.ascontiguousarray(hst[k]) for k in ("x", "z", "vx", "vy", "vz")]
+    n_host = len(host[0])
+    e2e_t = [float("inf")]
+    e2e_ps = 0
+    for _ in range(0 if args.no_e2e else 2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ion.set_particles(*host)
+        pic.advance(e2e_chunk)
+        dd = ion.diag()
+        e2e_t.append(time.perf_counter() - t0)
+        e2e_ps = dd["n_live"] * e2e_chunk
+    e2e_val = e2e_ps / min(e2e_t) if e2e_ps else 0.0
+
+    # max over ranks
+    vals = torch.tensor([total_s, psteps, e2e_val, launches], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        tmax = vals[0].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        tot = vals[1:2].clone()
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        e2 = vals[2:3].clone()
+        dist.all_reduce(e2, op=dist.ReduceOp.SUM)
+        total_s, psteps_all, e2e_all = float(tmax), float(tot), float(e2)
+    else:
+        psteps_all, e2e_all = float(psteps), float(e2e_val)
+    if rank == 0:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        peak = peaks.get("hbm_gbs", 6800.0)
+        traffic_ps = _load_profile_traffic()
+        base = None
+        if not args.no_cpu_baseline:
+            base = cpu_baseline(sample_particles=20_000, sample_steps=50)
+        line = {
+            "metric": METRIC, "value": psteps_all / total_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": _config(world, args.particles),
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_all, "unit": UNIT, "h2d_bytes_per_step": int(5 * 8 * n_host / e2e_chunk),
+                    "d2h_bytes_per_step": int(64 / e2e_chunk) + 1,
+                    "note": f"e2e step = set_particles from host FP64 arrays + advance({e2e_chunk}) + diag read"},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak,
+                         "traffic": (traffic_ps * live_now) if traffic_ps else None,
+                         "kernel": "k_push<0,2> (gather + Boris + MCC test + boundary)",
+                         "alg_bytes_per_launch": alg_bytes, "kernel_ms": push_ms,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured" if peaks else "fallback"},
+            "kernel_ms_per_step": {"solve": kern[0] / nk, "particles": kern[1] / nk, "collide": kern[2] / nk},
+        }
+        if base is not None:
+            line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(line), flush=True)
+    pic.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--particles", type=int, default=N_IONS, help="ions per GPU (default: the workload's 1e6)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

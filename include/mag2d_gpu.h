@@ -1,0 +1,184 @@
+/* mag2d_gpu — GB300 (sm_103a) implementation of the mag2d PIC-MCC time step.
+ *
+ * C ABI of libmag2d_gpu.so.  Plain pointers and sizes only; every call returns
+ * an int status (MAG_OK = 0, negative on error) and mag_last_error() gives the
+ * message of the last failing call on the calling thread.  No C++ exception
+ * crosses this boundary.
+ *
+ * The reference (rouckas/mag2d) has no plugin or FFI layer: its time loop is a
+ * C++ driver (src/test.cpp:18-97) that builds a Param from config.txt, a
+ * Pic<D> from it, runs the initscript, advance_init() and then advance() once
+ * per iteration.  Each entry point below replaces one of those C++ calls; the
+ * comment names the reference interface (file:line) it stands in for.
+ *
+ * Threading: one mag_sim per host thread.  Device memory belongs to the
+ * handle; every host buffer passed in or out is owned by the caller.  All work
+ * of a handle runs in order on the handle's own CUDA stream.
+ */
+#ifndef MAG2D_GPU_H
+#define MAG2D_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MAG_OK = 0,
+    MAG_EINVAL = -1,     /* bad argument or configuration (Param / config_parse errors) */
+    MAG_ECUDA = -2,      /* CUDA runtime error */
+    MAG_ERANGE = -3,     /* particle or node index outside the grid (Field2D range checks) */
+    MAG_ENOTCONV = -4,   /* Poisson solve did not reach its tolerance */
+    MAG_ETIMEOUT = -5,   /* a bounded device-side wait gave up */
+    MAG_EIO = -6,        /* file could not be read */
+    MAG_ENOMEM = -7
+};
+
+/* Field selectors for mag_get_field / mag_set_field (Fields members, src/fields.hpp:187-222) */
+enum {
+    MAG_U = 0,        /* electrostatic potential u [V] */
+    MAG_URF = 1,      /* RF unit potential uRF [V per V of rf_amplitude] */
+    MAG_RHO = 2,      /* field.rho: summed species charge per node [C], as deposited */
+    MAG_MASK = 3,     /* t_grid::mask: FIXED=0, FIXED_RF=1, FREE=2, BOUNDARY=3 */
+    MAG_VOLTAGE = 4,  /* t_grid::voltage [V] */
+    MAG_SPECIES_RHO = 5 /* + species index: BaseSpecies::rho [C] */
+};
+
+typedef struct mag_sim mag_sim;
+
+typedef struct {
+    int device;            /* CUDA device ordinal */
+    uint64_t seed;         /* Philox key of every random draw */
+    int sort_interval;     /* counting sort of particles by cell every N steps (0 = never) */
+    double poisson_tol;    /* Jacobi-scaled residual / max|u| at which the solve stops (0 = 1e-12) */
+    int poisson_max_iter;  /* outer refinement iterations before MAG_ENOTCONV (0 = 200) */
+    int64_t capacity_hint; /* particle slots to reserve per species (0 = grow as needed) */
+} mag_opts;
+
+typedef struct {
+    char name[64];
+    int type;              /* SpeciesType: NEUTRAL=0, ELECTRON=1, ION=2 (src/parser.hpp:14) */
+    double mass, charge, dt, density, temperature, E_max, v_max, lifetime;
+    int64_t n_live;        /* BaseSpecies::n_particles (src/particles.hpp:248) */
+    int64_t capacity;
+    uint64_t niter;        /* steps this species has advanced */
+} mag_species_info;
+
+typedef struct {
+    int64_t n_live;
+    double mean_energy_eV;   /* mean (vx^2+vy^2+vz^2) m / 2 / q_e over live particles (FP64) */
+    double total_charge;     /* n_live * charge * macroparticle factor of the deposit [C] */
+    int64_t collisions;      /* real (non-null) collisions since creation */
+    int64_t null_collisions; /* candidates that the null-collision test rejected */
+    int64_t removed;         /* particles removed at the boundary since creation */
+    int64_t particle_steps;  /* sum over completed steps of the live particles after the step */
+    uint64_t niter;          /* completed steps of this species */
+} mag_diag_out;
+
+typedef struct {
+    int iterations;          /* outer FP64 refinement iterations of the last solve */
+    double residual;         /* Jacobi-scaled residual / max|u| after the last solve */
+    int status;              /* MAG_OK or MAG_ENOTCONV */
+    int levels;              /* multigrid levels (1 = plain red-black SOR) */
+} mag_solve_info;
+
+const char* mag_last_error(void);
+
+/* Library version string. */
+const char* mag_version(void);
+
+/* Param(GetPot&) + Pic<D>(param) + run_initscript (src/test.cpp:24-53,
+ * src/param.cpp:12-143, src/pic.cpp:127-189, :241-328).  initscript may be
+ * NULL.  opts may be NULL for defaults. */
+int mag_create(const char* config_path, const char* species_conf_path, const char* initscript_path,
+               const mag_opts* opts, mag_sim** out);
+void mag_destroy(mag_sim* sim);
+
+/* Pic::run_initscript (src/pic.cpp:241-328) */
+int mag_run_initscript(mag_sim* sim, const char* initscript_path);
+
+/* Pic::advance_init (src/pic.cpp:359-384) */
+int mag_advance_init(mag_sim* sim);
+
+/* nsteps calls of Pic::advance (src/pic.cpp:330-358).  Asynchronous: returns
+ * once the work is queued; errors found on the device are reported by the
+ * next synchronising call (mag_sync, getters). */
+int mag_advance(mag_sim* sim, uint64_t nsteps);
+
+/* mag_advance with CUDA events recorded on the handle's stream between the
+ * kernels of every step; ms_out[0..2] receive the summed device time of the
+ * Poisson solve, the particle kernel and the collision kernel.  Synchronises. */
+int mag_advance_timed(mag_sim* sim, uint64_t nsteps, double* ms_out);
+
+/* Wait for queued work and report any device-side error flag. */
+int mag_sync(mag_sim* sim);
+
+/* Grid of field u (Field2D::GetDx/GetDy/GetXMin..., src/Field2D.hpp:32-37). */
+int mag_grid(mag_sim* sim, int* nx, int* nz, double* dx, double* dz, double* x_min, double* z_min);
+
+int mag_n_species(mag_sim* sim);
+int mag_species(mag_sim* sim, int species, mag_species_info* out);
+
+/* Copy a field to host (Field2D data, row-major, z fastest; x_sampl*z_sampl doubles). */
+int mag_get_field(mag_sim* sim, int which, double* host_out);
+/* Overwrite u, uRF or rho from host doubles (e.g. for a solve of a given rho). */
+int mag_set_field(mag_sim* sim, int which, const double* host_in);
+
+/* Fields::boundary_solve (src/fields.cpp:278-312): solve for u from the current
+ * rho (MAG_RHO) exactly as a self-consistent step does. */
+int mag_field_solve(mag_sim* sim, mag_solve_info* info);
+
+/* Live particles of a species as SoA doubles in SI units (the t_particle
+ * fields x, z, vx, vy, vz of src/particles.hpp:26-33) plus a persistent id.
+ * Any pointer may be NULL.  *n_out receives the number written (<= cap). */
+int mag_get_particles(mag_sim* sim, int species, int64_t cap, double* x, double* z, double* vx,
+                      double* vy, double* vz, uint32_t* id, int64_t* n_out);
+/* Replace the particles of a species (ids 0..n-1 in input order). */
+int mag_set_particles(mag_sim* sim, int species, int64_t n, const double* x, const double* z,
+                      const double* vx, const double* vy, const double* vz);
+
+/* Diagnostics of one species (BaseSpecies::print_status, src/particles.cpp:367-375). */
+int mag_diag(mag_sim* sim, int species, mag_diag_out* out);
+
+/* Fixed-point charge accumulator of a species: int64 per node, each live
+ * particle contributing exactly 2^40 split over its four CIC nodes
+ * (Field2D::accumulate weights, src/Field2D.hpp:45-62, quantised to 2^-20 per
+ * axis).  Reflects the deposit of the last step. */
+int mag_get_rho_fixed(mag_sim* sim, int species, int64_t* host_out);
+
+/* Recompute the fixed-point deposit of the current particles of every species
+ * (Species::accumulate, src/particles.hpp:358-367) without moving them. */
+int mag_deposit(mag_sim* sim);
+
+/* ---- host-only inspection (no GPU needed) -------------------------------- */
+
+/* A value of the Param built from config_path (src/param.cpp:12-143), by key:
+ * the config keys (x_max, z_max, x_sampl, z_sampl, extern_field, rf_omega,
+ * macroparticle_factor, Br, Bz, Bt, ...), the derived dx, dz, idx, idz, V, dV,
+ * dy, neutral_density, and the enumerations coord, boundary, geometry,
+ * selfconsistent, rf, electric_field_from_file as numbers. */
+int mag_config_param(const char* config_path, const char* key, double* value);
+
+/* t_grid mask and voltage of the config's geometry (src/fields.cpp:374-868).
+ * cap = capacity of the output arrays in nodes; *nx, *nz receive the grid. */
+int mag_config_geometry(const char* config_path, int64_t cap, int8_t* mask, double* voltage, int* nx, int* nz);
+
+/* Species 'index' of species_conf_path as parsed (src/parser.cpp:25-147), with
+ * its null-collision rates against every species (rates_out, n_species
+ * doubles) and lifetime (BaseSpecies::lifetime_init, src/particles.cpp:142-206).
+ * Returns the number of species. */
+int mag_config_species(const char* config_path, const char* species_conf_path, int index,
+                       mag_species_info* out, double* rates_out);
+
+/* Device stream of the handle (a cudaStream_t) so callers can order their own
+ * work and timing events with the simulation's. */
+void* mag_stream(mag_sim* sim);
+
+/* Number of kernel launches the handle has issued since creation. */
+int64_t mag_kernel_launches(mag_sim* sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,362 @@
+// C ABI of libmag2d_gpu.so (include/mag2d_gpu.h).  Every entry point catches
+// C++ exceptions and turns them into a status code plus mag_last_error().
+#include "mag2d_gpu.h"
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+
+#include "sim.hpp"
+
+struct mag_sim {
+    std::unique_ptr<mag::Sim> s;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const mag::Error& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "out of host memory";
+        return MAG_ENOMEM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return MAG_EINVAL;
+    }
+}
+
+int check_species(mag_sim* sim, int s)
+{
+    if (!sim || !sim->s) throw mag::Error(MAG_EINVAL, "null simulation handle");
+    if (s < 0 || s >= (int)sim->s->sp.size()) throw mag::Error(MAG_EINVAL, "species index out of range");
+    return 0;
+}
+
+int device_status(mag_sim* sim)
+{
+    const int e = sim->s->sync();
+    if (e == 0) return MAG_OK;
+    switch (e) {
+    case -4: g_last_error = "Poisson solve did not reach its tolerance"; break;
+    case -5: g_last_error = "a bounded device-side wait gave up"; break;
+    case -3: g_last_error = "particle or node index outside the grid"; break;
+    default: g_last_error = "device error " + std::to_string(e); break;
+    }
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mag_last_error(void) { return g_last_error.c_str(); }
+
+const char* mag_version(void) { return "mag2d_gb300 0.1 (sm_103a)"; }
+
+int mag_create(const char* config_path, const char* species_conf_path, const char* initscript_path,
+               const mag_opts* opts, mag_sim** out)
+{
+    return guarded([&]() {
+        if (!config_path || !species_conf_path || !out) throw mag::Error(MAG_EINVAL, "null argument");
+        mag::SimOptions o;
+        if (opts) {
+            o.device = opts->device;
+            o.seed = opts->seed;
+            o.sort_interval = opts->sort_interval;
+            o.poisson_tol = opts->poisson_tol;
+            o.poisson_max_iter = opts->poisson_max_iter;
+            o.capacity_hint = opts->capacity_hint;
+        }
+        auto h = std::make_unique<mag_sim>();
+        h->s = std::make_unique<mag::Sim>(config_path, species_conf_path, o);
+        if (initscript_path && *initscript_path) h->s->run_initscript(initscript_path);
+        *out = h.release();
+        return MAG_OK;
+    });
+}
+
+void mag_destroy(mag_sim* sim) { delete sim; }
+
+int mag_run_initscript(mag_sim* sim, const char* path)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->run_initscript(path);
+        return MAG_OK;
+    });
+}
+
+int mag_advance_init(mag_sim* sim)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->advance_init();
+        return MAG_OK;
+    });
+}
+
+int mag_advance(mag_sim* sim, uint64_t nsteps)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->advance(nsteps);
+        return MAG_OK;
+    });
+}
+
+int mag_advance_timed(mag_sim* sim, uint64_t nsteps, double* ms_out)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->advance_timed(nsteps, ms_out);
+        return device_status(sim);
+    });
+}
+
+int mag_sync(mag_sim* sim)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        return device_status(sim);
+    });
+}
+
+int mag_grid(mag_sim* sim, int* nx, int* nz, double* dx, double* dz, double* x_min, double* z_min)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        mag::Sim& s = *sim->s;
+        if (nx) *nx = s.nx;
+        if (nz) *nz = s.nz;
+        if (dx) *dx = s.dx;
+        if (dz) *dz = s.dz;
+        if (x_min) *x_min = s.x0;
+        if (z_min) *z_min = s.z0;
+        return MAG_OK;
+    });
+}
+
+int mag_n_species(mag_sim* sim)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        return (int)sim->s->sp.size();
+    });
+}
+
+int mag_species(mag_sim* sim, int species, mag_species_info* out)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        mag::Sim& s = *sim->s;
+        const mag::SpeciesState& S = s.sp[species];
+        std::memset(out, 0, sizeof *out);
+        std::strncpy(out->name, S.prm.name.c_str(), sizeof out->name - 1);
+        out->type = S.prm.type;
+        out->mass = S.prm.mass;
+        out->charge = S.prm.charge;
+        out->dt = S.prm.dt;
+        out->density = S.prm.density;
+        out->temperature = S.prm.temperature;
+        out->E_max = S.E_max;
+        out->v_max = S.v_max;
+        out->lifetime = S.lifetime;
+        out->capacity = S.cap;
+        if (S.n_slots > 0) {
+            double e2;
+            unsigned long long n;
+            s.energy(species, e2, n);
+            out->n_live = (int64_t)n;
+        }
+        out->niter = s.niter(species);
+        return MAG_OK;
+    });
+}
+
+int mag_get_field(mag_sim* sim, int which, double* host_out)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->get_field(which, host_out);
+        return MAG_OK;
+    });
+}
+
+int mag_set_field(mag_sim* sim, int which, const double* host_in)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->set_field(which, host_in);
+        return MAG_OK;
+    });
+}
+
+int mag_field_solve(mag_sim* sim, mag_solve_info* info)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        mag::SolveStatus st = sim->s->field_solve();
+        int rc = device_status(sim);
+        if (info) {
+            info->iterations = st.iterations;
+            info->residual = st.residual;
+            info->status = st.converged ? MAG_OK : MAG_ENOTCONV;
+            info->levels = sim->s->solver_levels();
+        }
+        return rc;
+    });
+}
+
+int mag_get_particles(mag_sim* sim, int species, int64_t cap, double* x, double* z, double* vx, double* vy,
+                      double* vz, uint32_t* id, int64_t* n_out)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        int64_t n = 0;
+        sim->s->get_particles(species, cap, x, z, vx, vy, vz, id, &n);
+        if (n_out) *n_out = n;
+        return device_status(sim);
+    });
+}
+
+int mag_set_particles(mag_sim* sim, int species, int64_t n, const double* x, const double* z, const double* vx,
+                      const double* vy, const double* vz)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (n < 0) throw mag::Error(MAG_EINVAL, "negative particle count");
+        sim->s->set_particles(species, n, x, z, vx, vy, vz);
+        return MAG_OK;
+    });
+}
+
+int mag_diag(mag_sim* sim, int species, mag_diag_out* out)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        mag::Sim& s = *sim->s;
+        const mag::SpeciesState& S = s.sp[species];
+        std::memset(out, 0, sizeof *out);
+        double e2 = 0;
+        unsigned long long n = 0;
+        if (S.n_slots > 0) s.energy(species, e2, n);
+        out->n_live = (int64_t)n;
+        out->mean_energy_eV = n ? e2 / (double)n * S.prm.mass * 0.5 / mag::kQe : 0.0;
+        out->total_charge = (double)n * S.prm.charge * s.p.macroparticle_factor;
+        const mag::Counters c = s.counters(species);
+        out->collisions = (int64_t)c.ncoll;
+        out->null_collisions = (int64_t)c.nnull;
+        out->removed = (int64_t)c.removed;
+        out->particle_steps = (int64_t)c.live_sum;
+        out->niter = s.niter(species);
+        return device_status(sim);
+    });
+}
+
+int mag_get_rho_fixed(mag_sim* sim, int species, int64_t* host_out)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        sim->s->get_rho_fixed(species, host_out);
+        return MAG_OK;
+    });
+}
+
+int mag_deposit(mag_sim* sim)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->deposit_all();
+        return device_status(sim);
+    });
+}
+
+int mag_config_param(const char* config_path, const char* key, double* value)
+{
+    return guarded([&]() {
+        const mag::Param p = mag::make_param(mag::KeyValueConfig::from_file(config_path));
+        const std::string k = key;
+        const std::map<std::string, double> v = {
+            {"x_max", p.x_max}, {"y_max", p.y_max}, {"z_max", p.z_max}, {"x_sampl", (double)p.x_sampl},
+            {"z_sampl", (double)p.z_sampl}, {"n_particles_total", p.n_particles_total},
+            {"density_total", p.density_total}, {"pressure", p.pressure},
+            {"neutral_temperature", p.neutral_temperature}, {"probe_radius", p.probe_radius},
+            {"u_probe", p.u_probe}, {"extern_field", p.extern_field}, {"Br", p.Br}, {"Bz", p.Bz}, {"Bt", p.Bt},
+            {"rf_amplitude", p.rf_amplitude}, {"rf_U0", p.rf_U0}, {"rf_omega", p.rf_omega},
+            {"macroparticle_factor", p.macroparticle_factor}, {"dx", p.dx}, {"dz", p.dz}, {"idx", p.idx},
+            {"idz", p.idz}, {"V", p.V}, {"dV", p.dV}, {"dy", p.dy}, {"neutral_density", p.neutral_density},
+            {"coord", (double)p.coord}, {"boundary", (double)p.boundary}, {"geometry", (double)p.geometry},
+            {"selfconsistent", (double)p.selfconsistent}, {"rf", (double)p.rf},
+            {"electric_field_from_file", (double)p.electric_field_from_file},
+            {"magnetic_field_const", (double)p.magnetic_field_const}, {"niter", (double)p.niter},
+            {"t_print", (double)p.t_print}, {"t_dist_sample", (double)p.t_dist_sample},
+            {"t_equilib", (double)p.t_equilib}, {"mover", (double)p.mover}};
+        auto it = v.find(k);
+        if (it == v.end()) throw mag::Error(MAG_EINVAL, "unknown Param key " + k);
+        *value = it->second;
+        return MAG_OK;
+    });
+}
+
+int mag_config_geometry(const char* config_path, int64_t cap, int8_t* mask, double* voltage, int* nx, int* nz)
+{
+    return guarded([&]() {
+        const mag::Param p = mag::make_param(mag::KeyValueConfig::from_file(config_path));
+        std::vector<int8_t> m;
+        std::vector<double> v;
+        mag::build_geometry(p, m, v);
+        if (nx) *nx = p.x_sampl;
+        if (nz) *nz = p.z_sampl;
+        if ((int64_t)m.size() > cap) throw mag::Error(MAG_EINVAL, "output arrays too small");
+        if (mask) std::copy(m.begin(), m.end(), mask);
+        if (voltage) std::copy(v.begin(), v.end(), voltage);
+        return MAG_OK;
+    });
+}
+
+int mag_config_species(const char* config_path, const char* species_conf_path, int index, mag_species_info* out,
+                       double* rates_out)
+{
+    return guarded([&]() {
+        (void)config_path;
+        std::vector<mag::SpeciesParams> sp;
+        std::vector<mag::InteractionParams> in;
+        mag::parse_species_conf(species_conf_path, sp, in);
+        if (index < 0 || index >= (int)sp.size()) throw mag::Error(MAG_EINVAL, "species index out of range");
+        std::vector<double> rates;
+        double lifetime;
+        mag::species_rates(sp, in, index, rates, lifetime);
+        const mag::SpeciesParams& S = sp[index];
+        if (out) {
+            std::memset(out, 0, sizeof *out);
+            std::strncpy(out->name, S.name.c_str(), sizeof out->name - 1);
+            out->type = S.type;
+            out->mass = S.mass;
+            out->charge = S.charge;
+            out->dt = S.dt;
+            out->density = S.density;
+            out->temperature = S.temperature;
+            out->E_max = S.E_max > 0. ? S.E_max : S.temperature * mag::kKB / mag::kQe * 10.0;
+            out->v_max = std::sqrt(2.0 * mag::kKB * S.temperature / S.mass);
+            out->lifetime = lifetime;
+        }
+        if (rates_out) std::copy(rates.begin(), rates.end(), rates_out);
+        return (int)sp.size();
+    });
+}
+
+void* mag_stream(mag_sim* sim) { return sim && sim->s ? (void*)sim->s->stream : nullptr; }
+
+int64_t mag_kernel_launches(mag_sim* sim) { return sim && sim->s ? sim->s->launches : 0; }
+
+}  // extern "C"

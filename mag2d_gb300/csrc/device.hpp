@@ -1,0 +1,169 @@
+// Data shared between the host orchestration and the sm_103a kernels.
+//
+// HBM layout of one species (SoA, one array per component, length = slots):
+//   x, z   float   position in grid units of the field grid, (x - x_min)/dx and
+//                  (z - z_min)/dz; a removed particle holds x = -1
+//   vx, vy, vz float  velocity [m/s]; (vx, vy, vz) = (radial/x, azimuthal/y, axial/z)
+//                  as in t_particle (src/particles.hpp:26-33)
+//   id     uint32  persistent particle id (key of its random stream)
+// Fields live on node grids of nx*nz points, row-major with z fastest
+// (Array2D, src/Array.hpp:14-23).  The electric field is kept on cell faces:
+//   Exf[(nx+1)*nz]  -du/dx between nodes i-1 and i, with the end faces repeated
+//   Ezf[nx*(nz+1)]  -du/dz between nodes j-1 and j
+// which makes the staggered gradient of Field2D::grad (src/Field2D.hpp:80-168)
+// a plain bilinear interpolation of four face values per component.
+#pragma once
+#include <cstdint>
+
+namespace mag {
+
+constexpr int kMaxSpecies = 16;
+constexpr int kMaxInteractions = 64;
+constexpr int kMaxLevels = 12;
+constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis
+constexpr float kDeadX = -1.0f;
+
+// CollType of the species_conf INTERACTION blocks (src/parser.hpp:15)
+enum CollType { ELASTIC = 0, LANGEVIN = 1, CX = 2, COULOMB = 3, SUPERELASTIC = 4 };
+
+struct Counters {
+    unsigned long long niter;      // steps advanced by this species
+    unsigned long long live_step;  // live particles counted by the running step
+    unsigned long long live_last;  // live particles after the last completed step
+    unsigned long long live_sum;   // sum over completed steps of live particles
+    unsigned long long removed;    // particles removed at the boundary
+    unsigned long long ncand;      // collision candidates of the running step
+    unsigned long long ncoll;      // real collisions
+    unsigned long long nnull;      // null collisions
+    unsigned long long partner_miss;
+    unsigned long long done_blocks;
+    int error;                     // first device error code (0 = none)
+    int pad;
+};
+
+struct PushArgs {
+    float *x, *z, *vx, *vy, *vz;
+    const uint32_t* id;
+    int64_t n;
+    int nx, nz;
+    float xmaxg, zmaxg;   // domain extent in grid units
+    int periodic;
+    int check_mask;       // kill particles in cells with no FREE corner (t_grid::is_free)
+    const int8_t* mask;   // nx*nz
+    // electric field: 0 uniform (0, extern_ez), 1 from u, 2 from u and uRF
+    int emode;
+    const float* Exf;
+    const float* Ezf;
+    const float* Exf_rf;
+    const float* Ezf_rf;
+    float extern_ez;
+    double rf_omega, rf_amp, rf_U0, dt;
+    // magnetic field: constant Boris vectors, or tables Br/Bz (Field2D::interpolate)
+    int btab;
+    float tx, ty, tz, sx, sy, sz;
+    const float* Br;
+    const float* Bz;
+    int bnx, bnz;
+    float b_x0, b_z0, b_ix, b_iz;  // table index = (xg*dx + x_min - b_xmin) * b_idx
+    float gdx, gdz, gx0, gz0;      // field grid dx, dz, x_min, z_min (for tables)
+    float q_dt_2m;                 // charge*dt/(2*mass)
+    float hq;                      // charge/mass*dt/2
+    float cx, cz;                  // dt/dx, dt/dz
+    unsigned long long* rho;       // fixed-point deposit (nx*nz) or null
+    uint32_t coll_threshold;       // collision probability * 2^32 (0: no test)
+    uint32_t* cand;
+    uint64_t seed;
+    uint32_t species;
+    Counters* cnt;
+};
+
+struct InterDev {
+    int type;          // CollType
+    int target;        // secondary species index
+    double DE;         // [J]
+    double rate;       // RATE (LANGEVIN: already times cutoff^2)
+    double cutoff;
+    double mu;         // reduced mass
+    int tab_off, tab_n;
+    double coul_lambda_D, coul_q1q2;
+};
+
+struct CollideArgs {
+    float *vx, *vy, *vz;
+    const uint32_t* id;
+    const uint32_t* cand;
+    Counters* cnt;
+    double mass, inv_lifetime;
+    int nsp;
+    double rates[kMaxSpecies];
+    double t_mass[kMaxSpecies], t_density[kMaxSpecies], t_sigma_v[kMaxSpecies];
+    int t_has_slots[kMaxSpecies];
+    float* t_x[kMaxSpecies];
+    float* t_vx[kMaxSpecies];
+    float* t_vy[kMaxSpecies];
+    float* t_vz[kMaxSpecies];
+    int64_t t_n[kMaxSpecies];
+    int inter_begin[kMaxSpecies], inter_end[kMaxSpecies];
+    const InterDev* inter;
+    const double* tables;  // E_eV then sigma, per interaction
+    uint64_t seed;
+    uint32_t species;
+    // step-end bookkeeping done by the last block
+    unsigned long long* rho_unused;
+};
+
+struct SolveStatus {
+    int iterations;
+    int converged;
+    double residual;
+    int aborted;
+    int pad;
+};
+
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+    unsigned int abort;
+    unsigned int pad;
+};
+
+struct MGLevelDev {
+    int nx, nz;
+    float* e;               // correction
+    float* r;               // right-hand side of the correction equation
+    float* t;               // residual scratch
+    const float* coef;      // 9 planes of nx*nz (levels >= 1), plane k = (di+1)*3 + (dj+1)
+    const float* inv_diag;  // levels >= 1
+};
+
+struct SolveArgs {
+    int coord;              // 0 Cartesian, 1 cylindrical
+    int nx, nz;
+    double dx, dz;
+    const int8_t* mask;
+    const double* voltage;
+    double* u;              // FP64 solution (in/out, warm start)
+    double* b;              // FP64 right-hand side (scratch)
+    int rf_solve;           // boundary_solve_rf: FIXED -> 0, FIXED_RF -> voltage
+    int rho_src;            // 0 none, 1 fixed-point species accumulators, 2 FP64 array
+    const unsigned long long* rho_fixed[kMaxSpecies];
+    double rho_weight[kMaxSpecies];  // charge * 2^-40
+    int nsp;
+    const double* rho64;
+    int clear_rho;
+    double mpf, dV;         // macroparticle_factor, cell volume (Cartesian scaling)
+    int nlev;
+    MGLevelDev lev[kMaxLevels];
+    int nu1, nu2, ncoarse;
+    float omega;            // SOR factor for the one-level smoother
+    double tol;
+    int max_outer;
+    float* Exf;             // faces of -grad u (may be null)
+    float* Ezf;
+    double* red;            // reduction scratch (4 doubles)
+    GridBarrier* bar;
+    SolveStatus* status;
+    int* err;
+};
+
+}  // namespace mag

@@ -1,0 +1,149 @@
+// Small kernels: particle loaders of the initscript, fills and reductions.
+#include "device.hpp"
+#include "kernels.hpp"
+#include "philox.hpp"
+
+namespace mag {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+struct LoadArgs {
+    float *x, *z, *vx, *vy, *vz;
+    uint32_t* id;
+    int64_t n;
+    uint32_t id0;
+    int kind;  // 0 disk, 1 everywhere, 2 bessel, 3 cylinder (r-z)
+    double cx, cz, radius, zlo, zhi, x0, z0, dx, dz, xmax, zmax, vsig;
+    uint64_t seed;
+    uint32_t species;
+};
+
+struct LStream {
+    uint64_t seed;
+    uint32_t sp, id;
+    uint32_t blk = 0;
+    U4 buf;
+    int pos = 4;
+    __device__ double uni()
+    {
+        if (pos >= 4) {
+            buf = draw(seed, sp, id, 0, TAG_LOAD, blk++);
+            pos = 0;
+        }
+        const uint32_t a = pos == 0 ? buf.x : buf.z;
+        const uint32_t b = pos == 0 ? buf.y : buf.w;
+        pos += 2;
+        return u01d(a, b);
+    }
+    __device__ double normal()
+    {
+        const double u1 = 1.0 - uni(), u2 = uni();
+        return sqrt(-2.0 * log(u1)) * cos(2.0 * kPi * u2);
+    }
+};
+
+// Species::add_particles_on_disk / _everywhere / _bessel (src/particles.cpp:685-749)
+// with Philox draws; kind 3 (uniform in a cylinder r < radius, zlo < z < zhi,
+// r = radius * sqrt(u)) is the r-z loader the reference leaves undefined.
+__global__ void k_load(const LoadArgs a)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const uint32_t pid = a.id0 + (uint32_t)k;
+    LStream r{a.seed, a.species, pid};
+    double x = 0, z = 0;
+    bool ok = true;
+    if (a.kind == 0) {
+        double px, py;
+        int t = 0;
+        do {
+            px = r.uni() - 0.5;
+            py = r.uni() - 0.5;
+        } while (px * px + py * py > 0.25 && ++t < 200);
+        x = px * 2 * a.radius + a.cx;
+        z = py * 2 * a.radius + a.cz;
+    } else if (a.kind == 1) {
+        x = a.x0 + (a.xmax - a.x0) * r.uni();
+        z = a.z0 + (a.zmax - a.z0) * r.uni();
+    } else if (a.kind == 2) {
+        const double root = 2.404825557695773;
+        double px, py, rr;
+        int t = 0;
+        do {
+            px = r.uni() * 2 - 1.0;
+            py = r.uni() * 2 - 1.0;
+            rr = sqrt(px * px + py * py);
+        } while ((rr > 1.0 || r.uni() > j0(rr * root)) && ++t < 400);
+        x = px * a.radius + a.cx;
+        z = py * a.radius + a.cz;
+    } else {
+        x = a.radius * sqrt(r.uni());
+        z = a.zlo + (a.zhi - a.zlo) * r.uni();
+    }
+    if (x < a.x0 || x > a.xmax || z < a.z0 || z > a.zmax) ok = false;
+    a.x[k] = ok ? (float)((x - a.x0) / a.dx) : kDeadX;
+    a.z[k] = (float)((z - a.z0) / a.dz);
+    a.vx[k] = (float)(r.normal() * a.vsig);
+    a.vz[k] = (float)(r.normal() * a.vsig);
+    a.vy[k] = (float)(r.normal() * a.vsig);
+    a.id[k] = pid;
+}
+
+__global__ void k_fill_u32(uint32_t* p, uint32_t v0, int64_t n)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        p[k] = v0 + (uint32_t)k;
+}
+
+__global__ void k_energy(const float* x, const float* vx, const float* vy, const float* vz, int64_t n, double* sum,
+                         unsigned long long* cnt)
+{
+    double s = 0.0;
+    unsigned long long c = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        if (!(x[k] >= 0.f)) continue;
+        const double a = vx[k], b = vy[k], d = vz[k];
+        s += a * a + b * b + d * d;
+        ++c;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(sum, s);
+        atomicAdd(cnt, c);
+    }
+}
+
+}  // namespace
+
+int launch_load_disk(float* x, float* z, float* vx, float* vy, float* vz, uint32_t* id, int64_t n, uint32_t id0,
+                     int kind, double cx, double cz, double radius, double zlo, double zhi, double x0, double z0,
+                     double dx, double dz, double xmax, double zmax, double vsig, uint64_t seed, uint32_t species,
+                     int, cudaStream_t s)
+{
+    if (n == 0) return 0;
+    LoadArgs a{x, z, vx, vy, vz, id, n, id0, kind, cx, cz, radius, zlo, zhi, x0, z0, dx, dz, xmax, zmax, vsig, seed, species};
+    k_load<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    return 1;
+}
+
+int launch_fill_u32(uint32_t* p, uint32_t v0, int64_t n, cudaStream_t s)
+{
+    if (n == 0) return 0;
+    k_fill_u32<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(p, v0, n);
+    return 1;
+}
+
+int launch_energy(const float* x, const float* vx, const float* vy, const float* vz, int64_t n, double* out_sum_v2,
+                  unsigned long long* out_n, cudaStream_t s)
+{
+    if (n == 0) return 0;
+    k_energy<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8), 256, 0, s>>>(x, vx, vy, vz, n, out_sum_v2, out_n);
+    return 1;
+}
+
+}  // namespace mag

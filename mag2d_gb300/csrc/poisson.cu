@@ -1,0 +1,451 @@
+// Poisson solve of Fields::boundary_solve / boundary_solve_rf
+// (src/fields.cpp:278-348) on the reference's own 5-point operator
+// (assembly src/fields.cpp:136-259, solved as the row stencil through
+// UMFPACK_At at :311).
+//
+// One persistent kernel runs the whole solve: it builds the FP64 right-hand
+// side exactly as the reference scales rho, then iterates
+//     r = b - A u            (FP64, Jacobi-scaled max-norm as stopping test)
+//     A e = r                (FP32 multigrid V-cycle: red-black Gauss-Seidel
+//                             on the fine 5-point operator, 4-colour
+//                             Gauss-Seidel on Galerkin 9-point coarse levels)
+//     u += e                 (FP64)
+// until |r/diag|_inf <= tol * |u|_inf, and finally writes the face electric
+// field used by the particle kernel.  When the grid cannot be coarsened the
+// inner solve is red-black SOR.  A single block (barrier = __syncthreads)
+// serves grids up to a few 1e4 nodes; larger grids run the same code on many
+// blocks under a cooperative launch with a bounded grid barrier.
+#include <cooperative_groups.h>
+
+#include "device.hpp"
+#include "kernels.hpp"
+
+namespace mag {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kEps0d = 8.854187817e-12;
+constexpr long long kBarrierSpinLimit = 20000000;  // ~seconds of __nanosleep(64) polling
+
+struct Team {
+    GridBarrier* bar;
+    unsigned nblocks;
+    unsigned tid, nthreads;
+    __device__ Team(GridBarrier* b)
+        : bar(b), nblocks(gridDim.x), tid(blockIdx.x * blockDim.x + threadIdx.x), nthreads(gridDim.x * blockDim.x)
+    {
+    }
+    // returns false when the grid barrier gave up (the kernel then returns)
+    __device__ bool sync()
+    {
+        __syncthreads();
+        if (nblocks == 1) return true;
+        __shared__ int s_ok;
+        if (threadIdx.x == 0) {
+            volatile unsigned* genp = &bar->gen;
+            const unsigned g = *genp;
+            __threadfence();
+            const unsigned arrived = atomicAdd(&bar->count, 1u);
+            int ok = 1;
+            if (arrived == nblocks - 1) {
+                atomicExch(&bar->count, 0u);
+                __threadfence();
+                atomicAdd(&bar->gen, 1u);
+            } else {
+                long long spins = 0;
+                while (*genp == g) {
+                    if (++spins > kBarrierSpinLimit || *((volatile unsigned*)&bar->abort)) {
+                        atomicExch(&bar->abort, 1u);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+            s_ok = ok && !*((volatile unsigned*)&bar->abort);
+        }
+        __syncthreads();
+        return s_ok;
+    }
+};
+
+__device__ __forceinline__ bool is_fixed(int8_t m) { return m == 0 || m == 1; }
+
+// 5-point row of the fine operator (fields.cpp:149-238) at node (i, j)
+struct Stencil5 {
+    double w, e, s, n, c;
+};
+__device__ __forceinline__ Stencil5 fine_stencil(int coord, int i, double dx, double dz)
+{
+    Stencil5 st;
+    if (coord == 1) {
+        const double k2 = 1.0 / (dz * dz);
+        if (i == 0) {
+            const double k3 = 1.0 / (dx * dx * 0.25);
+            st = {0.0, k3, k2, k2, -2.0 * k2 - k3};
+        } else {
+            const double k1 = (i - 0.5) / (dx * dx * i);
+            const double k3 = (i + 0.5) / (dx * dx * i);
+            st = {k1, k3, k2, k2, -2.0 * k2 - k1 - k3};
+        }
+    } else {
+        st = {1.0, 1.0, 1.0, 1.0, -4.0};
+    }
+    return st;
+}
+
+__device__ __forceinline__ double atomic_max_nonneg(double* p, double v)
+{
+    return __longlong_as_double(
+        (long long)atomicMax((unsigned long long*)p, (unsigned long long)__double_as_longlong(v)));
+}
+
+template <class T>
+__device__ T block_max(T v)
+{
+    __shared__ T s[32];
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) s[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = l < (int)(blockDim.x >> 5) ? s[l] : T(0);
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (l == 0) s[0] = v;
+    }
+    __syncthreads();
+    const T r = s[0];
+    __syncthreads();
+    return r;
+}
+
+// ---- FP32 multigrid pieces -------------------------------------------------
+
+// red-black Gauss-Seidel (or SOR) sweeps on the fine level
+__device__ void smooth_fine(const SolveArgs& a, Team& t, int sweeps, bool reverse, float omega, bool& ok)
+{
+    const MGLevelDev& L = a.lev[0];
+    const int nx = L.nx, nz = L.nz, hz = (nz + 1) / 2;
+    for (int s = 0; s < sweeps && ok; ++s)
+        for (int cc = 0; cc < 2 && ok; ++cc) {
+            const int color = reverse ? 1 - cc : cc;
+            for (unsigned q = t.tid; q < (unsigned)(nx * hz); q += t.nthreads) {
+                const int i = q / hz;
+                const int j = 2 * (q % hz) + ((i + color) & 1);
+                if (j >= nz) continue;
+                const size_t k = (size_t)i * nz + j;
+                if (is_fixed(a.mask[k])) continue;
+                const Stencil5 st = fine_stencil(a.coord, i, a.dx, a.dz);
+                float acc = L.r[k];
+                if (i > 0) acc -= (float)st.w * L.e[k - nz];
+                acc -= (float)st.e * L.e[k + nz];
+                acc -= (float)st.s * L.e[k - 1];
+                acc -= (float)st.n * L.e[k + 1];
+                const float enew = acc / (float)st.c;
+                L.e[k] = omega == 1.f ? enew : L.e[k] + omega * (enew - L.e[k]);
+            }
+            ok = t.sync();
+        }
+}
+
+__device__ __forceinline__ float coarse_apply(const MGLevelDev& L, int i, int j, size_t k, const float* e, bool skip_center)
+{
+    const int nx = L.nx, nz = L.nz;
+    const size_t n = (size_t)nx * nz;
+    float acc = 0.f;
+#pragma unroll
+    for (int di = -1; di <= 1; ++di) {
+        if (i + di < 0 || i + di >= nx) continue;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+            if (j + dj < 0 || j + dj >= nz) continue;
+            if (skip_center && di == 0 && dj == 0) continue;
+            const int p = (di + 1) * 3 + (dj + 1);
+            acc += L.coef[p * n + k] * e[k + (ptrdiff_t)di * nz + dj];
+        }
+    }
+    return acc;
+}
+
+// 4-colour Gauss-Seidel on a Galerkin level (9-point stencil)
+__device__ void smooth_coarse(const SolveArgs& a, Team& t, int l, int sweeps, bool reverse, bool& ok)
+{
+    const MGLevelDev& L = a.lev[l];
+    const int nx = L.nx, nz = L.nz;
+    const int hx = (nx + 1) / 2, hz = (nz + 1) / 2;
+    for (int s = 0; s < sweeps && ok; ++s)
+        for (int cc = 0; cc < 4 && ok; ++cc) {
+            const int color = reverse ? 3 - cc : cc;
+            const int ci = color >> 1, cj = color & 1;
+            for (unsigned q = t.tid; q < (unsigned)(hx * hz); q += t.nthreads) {
+                const int i = 2 * (q / hz) + ci, j = 2 * (q % hz) + cj;
+                if (i >= nx || j >= nz) continue;
+                const size_t k = (size_t)i * nz + j;
+                const float off = coarse_apply(L, i, j, k, L.e, true);
+                L.e[k] = (L.r[k] - off) * L.inv_diag[k];
+            }
+            ok = t.sync();
+        }
+}
+
+// t = r - A e on level l (fine level: free nodes only)
+__device__ void residual_level(const SolveArgs& a, Team& t, int l, float* out)
+{
+    const MGLevelDev& L = a.lev[l];
+    const int nx = L.nx, nz = L.nz;
+    for (unsigned q = t.tid; q < (unsigned)(nx * nz); q += t.nthreads) {
+        const int i = q / nz, j = q % nz;
+        const size_t k = q;
+        if (l == 0) {
+            if (is_fixed(a.mask[k])) {
+                out[k] = 0.f;
+                continue;
+            }
+            const Stencil5 st = fine_stencil(a.coord, i, a.dx, a.dz);
+            float acc = L.r[k] - (float)st.c * L.e[k];
+            if (i > 0) acc -= (float)st.w * L.e[k - nz];
+            acc -= (float)st.e * L.e[k + nz];
+            acc -= (float)st.s * L.e[k - 1];
+            acc -= (float)st.n * L.e[k + 1];
+            out[k] = acc;
+        } else {
+            out[k] = L.r[k] - coarse_apply(L, i, j, k, L.e, false);
+        }
+    }
+}
+
+// r_{l+1} = P^T t_l (weights 1, 1/2, 1/4; fixed fine nodes carry no residual); e_{l+1} = 0
+__device__ void restrict_level(const SolveArgs& a, Team& t, int l, const float* tl)
+{
+    const MGLevelDev& F = a.lev[l];
+    const MGLevelDev& C = a.lev[l + 1];
+    for (unsigned q = t.tid; q < (unsigned)(C.nx * C.nz); q += t.nthreads) {
+        const int I = q / C.nz, J = q % C.nz;
+        float acc = 0.f;
+#pragma unroll
+        for (int di = -1; di <= 1; ++di) {
+            const int i = 2 * I + di;
+            if (i < 0 || i >= F.nx) continue;
+            const float wi = di == 0 ? 1.f : 0.5f;
+#pragma unroll
+            for (int dj = -1; dj <= 1; ++dj) {
+                const int j = 2 * J + dj;
+                if (j < 0 || j >= F.nz) continue;
+                const float wj = dj == 0 ? 1.f : 0.5f;
+                acc += wi * wj * tl[(size_t)i * F.nz + j];
+            }
+        }
+        C.r[q] = acc;
+        C.e[q] = 0.f;
+    }
+}
+
+// e_l += P e_{l+1} (bilinear; fixed fine nodes untouched)
+__device__ void prolong_level(const SolveArgs& a, Team& t, int l)
+{
+    const MGLevelDev& F = a.lev[l];
+    const MGLevelDev& C = a.lev[l + 1];
+    for (unsigned q = t.tid; q < (unsigned)(F.nx * F.nz); q += t.nthreads) {
+        if (l == 0 && is_fixed(a.mask[q])) continue;
+        const int i = q / F.nz, j = q % F.nz;
+        const int I0 = i >> 1, J0 = j >> 1;
+        const bool oi = i & 1, oj = j & 1;
+        const float* ec = C.e;
+        const size_t b = (size_t)I0 * C.nz + J0;
+        float v;
+        if (!oi && !oj) v = ec[b];
+        else if (oi && !oj) v = 0.5f * (ec[b] + ec[b + C.nz]);
+        else if (!oi && oj) v = 0.5f * (ec[b] + ec[b + 1]);
+        else v = 0.25f * (ec[b] + ec[b + C.nz] + ec[b + 1] + ec[b + C.nz + 1]);
+        F.e[q] += v;
+    }
+}
+
+__device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
+{
+    const int L = a.nlev;
+    if (L == 1) {
+        smooth_fine(a, t, a.ncoarse, false, a.omega, ok);
+        return;
+    }
+    for (int l = 0; l < L - 1 && ok; ++l) {
+        if (l == 0) smooth_fine(a, t, a.nu1, false, 1.f, ok);
+        else smooth_coarse(a, t, l, a.nu1, false, ok);
+        if (!ok) return;
+        residual_level(a, t, l, a.lev[l].t);
+        ok = t.sync();
+        if (!ok) return;
+        restrict_level(a, t, l, a.lev[l].t);
+        ok = t.sync();
+    }
+    if (!ok) return;
+    smooth_coarse(a, t, L - 1, a.ncoarse, false, ok);
+    for (int l = L - 2; l >= 0 && ok; --l) {
+        prolong_level(a, t, l);
+        ok = t.sync();
+        if (!ok) return;
+        if (l == 0) smooth_fine(a, t, a.nu2, true, 1.f, ok);
+        else smooth_coarse(a, t, l, a.nu2, true, ok);
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_solve(const SolveArgs a)
+{
+    Team t(a.bar);
+    const int nx = a.nx, nz = a.nz;
+    const unsigned nn = (unsigned)(nx * nz);
+    bool ok = true;
+    // 1. right-hand side and Dirichlet values (boundary_solve / boundary_solve_rf)
+    for (unsigned k = t.tid; k < nn; k += t.nthreads) {
+        const int i = k / nz;
+        const int8_t m = a.mask[k];
+        if (is_fixed(m)) {
+            const double v = a.rf_solve ? (m == 1 ? a.voltage[k] : 0.0) : (m == 0 ? a.voltage[k] : 0.0);
+            a.u[k] = v;
+            a.b[k] = v;
+        } else {
+            double rho = 0.0;
+            if (a.rho_src == 1) {
+                for (int s = 0; s < a.nsp; ++s) rho += a.rho_weight[s] * (double)a.rho_fixed[s][k];
+            } else if (a.rho_src == 2) {
+                rho = a.rho64[k];
+            }
+            double scale;
+            if (a.coord == 1)
+                scale = i > 0 ? -1.0 / kEps0d / (kPi * a.dx * a.dx * 2.0 * i * a.dz) * a.mpf
+                              : -1.0 / kEps0d / (kPi * a.dx * a.dx * 0.25 * a.dz) * a.mpf;
+            else
+                scale = -(a.dx * a.dx) / kEps0d / a.dV;
+            a.b[k] = rho * scale;
+        }
+        if (a.clear_rho && a.rho_src == 1)
+            for (int s = 0; s < a.nsp; ++s) ((unsigned long long*)a.rho_fixed[s])[k] = 0ull;
+    }
+    ok = t.sync();
+    // 2. FP64 residual refinement around the FP32 multigrid
+    int it = 0;
+    double res = 0.0;
+    bool conv = false;
+    const MGLevelDev& F = a.lev[0];
+    for (; ok; ++it) {
+        double lres = 0.0, lumax = 0.0;
+        for (unsigned k = t.tid; k < nn; k += t.nthreads) {
+            const int i = k / nz;
+            lumax = fmax(lumax, fabs(a.u[k]));
+            F.e[k] = 0.f;
+            if (is_fixed(a.mask[k])) {
+                F.r[k] = 0.f;
+                continue;
+            }
+            const Stencil5 st = fine_stencil(a.coord, i, a.dx, a.dz);
+            double acc = st.c * a.u[k];
+            if (i > 0) acc += st.w * a.u[k - nz];
+            acc += st.e * a.u[k + nz];
+            acc += st.s * a.u[k - 1];
+            acc += st.n * a.u[k + 1];
+            const double r = a.b[k] - acc;
+            F.r[k] = (float)r;
+            lres = fmax(lres, fabs(r / st.c));
+        }
+        lres = block_max(lres);
+        lumax = block_max(lumax);
+        if (t.nblocks > 1) {
+            const int slot = (it & 1) * 2;
+            if (threadIdx.x == 0) {
+                atomic_max_nonneg(&a.red[slot], lres);
+                atomic_max_nonneg(&a.red[slot + 1], lumax);
+            }
+            ok = t.sync();
+            if (!ok) break;
+            lres = *((volatile double*)&a.red[slot]);
+            lumax = *((volatile double*)&a.red[slot + 1]);
+            if (t.tid == 0) {
+                a.red[2 - slot] = 0.0;
+                a.red[3 - slot] = 0.0;
+            }
+        }
+        res = lumax > 0.0 ? lres / lumax : lres;
+        if (res <= a.tol || lres == 0.0) {
+            conv = true;
+            break;
+        }
+        if (it >= a.max_outer) break;
+        ok = t.sync();
+        if (!ok) break;
+        vcycle(a, t, ok);
+        if (!ok) break;
+        for (unsigned k = t.tid; k < nn; k += t.nthreads)
+            if (!is_fixed(a.mask[k])) a.u[k] += (double)F.e[k];
+        ok = t.sync();
+    }
+    // 3. face electric field E = -grad u for the particle kernel
+    if (ok && a.Exf != nullptr) {
+        const double idx = 1.0 / a.dx, idz = 1.0 / a.dz;
+        for (unsigned q = t.tid; q < (unsigned)((nx + 1) * nz); q += t.nthreads) {
+            int i = q / nz;
+            const int j = q % nz;
+            i = i < 1 ? 1 : (i > nx - 1 ? nx - 1 : i);
+            a.Exf[q] = (float)(-(a.u[(size_t)i * nz + j] - a.u[(size_t)(i - 1) * nz + j]) * idx);
+        }
+        for (unsigned q = t.tid; q < (unsigned)(nx * (nz + 1)); q += t.nthreads) {
+            const int i = q / (nz + 1);
+            int j = q % (nz + 1);
+            j = j < 1 ? 1 : (j > nz - 1 ? nz - 1 : j);
+            a.Ezf[q] = (float)(-(a.u[(size_t)i * nz + j] - a.u[(size_t)i * nz + j - 1]) * idz);
+        }
+    }
+    if (t.tid == 0) {
+        a.status->iterations = it;
+        a.status->residual = res;
+        a.status->converged = conv ? 1 : 0;
+        a.status->aborted = ok ? 0 : 1;
+        if (!ok) atomicCAS(a.err, 0, -5);
+        else if (!conv) atomicCAS(a.err, 0, -4);
+    }
+}
+
+__global__ void k_faces(const double* __restrict__ u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf)
+{
+    const double idx = 1.0 / dx, idz = 1.0 / dz;
+    const unsigned n1 = (unsigned)((nx + 1) * nz), n2 = (unsigned)(nx * (nz + 1));
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n1 + n2; q += gridDim.x * blockDim.x) {
+        if (q < n1) {
+            int i = q / nz;
+            const int j = q % nz;
+            i = i < 1 ? 1 : (i > nx - 1 ? nx - 1 : i);
+            Exf[q] = (float)(-(u[(size_t)i * nz + j] - u[(size_t)(i - 1) * nz + j]) * idx);
+        } else {
+            const unsigned p = q - n1;
+            const int i = p / (nz + 1);
+            int j = p % (nz + 1);
+            j = j < 1 ? 1 : (j > nz - 1 ? nz - 1 : j);
+            Ezf[p] = (float)(-(u[(size_t)i * nz + j] - u[(size_t)i * nz + j - 1]) * idz);
+        }
+    }
+}
+
+}  // namespace
+
+int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s)
+{
+    if (nblocks <= 1) {
+        k_solve<<<1, 1024, 0, s>>>(a);
+    } else {
+        void* args[] = {(void*)&a};
+        cudaLaunchCooperativeKernel((const void*)k_solve, dim3(nblocks), dim3(1024), args, 0, s);
+    }
+    return 1;
+}
+
+int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s)
+{
+    const long long n = (long long)(nx + 1) * nz + (long long)nx * (nz + 1);
+    const int grid = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+    k_faces<<<grid, 256, 0, s>>>(u, nx, nz, dx, dz, Exf, Ezf);
+    return 1;
+}
+
+}  // namespace mag

@@ -1,0 +1,921 @@
+// Host orchestration of the GPU PIC-MCC step.
+#include "sim.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+#include "kernels.hpp"
+
+namespace mag {
+
+void check_cuda(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw Error(-2, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+bool fixed_node(int8_t m) { return m == FIXED || m == FIXED_RF; }
+
+// 9-point operator planes: plane (di+1)*3 + (dj+1) holds the coefficient of node (i+di, j+dj)
+inline int plane(int di, int dj) { return (di + 1) * 3 + (dj + 1); }
+
+// Fine-level operator of the correction equation: the reference's rows
+// (src/fields.cpp:149-238) on free nodes with the columns of Dirichlet nodes
+// removed; Dirichlet rows are identity.
+void fine_operator(int coord, int nx, int nz, double dx, double dz, const std::vector<int8_t>& mask,
+                   std::vector<double>& A)
+{
+    const size_t n = (size_t)nx * nz;
+    A.assign(9 * n, 0.0);
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) {
+            const size_t k = (size_t)i * nz + j;
+            if (fixed_node(mask[k])) {
+                A[4 * n + k] = 1.0;
+                continue;
+            }
+            double w, e, s, nn, c;
+            if (coord == CYLINDRICAL) {
+                const double k2 = 1.0 / (dz * dz);
+                if (i == 0) {
+                    const double k3 = 1.0 / (dx * dx * 0.25);
+                    w = 0.0; e = k3; s = k2; nn = k2; c = -2.0 * k2 - k3;
+                } else {
+                    const double k1 = (i - 0.5) / (dx * dx * i), k3 = (i + 0.5) / (dx * dx * i);
+                    w = k1; e = k3; s = k2; nn = k2; c = -2.0 * k2 - k1 - k3;
+                }
+            } else {
+                w = e = s = nn = 1.0;
+                c = -4.0;
+            }
+            A[4 * n + k] = c;
+            if (i > 0 && !fixed_node(mask[k - nz])) A[(size_t)plane(-1, 0) * n + k] = w;
+            if (i < nx - 1 && !fixed_node(mask[k + nz])) A[(size_t)plane(1, 0) * n + k] = e;
+            if (j > 0 && !fixed_node(mask[k - 1])) A[(size_t)plane(0, -1) * n + k] = s;
+            if (j < nz - 1 && !fixed_node(mask[k + 1])) A[(size_t)plane(0, 1) * n + k] = nn;
+        }
+}
+
+// Galerkin coarse operator Ac = P^T Af P with bilinear P (rows of fixed fine
+// nodes are zero).  Coarse rows left without a diagonal become identity.
+void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int& nxc,
+              int& nzc, std::vector<double>& Ac)
+{
+    nxc = (nxf - 1) / 2 + 1;
+    nzc = (nzf - 1) / 2 + 1;
+    const size_t nf = (size_t)nxf * nzf, nc = (size_t)nxc * nzc;
+    Ac.assign(9 * nc, 0.0);
+    auto pw = [](int a) { return a == 0 ? 1.0 : 0.5; };
+    for (int J0 = 0; J0 < nxc; ++J0)
+        for (int J1 = 0; J1 < nzc; ++J1) {
+            double v[3][3] = {{0}};
+            for (int a = -1; a <= 1; ++a)
+                for (int b = -1; b <= 1; ++b) {
+                    const int i = 2 * J0 + a, j = 2 * J1 + b;
+                    if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
+                    if (fixed_f[(size_t)i * nzf + j]) continue;
+                    v[a + 1][b + 1] = pw(a) * pw(b);
+                }
+            double w[5][5] = {{0}};
+            for (int a = -2; a <= 2; ++a)
+                for (int b = -2; b <= 2; ++b) {
+                    const int i = 2 * J0 + a, j = 2 * J1 + b;
+                    if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
+                    const size_t f = (size_t)i * nzf + j;
+                    double acc = 0.0;
+                    for (int di = -1; di <= 1; ++di)
+                        for (int dj = -1; dj <= 1; ++dj) {
+                            const int ga = a + di, gb = b + dj;
+                            if (ga < -1 || ga > 1 || gb < -1 || gb > 1) continue;
+                            const double vv = v[ga + 1][gb + 1];
+                            if (vv == 0.0) continue;
+                            acc += Af[(size_t)plane(di, dj) * nf + f] * vv;
+                        }
+                    w[a + 2][b + 2] = acc;
+                }
+            for (int I0 = J0 - 1; I0 <= J0 + 1; ++I0)
+                for (int I1 = J1 - 1; I1 <= J1 + 1; ++I1) {
+                    if (I0 < 0 || I0 >= nxc || I1 < 0 || I1 >= nzc) continue;
+                    double acc = 0.0;
+                    for (int a = -1; a <= 1; ++a)
+                        for (int b = -1; b <= 1; ++b) {
+                            const int i = 2 * I0 + a, j = 2 * I1 + b;
+                            if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
+                            if (fixed_f[(size_t)i * nzf + j]) continue;
+                            const int wa = i - 2 * J0, wb = j - 2 * J1;
+                            if (wa < -2 || wa > 2 || wb < -2 || wb > 2) continue;
+                            acc += pw(a) * pw(b) * w[wa + 2][wb + 2];
+                        }
+                    Ac[(size_t)plane(J0 - I0, J1 - I1) * nc + (size_t)I0 * nzc + I1] = acc;
+                }
+        }
+    for (size_t k = 0; k < nc; ++k)
+        if (Ac[4 * nc + k] == 0.0) {
+            for (int q = 0; q < 9; ++q) Ac[q * nc + k] = 0.0;
+            Ac[4 * nc + k] = 1.0;
+        }
+}
+
+std::vector<std::string> tokens(const std::string& line)
+{
+    std::istringstream is(line);
+    std::vector<std::string> t;
+    for (std::string s; is >> s;) t.push_back(s);
+    return t;
+}
+
+double to_num(const std::string& s)
+{
+    std::istringstream is(s);
+    double v;
+    if (!(is >> v)) throw Error(-1, "string2: error converting string " + s + " to T");
+    return v;
+}
+
+int to_int(const std::string& s)
+{
+    std::istringstream is(s);
+    int v;
+    if (!(is >> v)) throw Error(-1, "string2: error converting string " + s + " to T");
+    return v;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+Sim::Sim(const std::string& config, const std::string& species_conf, const SimOptions& opts)
+{
+    device = opts.device;
+    seed = opts.seed;
+    poisson_tol = opts.poisson_tol > 0 ? opts.poisson_tol : 1e-12;
+    poisson_max_iter = opts.poisson_max_iter > 0 ? opts.poisson_max_iter : 200;
+    p = make_param(KeyValueConfig::from_file(config));
+    if (p.mover != ADVANCE_BORIS)
+        throw Error(-1, "mover ADVANCE_MULTICOLL is not provided by this library (Boris mover only)");
+    if (p.use_source) throw Error(-1, "use_source: particle sources are not provided by this library");
+    if (p.u_smooth) throw Error(-1, "u_smooth: potential smoothing is not provided by this library");
+    parse_species_conf(species_conf, species_prm, inters);
+    if (species_prm.empty()) throw Error(-1, "species_conf defines no species");
+    if ((int)species_prm.size() > kMaxSpecies) throw Error(-1, "too many species");
+    if ((int)inters.size() > kMaxInteractions) throw Error(-1, "too many interactions");
+    build_geometry(p, mask, voltage);
+    MAG_CK(cudaSetDevice(device));
+    MAG_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    d_err.alloc(1);
+    d_err.zero(stream);
+    d_status.alloc(1);
+    d_status.zero(stream);
+    d_bar.alloc(1);
+    d_bar.zero(stream);
+    red.alloc(4);
+    red.zero(stream);
+    setup_fields();
+    setup_species();
+    if (opts.capacity_hint > 0)
+        for (size_t s = 0; s < sp.size(); ++s) ensure_capacity((int)s, opts.capacity_hint);
+    MAG_CK(cudaStreamSynchronize(stream));
+    int e = sync();
+    if (e != 0) throw Error(e, "initial field solve failed (device status " + std::to_string(e) + ")");
+}
+
+Sim::~Sim()
+{
+    if (stream) {
+        cudaSetDevice(device);
+        cudaStreamSynchronize(stream);
+        sp.clear();
+        lv = SolverLevels{};
+        cudaStreamDestroy(stream);
+    }
+}
+
+int Sim::sync()
+{
+    MAG_CK(cudaStreamSynchronize(stream));
+    int err = 0;
+    MAG_CK(cudaMemcpy(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    MAG_CK(cudaMemcpy(&last_solve, d_status.p, sizeof(SolveStatus), cudaMemcpyDeviceToHost));
+    for (auto& s : sp) {
+        if (!s.cnt.p) continue;
+        Counters c;
+        MAG_CK(cudaMemcpy(&c, s.cnt.p, sizeof c, cudaMemcpyDeviceToHost));
+        if (c.error && !err) err = c.error;
+    }
+    if (err) {
+        int zero = 0;
+        MAG_CK(cudaMemcpy(d_err.p, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    }
+    return err;
+}
+
+// Fields: geometry, loaded or solved u and uRF, magnetic tables (pic.cpp:127-189)
+void Sim::setup_fields()
+{
+    if (p.electric_field_from_file) {
+        LoadedField u = load_field_table(p.electric_field_static_file);
+        nx = u.nx;
+        nz = u.nz;
+        dx = u.dx;
+        dz = u.dz;
+        x0 = u.xmin;
+        z0 = u.zmin;
+        xmax = x0 + (nx - 1) * dx;
+        zmax = z0 + (nz - 1) * dz;
+        u64.upload(u.v.data(), u.v.size(), stream);
+        urf64.alloc(u.v.size());
+        urf64.zero(stream);
+        if (p.rf) {
+            LoadedField r = load_field_table(p.electric_field_rf_file);
+            if (r.nx != nx || r.nz != nz || r.dx != dx || r.dz != dz || r.xmin != x0 || r.zmin != z0)
+                throw Error(-1, "electric_field_rf_file grid differs from electric_field_static_file grid");
+            urf64.upload(r.v.data(), r.v.size(), stream);
+        }
+        check_mask = false;  // advance_boundary skips is_free in this mode (particles.hpp:395)
+    } else {
+        nx = p.x_sampl;
+        nz = p.z_sampl;
+        dx = p.dx;
+        dz = p.dz;
+        x0 = 0;
+        z0 = 0;
+        xmax = p.x_max;
+        zmax = p.z_max;
+        u64.alloc((size_t)nx * nz);
+        u64.zero(stream);
+        urf64.alloc((size_t)nx * nz);
+        urf64.zero(stream);
+        check_mask = true;
+    }
+    const size_t nn = (size_t)nx * nz;
+    b64.alloc(std::max(nn, mask.size()));
+    rho64.alloc(nn);
+    rho64.zero(stream);
+    Exf.alloc((size_t)(nx + 1) * nz);
+    Ezf.alloc((size_t)nx * (nz + 1));
+    Exf_rf.alloc((size_t)(nx + 1) * nz);
+    Ezf_rf.alloc((size_t)nx * (nz + 1));
+    d_mask.upload(mask.data(), mask.size(), stream);
+    d_volt.upload(voltage.data(), voltage.size(), stream);
+    if (p.geometry == GEO_EMPTY && !p.selfconsistent) emode = 0;
+    else emode = p.rf ? 2 : 1;
+    if (!p.magnetic_field_const) {
+        std::vector<double> bz;
+        LoadedField br = load_field_table(p.magnetic_field_file, 2, &bz);
+        std::vector<float> f1(br.v.begin(), br.v.end()), f2(bz.begin(), bz.end());
+        d_Br.upload(f1.data(), f1.size(), stream);
+        d_Bz.upload(f2.data(), f2.size(), stream);
+        bnx = br.nx;
+        bnz = br.nz;
+        b_x0 = br.xmin;
+        b_z0 = br.zmin;
+        b_dx = br.dx;
+        b_dz = br.dz;
+    }
+    if (p.electric_field_from_file) {
+        launches += launch_faces(u64.p, nx, nz, dx, dz, Exf.p, Ezf.p, stream);
+        launches += launch_faces(urf64.p, nx, nz, dx, dz, Exf_rf.p, Ezf_rf.p, stream);
+    } else {
+        // Pic constructor: boundary_solve_rf always, boundary_solve when not self-consistent
+        setup_solver();
+        solve(true, 0, false, false);
+        if (!p.selfconsistent) solve(false, 0, false, false);
+        else launches += launch_faces(u64.p, nx, nz, dx, dz, Exf.p, Ezf.p, stream);
+    }
+}
+
+void Sim::validate_operator() const
+{
+    for (int i = 0; i < p.x_sampl; ++i)
+        for (int j = 0; j < p.z_sampl; ++j) {
+            if (fixed_node(mask[(size_t)i * p.z_sampl + j])) continue;
+            const bool axis_ok = p.coord == CYLINDRICAL && i == 0;
+            if ((i == 0 && !axis_ok) || i == p.x_sampl - 1 || j == 0 || j == p.z_sampl - 1)
+                throw Error(-1, "geometry leaves a free node on the domain edge at (" + std::to_string(i) + "," +
+                                    std::to_string(j) + "); the reference operator (fields.cpp:136-259) is undefined there");
+        }
+}
+
+void Sim::setup_solver()
+{
+    if (solver_ready) return;
+    validate_operator();
+    const int coord = p.coord == CYLINDRICAL ? 1 : 0;
+    std::vector<int> lnx{nx}, lnz{nz};
+    while (lnx.size() < (size_t)kMaxLevels && (lnx.back() - 1) % 2 == 0 && (lnz.back() - 1) % 2 == 0 &&
+           lnx.back() >= 5 && lnz.back() >= 5) {
+        lnx.push_back((lnx.back() - 1) / 2 + 1);
+        lnz.push_back((lnz.back() - 1) / 2 + 1);
+    }
+    lv.nlev = (int)lnx.size();
+    lv.nx = lnx;
+    lv.nz = lnz;
+    lv.e.resize(lv.nlev);
+    lv.r.resize(lv.nlev);
+    lv.t.resize(lv.nlev);
+    lv.coef.resize(lv.nlev);
+    lv.inv_diag.resize(lv.nlev);
+    std::vector<double> A, Ac;
+    fine_operator(coord, nx, nz, dx, dz, mask, A);
+    std::vector<char> fixed_f(mask.size());
+    for (size_t k = 0; k < mask.size(); ++k) fixed_f[k] = fixed_node(mask[k]);
+    for (int l = 0; l < lv.nlev; ++l) {
+        const size_t n = (size_t)lnx[l] * lnz[l];
+        lv.e[l].alloc(n);
+        lv.r[l].alloc(n);
+        lv.t[l].alloc(n);
+        lv.e[l].zero(stream);
+        if (l == 0) continue;
+        int cx, cz;
+        galerkin(lnx[l - 1], lnz[l - 1], A, fixed_f, cx, cz, Ac);
+        std::vector<float> cf(Ac.begin(), Ac.end()), idg(n);
+        for (size_t k = 0; k < n; ++k) idg[k] = (float)(1.0 / Ac[4 * n + k]);
+        lv.coef[l].upload(cf.data(), cf.size(), stream);
+        lv.inv_diag[l].upload(idg.data(), idg.size(), stream);
+        MAG_CK(cudaStreamSynchronize(stream));
+        A.swap(Ac);
+        fixed_f.assign(n, 0);
+    }
+    solver_ready = true;
+}
+
+SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
+{
+    setup_solver();
+    SolveArgs a{};
+    a.coord = p.coord == CYLINDRICAL ? 1 : 0;
+    a.nx = nx;
+    a.nz = nz;
+    a.dx = dx;
+    a.dz = dz;
+    a.mask = d_mask.p;
+    a.voltage = d_volt.p;
+    a.u = rf_solve ? urf64.p : u64.p;
+    a.b = b64.p;
+    a.rf_solve = rf_solve ? 1 : 0;
+    a.rho_src = rho_src;
+    a.nsp = (int)sp.size();
+    for (size_t s = 0; s < sp.size(); ++s) {
+        a.rho_fixed[s] = sp[s].rho.p;
+        a.rho_weight[s] = sp[s].prm.charge * std::ldexp(1.0, -2 * kDepositShift);
+    }
+    a.rho64 = rho64.p;
+    a.clear_rho = clear_rho ? 1 : 0;
+    a.mpf = p.macroparticle_factor;
+    a.dV = p.dV;
+    a.nlev = lv.nlev;
+    for (int l = 0; l < lv.nlev; ++l) {
+        a.lev[l].nx = lv.nx[l];
+        a.lev[l].nz = lv.nz[l];
+        a.lev[l].e = lv.e[l].p;
+        a.lev[l].r = lv.r[l].p;
+        a.lev[l].t = lv.t[l].p;
+        a.lev[l].coef = lv.coef[l].p;
+        a.lev[l].inv_diag = lv.inv_diag[l].p;
+    }
+    a.nu1 = 2;
+    a.nu2 = 2;
+    a.ncoarse = lv.nlev == 1 ? 20 : 40;
+    a.omega = lv.nlev == 1 ? (float)(2.0 / (1.0 + std::sin(kPi / std::max(nx, nz)))) : 1.f;
+    a.tol = poisson_tol;
+    a.max_outer = lv.nlev == 1 ? 20 * poisson_max_iter : poisson_max_iter;
+    a.Exf = rf_solve ? Exf_rf.p : Exf.p;
+    a.Ezf = rf_solve ? Ezf_rf.p : Ezf.p;
+    a.red = red.p;
+    a.bar = d_bar.p;
+    a.status = d_status.p;
+    a.err = d_err.p;
+    const int nblocks = (size_t)nx * nz <= 70000 ? 1 : 1;  // multi-block path enabled once validated on the GPU
+    launches += launch_solve(a, nblocks, stream);
+    MAG_CK(cudaGetLastError());
+    SolveStatus st{};
+    if (wait) {
+        MAG_CK(cudaStreamSynchronize(stream));
+        MAG_CK(cudaMemcpy(&st, d_status.p, sizeof st, cudaMemcpyDeviceToHost));
+        last_solve = st;
+    }
+    return st;
+}
+
+// Speclist (pic.cpp:27-80) and lifetime_init (particles.cpp:142-206)
+void Sim::setup_species()
+{
+    const int ns = (int)species_prm.size();
+    sp.resize(ns);
+    std::map<std::string, int> idx;
+    for (int s = 0; s < ns; ++s) idx[species_prm[s].name] = s;
+    for (int s = 0; s < ns; ++s) {
+        SpeciesState& S = sp[s];
+        S.prm = species_prm[s];
+        S.E_max = S.prm.E_max > 0. ? S.prm.E_max : S.prm.temperature * kKB / kQe * 10.0;
+        S.v_max = std::sqrt(2.0 * kKB * S.prm.temperature / S.prm.mass);
+        S.by_target.assign(ns, {});
+        S.rates.assign(ns, 0.0);
+        S.cnt.alloc(1);
+        S.cnt.zero(stream);
+        S.rho.alloc((size_t)nx * nz);
+        S.rho.zero(stream);
+    }
+    std::vector<InterDev> idev;
+    std::vector<double> tab;
+    const std::vector<InteractionParams> raw_inters = inters;
+    for (size_t q = 0; q < inters.size(); ++q) {
+        const InteractionParams& in = inters[q];
+        auto pi = idx.find(in.primary), si = idx.find(in.secondary);
+        if (pi == idx.end())
+            throw Error(-1, "Speclist::Speclist: unrecognized primary species \"" + in.primary + "\" of interaction \"" +
+                                in.name + "\"");
+        if (si == idx.end())
+            throw Error(-1, "Speclist::Speclist: unrecognized primary species \"" + in.secondary +
+                                "\" of interaction \"" + in.name + "\"");
+        sp[pi->second].by_target[si->second].push_back((int)q);
+        if (in.type == LANGEVIN) inters[q].rate *= in.cutoff * in.cutoff;  // particles.hpp:81-82
+    }
+    for (int s = 0; s < ns; ++s) {
+        SpeciesState& S = sp[s];
+        species_rates(species_prm, raw_inters, s, S.rates, S.lifetime);
+        S.prob = 1.0 - std::exp(-S.prm.dt / S.lifetime);
+        const double th = S.prob * 4294967296.0;
+        S.threshold = S.prob <= 0.0 ? 0u : (th >= 4294967295.0 ? 0xffffffffu : (uint32_t)std::max(1.0, th));
+    }
+    // device interaction list grouped per primary species, then per target,
+    // in the order of the species_conf file (interactions_by_species)
+    auto make_dev = [&](int q) {
+        const InteractionParams& in = inters[q];
+        const int pr = idx[in.primary], se = idx[in.secondary];
+        InterDev d{};
+        d.type = in.type;
+        d.target = se;
+        d.DE = in.DE * kQe;
+        d.rate = in.rate;
+        d.cutoff = in.cutoff;
+        const double m1 = species_prm[pr].mass, m2 = species_prm[se].mass;
+        d.mu = m1 * m2 / (m1 + m2);
+        d.tab_off = (int)tab.size();
+        d.tab_n = (int)in.CS_energy.size();
+        tab.insert(tab.end(), in.CS_energy.begin(), in.CS_energy.end());
+        tab.insert(tab.end(), in.CS_value.begin(), in.CS_value.end());
+        const SpeciesParams& P = species_prm[pr];
+        d.coul_lambda_D = std::sqrt(kEps0 * kKB * P.temperature / (P.density * P.charge * P.charge));
+        d.coul_q1q2 = P.charge * species_prm[se].charge;
+        return d;
+    };
+    for (int s = 0; s < ns; ++s) {
+        sp[s].inter_off = (int)idev.size();
+        for (int t = 0; t < ns; ++t)
+            for (int q : sp[s].by_target[t]) idev.push_back(make_dev(q));
+    }
+    if (idev.empty()) idev.push_back(InterDev{});
+    if (tab.empty()) tab.push_back(0.0);
+    d_inter.upload(idev.data(), idev.size(), stream);
+    d_tables.upload(tab.data(), tab.size(), stream);
+}
+
+void Sim::ensure_capacity(int s, int64_t need)
+{
+    SpeciesState& S = sp[s];
+    if (need <= S.cap) return;
+    int64_t cap = std::max<int64_t>(need, (int64_t)(S.cap * 1.5) + 1024);
+    auto grow_f = [&](DevArray<float>& a) {
+        DevArray<float> b;
+        b.alloc(cap);
+        if (S.n_slots) MAG_CK(cudaMemcpyAsync(b.p, a.p, S.n_slots * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+        MAG_CK(cudaStreamSynchronize(stream));
+        a = std::move(b);
+    };
+    grow_f(S.x);
+    grow_f(S.z);
+    grow_f(S.vx);
+    grow_f(S.vy);
+    grow_f(S.vz);
+    DevArray<uint32_t> nid;
+    nid.alloc(cap);
+    if (S.n_slots) MAG_CK(cudaMemcpyAsync(nid.p, S.id.p, S.n_slots * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+    MAG_CK(cudaStreamSynchronize(stream));
+    S.id = std::move(nid);
+    S.cand.alloc(cap);
+    S.cap = cap;
+}
+
+void Sim::add_loaded(int s, int64_t n, int kind, double cx, double cz, double radius, double zlo, double zhi)
+{
+    if (n <= 0) return;
+    SpeciesState& S = sp[s];
+    if (S.n_slots == 0 && S.host_niter) MAG_CK(cudaMemcpyAsync(&S.cnt.p->niter, &S.host_niter, sizeof(uint64_t),
+                                                               cudaMemcpyHostToDevice, stream));
+    ensure_capacity(s, S.n_slots + n);
+    const double vsig = S.v_max * std::sqrt(0.5);
+    const int64_t o = S.n_slots;
+    launches += launch_load_disk(S.x.p + o, S.z.p + o, S.vx.p + o, S.vy.p + o, S.vz.p + o, S.id.p + o, n, S.next_id,
+                                 kind, cx, cz, radius, zlo, zhi, x0, z0, dx, dz, xmax, zmax, vsig, seed,
+                                 (uint32_t)s, p.coord, stream);
+    MAG_CK(cudaGetLastError());
+    S.n_slots += n;
+    S.next_id += (uint32_t)n;
+}
+
+void Sim::add_single(int s, double x, double z, double vx, double vy, double vz)
+{
+    SpeciesState& S = sp[s];
+    ensure_capacity(s, S.n_slots + 1);
+    const int64_t o = S.n_slots;
+    float fx = (float)((x - x0) / dx), fz = (float)((z - z0) / dz);
+    float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
+    uint32_t pid = S.next_id;
+    MAG_CK(cudaMemcpy(S.x.p + o, &fx, 4, cudaMemcpyHostToDevice));
+    MAG_CK(cudaMemcpy(S.z.p + o, &fz, 4, cudaMemcpyHostToDevice));
+    MAG_CK(cudaMemcpy(S.vx.p + o, &fvx, 4, cudaMemcpyHostToDevice));
+    MAG_CK(cudaMemcpy(S.vy.p + o, &fvy, 4, cudaMemcpyHostToDevice));
+    MAG_CK(cudaMemcpy(S.vz.p + o, &fvz, 4, cudaMemcpyHostToDevice));
+    MAG_CK(cudaMemcpy(S.id.p + o, &pid, 4, cudaMemcpyHostToDevice));
+    S.n_slots += 1;
+    S.next_id += 1;
+}
+
+// Pic::run_initscript (src/pic.cpp:241-328) plus one r-z loader
+void Sim::run_initscript(const std::string& path)
+{
+    std::ifstream fr(path);
+    if (!fr) throw Error(-6, "cannot open initscript " + path);
+    std::map<std::string, int> idx;
+    for (size_t s = 0; s < species_prm.size(); ++s) idx[species_prm[s].name] = (int)s;
+    auto species = [&](const std::string& name) {
+        auto it = idx.find(name);
+        if (it == idx.end()) throw Error(-1, "Pic::run_initscript: unrecognized species type \"" + name + "\"");
+        return it->second;
+    };
+    std::string line;
+    while (std::getline(fr, line)) {
+        if (!line.empty() && line[0] == '#') continue;
+        std::vector<std::string> t = tokens(line);
+        if (t.empty()) continue;
+        auto need = [&](size_t k) {
+            if (t.size() != k)
+                throw Error(-1, "Pic::run_initscript: wrong number of parameters (" + std::to_string(t.size()) +
+                                    ") to " + t[0]);
+        };
+        const bool cyl = p.coord == CYLINDRICAL;
+        if (t[0] == "add_particles_bessel" || t[0] == "add_particles_everywhere" || t[0] == "add_particles_on_disk") {
+            if (cyl) throw Error(-1, t[0] + " is not defined for CYLINDRICAL in the reference");
+        }
+        if (t[0] == "add_particles_bessel") {
+            need(6);
+            add_loaded(species(t[1]), to_int(t[2]), 2, to_num(t[3]), to_num(t[4]), to_num(t[5]), 0, 0);
+        } else if (t[0] == "add_particles_everywhere") {
+            need(3);
+            add_loaded(species(t[1]), to_int(t[2]), 1, 0, 0, 0, 0, 0);
+        } else if (t[0] == "add_particles_on_disk") {
+            need(6);
+            add_loaded(species(t[1]), to_int(t[2]), 0, to_num(t[3]), to_num(t[4]), to_num(t[5]), 0, 0);
+        } else if (t[0] == "add_tracked_particle") {
+            need(7);  // particles.hpp:297-309: y and z components are swapped on input
+            add_single(species(t[1]), to_num(t[2]), to_num(t[3]), to_num(t[4]), to_num(t[6]), to_num(t[5]));
+        } else if (t[0] == "add_particles_in_cylinder") {
+            // r-z loader: species n r_max z_min z_max, uniform in volume (r = r_max sqrt(u))
+            need(6);
+            if (!cyl) throw Error(-1, "add_particles_in_cylinder needs coord = CYLINDRICAL");
+            add_loaded(species(t[1]), to_int(t[2]), 3, 0, 0, to_num(t[3]), to_num(t[4]), to_num(t[5]));
+        }
+    }
+    MAG_CK(cudaStreamSynchronize(stream));
+}
+
+PushArgs Sim::push_args(int s, bool init)
+{
+    SpeciesState& S = sp[s];
+    PushArgs a{};
+    a.x = S.x.p;
+    a.z = S.z.p;
+    a.vx = S.vx.p;
+    a.vy = S.vy.p;
+    a.vz = S.vz.p;
+    a.id = S.id.p;
+    a.n = S.n_slots;
+    a.nx = nx;
+    a.nz = nz;
+    a.xmaxg = (float)((xmax - x0) / dx);
+    a.zmaxg = (float)((zmax - z0) / dz);
+    a.periodic = p.boundary == BND_PERIODIC ? 1 : 0;
+    a.check_mask = check_mask ? 1 : 0;
+    a.mask = d_mask.p;
+    a.emode = emode;
+    a.Exf = Exf.p;
+    a.Ezf = Ezf.p;
+    a.Exf_rf = Exf_rf.p;
+    a.Ezf_rf = Ezf_rf.p;
+    a.extern_ez = (float)p.extern_field;
+    a.rf_omega = p.rf_omega;
+    a.rf_amp = p.rf_amplitude;
+    a.rf_U0 = p.rf_U0;
+    a.dt = S.prm.dt;
+    const double q = S.prm.charge, m = S.prm.mass, dt = S.prm.dt;
+    const double rot = init ? -0.5 * q * dt / (2.0 * m) : q * dt / (2.0 * m);
+    a.q_dt_2m = (float)rot;
+    a.hq = (float)(init ? -q / m * dt / 2.0 : q / m * dt / 2.0);
+    const double tx = p.Br * rot, ty = p.Bt * rot, tz = p.Bz * rot;
+    const double f = 2.0 / (1 + tx * tx + ty * ty + tz * tz);
+    a.tx = (float)tx;
+    a.ty = (float)ty;
+    a.tz = (float)tz;
+    a.sx = (float)(tx * f);
+    a.sy = (float)(ty * f);
+    a.sz = (float)(tz * f);
+    a.btab = p.magnetic_field_const ? 0 : 1;
+    a.Br = d_Br.p;
+    a.Bz = d_Bz.p;
+    a.bnx = bnx;
+    a.bnz = bnz;
+    a.b_x0 = (float)b_x0;
+    a.b_z0 = (float)b_z0;
+    a.b_ix = (float)(1.0 / b_dx);
+    a.b_iz = (float)(1.0 / b_dz);
+    a.gdx = (float)dx;
+    a.gdz = (float)dz;
+    a.gx0 = (float)x0;
+    a.gz0 = (float)z0;
+    a.cx = (float)(dt / dx);
+    a.cz = (float)(dt / dz);
+    a.rho = p.selfconsistent ? S.rho.p : nullptr;
+    a.coll_threshold = init ? 0u : S.threshold;
+    a.cand = S.cand.p;
+    a.seed = seed;
+    a.species = (uint32_t)s;
+    a.cnt = S.cnt.p;
+    return a;
+}
+
+CollideArgs Sim::collide_args(int s)
+{
+    SpeciesState& S = sp[s];
+    CollideArgs a{};
+    a.vx = S.vx.p;
+    a.vy = S.vy.p;
+    a.vz = S.vz.p;
+    a.id = S.id.p;
+    a.cand = S.cand.p;
+    a.cnt = S.cnt.p;
+    a.mass = S.prm.mass;
+    a.inv_lifetime = std::isinf(S.lifetime) ? 0.0 : 1.0 / S.lifetime;
+    a.nsp = (int)sp.size();
+    int pos = S.inter_off;
+    for (size_t t = 0; t < sp.size(); ++t) {
+        a.rates[t] = S.rates[t];
+        a.t_mass[t] = sp[t].prm.mass;
+        a.t_density[t] = sp[t].prm.density;
+        a.t_sigma_v[t] = sp[t].v_max * std::sqrt(0.5);
+        a.t_has_slots[t] = sp[t].n_slots > 0 ? 1 : 0;
+        a.t_x[t] = sp[t].x.p;
+        a.t_vx[t] = sp[t].vx.p;
+        a.t_vy[t] = sp[t].vy.p;
+        a.t_vz[t] = sp[t].vz.p;
+        a.t_n[t] = sp[t].n_slots;
+        a.inter_begin[t] = pos;
+        pos += (int)S.by_target[t].size();
+        a.inter_end[t] = pos;
+    }
+    a.inter = d_inter.p;
+    a.tables = d_tables.p;
+    a.seed = seed;
+    a.species = (uint32_t)s;
+    return a;
+}
+
+// One Pic::advance (src/pic.cpp:330-358).  With ev != nullptr, events
+// ev[0..3] are recorded before the solve, after the solve, after the particle
+// kernels and after the collision kernels.
+void Sim::step(cudaEvent_t* ev)
+{
+    if (ev) MAG_CK(cudaEventRecord(ev[0], stream));
+    if (p.selfconsistent) solve(false, rho_override ? 2 : 1, true, false);
+    rho_override = false;
+    if (ev) MAG_CK(cudaEventRecord(ev[1], stream));
+    for (size_t s = 0; s < sp.size(); ++s) {
+        SpeciesState& S = sp[s];
+        if (S.n_slots == 0) continue;
+        PushArgs pa = push_args((int)s, false);
+        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, false, stream);
+    }
+    if (ev) MAG_CK(cudaEventRecord(ev[2], stream));
+    for (size_t s = 0; s < sp.size(); ++s) {
+        SpeciesState& S = sp[s];
+        if (S.n_slots == 0) {
+            S.host_niter++;
+            continue;
+        }
+        const double expect = (double)S.n_slots * S.prob;
+        const int grid = (int)std::min<double>(304.0, std::ceil(4.0 * expect / 128.0) + 1.0);
+        launches += launch_collide(collide_args((int)s), grid, stream);
+    }
+    if (ev) MAG_CK(cudaEventRecord(ev[3], stream));
+}
+
+void Sim::advance_timed(uint64_t nsteps, double* ms3)
+{
+    MAG_CK(cudaSetDevice(device));
+    cudaEvent_t ev[4];
+    for (auto& e : ev) MAG_CK(cudaEventCreate(&e));
+    ms3[0] = ms3[1] = ms3[2] = 0.0;
+    for (uint64_t k = 0; k < nsteps; ++k) {
+        step(ev);
+        MAG_CK(cudaEventSynchronize(ev[3]));
+        float a, b, c;
+        MAG_CK(cudaEventElapsedTime(&a, ev[0], ev[1]));
+        MAG_CK(cudaEventElapsedTime(&b, ev[1], ev[2]));
+        MAG_CK(cudaEventElapsedTime(&c, ev[2], ev[3]));
+        ms3[0] += a;
+        ms3[1] += b;
+        ms3[2] += c;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+}
+
+void Sim::advance(uint64_t nsteps)
+{
+    MAG_CK(cudaSetDevice(device));
+    for (uint64_t k = 0; k < nsteps; ++k) step();
+    MAG_CK(cudaGetLastError());
+}
+
+// Pic::advance_init (src/pic.cpp:359-384)
+void Sim::advance_init()
+{
+    MAG_CK(cudaSetDevice(device));
+    if (p.selfconsistent) {
+        deposit_all();
+        solve(false, 1, false, false);
+    }
+    for (size_t s = 0; s < sp.size(); ++s) {
+        if (sp[s].n_slots == 0) continue;
+        PushArgs pa = push_args((int)s, true);
+        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, true, stream);
+    }
+    MAG_CK(cudaGetLastError());
+}
+
+void Sim::deposit_all()
+{
+    for (size_t s = 0; s < sp.size(); ++s) {
+        sp[s].rho.zero(stream);
+        if (sp[s].n_slots == 0) continue;
+        PushArgs pa = push_args((int)s, false);
+        pa.rho = sp[s].rho.p;
+        launches += launch_deposit(pa, stream);
+    }
+    rho_override = false;
+}
+
+SolveStatus Sim::field_solve()
+{
+    if (p.electric_field_from_file)
+        throw Error(-1, "no Poisson solve with electric_field_from_file (the reference forbids it, param.cpp:62-64)");
+    return solve(false, rho_override ? 2 : 1, false, true);
+}
+
+void Sim::get_field(int which, double* out)
+{
+    const size_t nn = (size_t)nx * nz;
+    MAG_CK(cudaStreamSynchronize(stream));
+    if (which == 0) u64.download(out, nn, stream);
+    else if (which == 1) urf64.download(out, nn, stream);
+    else if (which == 3) {
+        for (size_t k = 0; k < mask.size(); ++k) out[k] = mask[k];
+        return;
+    } else if (which == 4) {
+        std::copy(voltage.begin(), voltage.end(), out);
+        return;
+    } else if (which == 2 && rho_override) {
+        rho64.download(out, nn, stream);
+    } else if (which == 2 || which >= 5) {
+        std::fill(out, out + nn, 0.0);
+        std::vector<int64_t> acc(nn);
+        const size_t s0 = which == 2 ? 0 : (size_t)(which - 5), s1 = which == 2 ? sp.size() : s0 + 1;
+        if (s0 >= sp.size()) throw Error(-1, "species index out of range");
+        for (size_t s = s0; s < s1; ++s) {
+            MAG_CK(cudaMemcpyAsync(acc.data(), sp[s].rho.p, nn * 8, cudaMemcpyDeviceToHost, stream));
+            MAG_CK(cudaStreamSynchronize(stream));
+            const double w = sp[s].prm.charge * std::ldexp(1.0, -2 * kDepositShift);
+            for (size_t k = 0; k < nn; ++k) out[k] += w * (double)acc[k];
+        }
+        return;
+    } else
+        throw Error(-1, "unknown field selector");
+    MAG_CK(cudaStreamSynchronize(stream));
+}
+
+void Sim::set_field(int which, const double* in)
+{
+    const size_t nn = (size_t)nx * nz;
+    if (which == 0) u64.upload(in, nn, stream);
+    else if (which == 1) urf64.upload(in, nn, stream);
+    else if (which == 2) {
+        rho64.upload(in, nn, stream);
+        rho_override = true;
+    } else
+        throw Error(-1, "only u, uRF and rho can be set");
+    if (which == 0) launches += launch_faces(u64.p, nx, nz, dx, dz, Exf.p, Ezf.p, stream);
+    if (which == 1) launches += launch_faces(urf64.p, nx, nz, dx, dz, Exf_rf.p, Ezf_rf.p, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
+}
+
+void Sim::get_particles(int s, int64_t cap, double* x, double* z, double* vx, double* vy, double* vz, uint32_t* id,
+                        int64_t* n_out)
+{
+    SpeciesState& S = sp[s];
+    const int64_t n = S.n_slots;
+    std::vector<float> hx(n), hz(n), hvx(n), hvy(n), hvz(n);
+    std::vector<uint32_t> hid(n);
+    S.x.download(hx.data(), n, stream);
+    S.z.download(hz.data(), n, stream);
+    S.vx.download(hvx.data(), n, stream);
+    S.vy.download(hvy.data(), n, stream);
+    S.vz.download(hvz.data(), n, stream);
+    S.id.download(hid.data(), n, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
+    int64_t m = 0;
+    for (int64_t k = 0; k < n && m < cap; ++k) {
+        if (!(hx[k] >= 0.f)) continue;
+        if (x) x[m] = x0 + (double)hx[k] * dx;
+        if (z) z[m] = z0 + (double)hz[k] * dz;
+        if (vx) vx[m] = hvx[k];
+        if (vy) vy[m] = hvy[k];
+        if (vz) vz[m] = hvz[k];
+        if (id) id[m] = hid[k];
+        ++m;
+    }
+    *n_out = m;
+}
+
+void Sim::set_particles(int s, int64_t n, const double* x, const double* z, const double* vx, const double* vy,
+                        const double* vz)
+{
+    SpeciesState& S = sp[s];
+    MAG_CK(cudaStreamSynchronize(stream));
+    S.n_slots = 0;
+    if (S.host_niter) MAG_CK(cudaMemcpy(&S.cnt.p->niter, &S.host_niter, sizeof(uint64_t), cudaMemcpyHostToDevice));
+    ensure_capacity(s, std::max<int64_t>(n, 1));
+    std::vector<float> hx(n), hz(n), hvx(n), hvy(n), hvz(n);
+    for (int64_t k = 0; k < n; ++k) {
+        hx[k] = (float)((x[k] - x0) / dx);
+        hz[k] = (float)((z[k] - z0) / dz);
+        hvx[k] = (float)vx[k];
+        hvy[k] = (float)vy[k];
+        hvz[k] = (float)vz[k];
+    }
+    S.x.upload(hx.data(), n, stream);
+    S.z.upload(hz.data(), n, stream);
+    S.vx.upload(hvx.data(), n, stream);
+    S.vy.upload(hvy.data(), n, stream);
+    S.vz.upload(hvz.data(), n, stream);
+    launches += launch_fill_u32(S.id.p, 0, n, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
+    S.n_slots = n;
+    S.next_id = (uint32_t)n;
+}
+
+void Sim::get_rho_fixed(int s, int64_t* out)
+{
+    MAG_CK(cudaStreamSynchronize(stream));
+    sp[s].rho.download((unsigned long long*)out, (size_t)nx * nz, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
+}
+
+Counters Sim::counters(int s)
+{
+    Counters c{};
+    MAG_CK(cudaStreamSynchronize(stream));
+    MAG_CK(cudaMemcpy(&c, sp[s].cnt.p, sizeof c, cudaMemcpyDeviceToHost));
+    return c;
+}
+
+uint64_t Sim::niter(int s)
+{
+    if (sp[s].n_slots == 0) return sp[s].host_niter;
+    return counters(s).niter;
+}
+
+void Sim::energy(int s, double& sum_v2, unsigned long long& n)
+{
+    DevArray<double> d;
+    d.alloc(1);
+    d.zero(stream);
+    DevArray<unsigned long long> c;
+    c.alloc(1);
+    c.zero(stream);
+    SpeciesState& S = sp[s];
+    launches += launch_energy(S.x.p, S.vx.p, S.vy.p, S.vz.p, S.n_slots, d.p, c.p, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
+    sum_v2 = 0;
+    n = 0;
+    if (S.n_slots) {
+        MAG_CK(cudaMemcpy(&sum_v2, d.p, 8, cudaMemcpyDeviceToHost));
+        MAG_CK(cudaMemcpy(&n, c.p, 8, cudaMemcpyDeviceToHost));
+    }
+}
+
+}  // namespace mag

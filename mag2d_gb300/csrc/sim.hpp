@@ -1,0 +1,172 @@
+// Host orchestration of the GPU time step: owns the device state of one
+// simulation and issues the kernels of Pic::advance (src/pic.cpp:330-358).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "device.hpp"
+#include "host_config.hpp"
+
+namespace mag {
+
+void check_cuda(cudaError_t e, const char* what);
+#define MAG_CK(call) ::mag::check_cuda((call), #call)
+
+// Owning device allocation.
+template <class T>
+struct DevArray {
+    T* p = nullptr;
+    size_t n = 0;
+    DevArray() = default;
+    DevArray(const DevArray&) = delete;
+    DevArray& operator=(const DevArray&) = delete;
+    DevArray(DevArray&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevArray& operator=(DevArray&& o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    ~DevArray() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count)
+    {
+        release();
+        if (count == 0) return;
+        MAG_CK(cudaMalloc((void**)&p, count * sizeof(T)));
+        n = count;
+    }
+    void zero(cudaStream_t s)
+    {
+        if (n) MAG_CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+    void upload(const T* h, size_t count, cudaStream_t s)
+    {
+        if (count > n) alloc(count);
+        if (count) MAG_CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void download(T* h, size_t count, cudaStream_t s) const
+    {
+        if (count) MAG_CK(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+};
+
+struct SimOptions {
+    int device = 0;
+    uint64_t seed = 1;
+    int sort_interval = 0;
+    double poisson_tol = 1e-12;
+    int poisson_max_iter = 200;
+    int64_t capacity_hint = 0;
+};
+
+struct SpeciesState {
+    SpeciesParams prm;
+    double v_max = 0, E_max = 0, lifetime = INFINITY, prob = 0;
+    uint32_t threshold = 0;
+    std::vector<double> rates;              // rates_by_species
+    std::vector<std::vector<int>> by_target;  // interaction indices per target species
+    // device particles
+    DevArray<float> x, z, vx, vy, vz;
+    DevArray<uint32_t> id, cand;
+    int64_t cap = 0, n_slots = 0;
+    uint32_t next_id = 0;
+    DevArray<unsigned long long> rho;  // fixed-point charge grid
+    DevArray<Counters> cnt;
+    uint64_t host_niter = 0;           // step counter of species without particle storage
+    int inter_off = 0;                 // first entry of this species in the device interaction list
+};
+
+struct SolverLevels {
+    int nlev = 0;
+    std::vector<int> nx, nz;
+    std::vector<DevArray<float>> e, r, t, coef, inv_diag;
+};
+
+class Sim {
+public:
+    Sim(const std::string& config, const std::string& species_conf, const SimOptions& opts);
+    ~Sim();
+
+    void run_initscript(const std::string& path);
+    void advance_init();
+    void advance(uint64_t nsteps);
+    void advance_timed(uint64_t nsteps, double* ms3);
+    int sync();  // returns first device error code (0 = none)
+
+    // accessors used by the C ABI
+    Param p;
+    std::vector<SpeciesParams> species_prm;
+    std::vector<InteractionParams> inters;
+    std::vector<SpeciesState> sp;
+    std::vector<int8_t> mask;
+    std::vector<double> voltage;
+    int nx = 0, nz = 0;
+    double dx = 0, dz = 0, x0 = 0, z0 = 0, xmax = 0, zmax = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t seed = 1;
+    int64_t launches = 0;
+    double poisson_tol = 1e-12;
+    int poisson_max_iter = 200;
+    bool rho_override = false;
+    SolveStatus last_solve{};
+
+    void get_field(int which, double* out);
+    void set_field(int which, const double* in);
+    SolveStatus field_solve();
+    void get_particles(int s, int64_t cap, double* x, double* z, double* vx, double* vy, double* vz, uint32_t* id,
+                       int64_t* n_out);
+    void set_particles(int s, int64_t n, const double* x, const double* z, const double* vx, const double* vy,
+                       const double* vz);
+    void deposit_all();
+    void get_rho_fixed(int s, int64_t* out);
+    Counters counters(int s);
+    void energy(int s, double& sum_v2, unsigned long long& n);
+    uint64_t niter(int s);
+    int solver_levels() const { return lv.nlev; }
+
+private:
+    int emode = 1;
+    bool check_mask = true;
+    DevArray<int8_t> d_mask;
+    DevArray<double> d_volt, u64, urf64, b64, rho64, red;
+    DevArray<float> Exf, Ezf, Exf_rf, Ezf_rf, d_Br, d_Bz;
+    int bnx = 0, bnz = 0;
+    double b_x0 = 0, b_z0 = 0, b_dx = 1, b_dz = 1;
+    DevArray<SolveStatus> d_status;
+    DevArray<GridBarrier> d_bar;
+    DevArray<int> d_err;
+    DevArray<InterDev> d_inter;
+    DevArray<double> d_tables;
+    SolverLevels lv;
+    bool solver_ready = false;
+
+    void setup_fields();
+    void setup_species();
+    void setup_solver();
+    void validate_operator() const;
+    SolveStatus solve(bool rf_solve, int rho_src, bool clear_rho, bool wait);
+    void ensure_capacity(int s, int64_t need);
+    void add_loaded(int s, int64_t n, int kind, double cx, double cz, double radius, double zlo, double zhi);
+    void add_single(int s, double x, double z, double vx, double vy, double vz);
+    PushArgs push_args(int s, bool init);
+    CollideArgs collide_args(int s);
+    void step(cudaEvent_t* ev = nullptr);
+};
+
+}  // namespace mag

@@ -1,0 +1,244 @@
+"""Python mirror of the reference's Pic / Fields / Species interface
+(src/pic.cpp:115-538, src/fields.hpp:187-222, src/particles.hpp:95-318) over
+the C ABI of libmag2d_gpu.so.
+
+    pic = Pic("config.txt", "species_conf.txt", initscript="initscript.txt", seed=1)
+    pic.advance_init()
+    for i in range(niter):
+        pic.advance()
+    u = pic.field.u                      # Field2D data as a numpy (x, z) array
+    e = pic.speclist["ELECTRON"]         # Species view
+    p = e.particles()                    # dict of SoA numpy arrays in SI units
+
+The compute happens on the GPU; this module only moves data and arguments.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import _lib
+from ._lib import (MAG_MASK, MAG_RHO, MAG_SPECIES_RHO, MAG_U, MAG_URF, MAG_VOLTAGE, MagDiag, MagOpts,
+                   MagSolveInfo, MagSpeciesInfo, check, lib)
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+class Fields:
+    """The Fields members u, uRF, rho and the t_grid mask/voltage, as numpy copies."""
+
+    def __init__(self, pic: "Pic"):
+        self._pic = pic
+
+    def _get(self, which: int) -> np.ndarray:
+        nx, nz = self._pic.shape if which not in (MAG_MASK, MAG_VOLTAGE) else self._pic.mask_shape
+        out = np.zeros((nx, nz))
+        check(lib().mag_get_field(self._pic.h, which, _dp(out)))
+        return out
+
+    @property
+    def u(self) -> np.ndarray:
+        return self._get(MAG_U)
+
+    @property
+    def uRF(self) -> np.ndarray:
+        return self._get(MAG_URF)
+
+    @property
+    def rho(self) -> np.ndarray:
+        return self._get(MAG_RHO)
+
+    @property
+    def mask(self) -> np.ndarray:
+        return self._get(MAG_MASK).astype(np.int8)
+
+    @property
+    def voltage(self) -> np.ndarray:
+        return self._get(MAG_VOLTAGE)
+
+    def set_rho(self, rho: np.ndarray) -> None:
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        check(lib().mag_set_field(self._pic.h, MAG_RHO, _dp(rho)))
+
+    def set_u(self, u: np.ndarray) -> None:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        check(lib().mag_set_field(self._pic.h, MAG_U, _dp(u)))
+
+    def boundary_solve(self, rho: np.ndarray | None = None) -> dict:
+        """Fields::boundary_solve (src/fields.cpp:278-312) of the given or current rho."""
+        if rho is not None:
+            self.set_rho(rho)
+        info = MagSolveInfo()
+        check(lib().mag_field_solve(self._pic.h, ctypes.byref(info)))
+        return {"iterations": info.iterations, "residual": info.residual, "status": info.status,
+                "levels": info.levels}
+
+
+class Species:
+    """View of one species (BaseSpecies / Species<D>)."""
+
+    def __init__(self, pic: "Pic", index: int):
+        self._pic = pic
+        self.index = index
+
+    def info(self) -> dict:
+        s = MagSpeciesInfo()
+        check(lib().mag_species(self._pic.h, self.index, ctypes.byref(s)))
+        return {k: (getattr(s, k).decode() if k == "name" else getattr(s, k)) for k, _ in s._fields_}
+
+    @property
+    def name(self) -> str:
+        return self.info()["name"]
+
+    def n_particles(self) -> int:
+        return int(self.info()["n_live"])
+
+    def particles(self) -> dict:
+        """Live particles as SoA numpy arrays: x, z [m], vx, vy, vz [m/s], id."""
+        cap = max(int(self.info()["capacity"]), 1)
+        arrs = {k: np.zeros(cap) for k in ("x", "z", "vx", "vy", "vz")}
+        ids = np.zeros(cap, dtype=np.uint32)
+        n = ctypes.c_int64()
+        check(lib().mag_get_particles(self._pic.h, self.index, cap, *[_dp(arrs[k]) for k in ("x", "z", "vx", "vy", "vz")],
+                                      ids.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(n)))
+        out = {k: v[: n.value].copy() for k, v in arrs.items()}
+        out["id"] = ids[: n.value].copy()
+        return out
+
+    def set_particles(self, x, z, vx, vy, vz) -> None:
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (x, z, vx, vy, vz)]
+        check(lib().mag_set_particles(self._pic.h, self.index, len(a[0]), *[_dp(v) for v in a]))
+
+    def diag(self) -> dict:
+        d = MagDiag()
+        check(lib().mag_diag(self._pic.h, self.index, ctypes.byref(d)))
+        return {k: getattr(d, k) for k, _ in d._fields_}
+
+    def rho_fixed(self) -> np.ndarray:
+        nx, nz = self._pic.shape
+        out = np.zeros((nx, nz), dtype=np.int64)
+        check(lib().mag_get_rho_fixed(self._pic.h, self.index, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return out
+
+    @property
+    def rho(self) -> np.ndarray:
+        return self._pic.field._get(MAG_SPECIES_RHO + self.index)
+
+
+class Speclist:
+    def __init__(self, pic: "Pic"):
+        self._pic = pic
+        self._sp = [Species(pic, i) for i in range(check(lib().mag_n_species(pic.h)))]
+
+    def __len__(self) -> int:
+        return len(self._sp)
+
+    def __iter__(self):
+        return iter(self._sp)
+
+    def __getitem__(self, key):
+        if isinstance(key, str):
+            for s in self._sp:
+                if s.name == key:
+                    return s
+            raise KeyError(key)
+        return self._sp[key]
+
+
+class Pic:
+    """Pic<D> of the reference, on the GPU."""
+
+    def __init__(self, config, species_conf, initscript=None, *, seed: int = 1, device: int = 0,
+                 poisson_tol: float = 0.0, poisson_max_iter: int = 0, capacity_hint: int = 0):
+        opts = MagOpts(device=device, seed=seed, sort_interval=0, poisson_tol=poisson_tol,
+                       poisson_max_iter=poisson_max_iter, capacity_hint=capacity_hint)
+        h = ctypes.c_void_p()
+        ini = str(initscript).encode() if initscript else None
+        check(lib().mag_create(str(config).encode(), str(species_conf).encode(), ini, ctypes.byref(opts),
+                               ctypes.byref(h)))
+        self.h = h
+        nx, nz = ctypes.c_int(), ctypes.c_int()
+        dx, dz, x0, z0 = (ctypes.c_double() for _ in range(4))
+        check(lib().mag_grid(self.h, ctypes.byref(nx), ctypes.byref(nz), ctypes.byref(dx), ctypes.byref(dz),
+                             ctypes.byref(x0), ctypes.byref(z0)))
+        self.shape = (nx.value, nz.value)
+        self.dx, self.dz, self.x_min, self.z_min = dx.value, dz.value, x0.value, z0.value
+        self.mask_shape = (int(config_param(config, "x_sampl")), int(config_param(config, "z_sampl")))
+        self.field = Fields(self)
+        self.speclist = Speclist(self)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().mag_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run_initscript(self, path) -> None:
+        check(lib().mag_run_initscript(self.h, str(path).encode()))
+
+    def advance_init(self) -> None:
+        check(lib().mag_advance_init(self.h))
+
+    def advance(self, n: int = 1) -> None:
+        check(lib().mag_advance(self.h, n))
+
+    def advance_timed(self, n: int = 1):
+        """advance(n) with per-kernel CUDA event timing: (solve_ms, particle_ms, collide_ms)."""
+        ms = np.zeros(3)
+        check(lib().mag_advance_timed(self.h, n, _dp(ms)))
+        return tuple(ms)
+
+    def sync(self) -> None:
+        check(lib().mag_sync(self.h))
+
+    def deposit(self) -> None:
+        check(lib().mag_deposit(self.h))
+
+    @property
+    def stream(self) -> int:
+        return lib().mag_stream(self.h) or 0
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().mag_kernel_launches(self.h))
+
+
+def config_param(config, key: str) -> float:
+    """Param value of a config file (host-only, no GPU)."""
+    v = ctypes.c_double()
+    check(lib().mag_config_param(str(config).encode(), key.encode(), ctypes.byref(v)))
+    return v.value
+
+
+def config_geometry(config):
+    """(mask, voltage) of the config's geometry (host-only, no GPU)."""
+    nx, nz = ctypes.c_int(), ctypes.c_int()
+    nx_ = int(config_param(config, "x_sampl"))
+    nz_ = int(config_param(config, "z_sampl"))
+    mask = np.zeros((nx_, nz_), dtype=np.int8)
+    volt = np.zeros((nx_, nz_))
+    check(lib().mag_config_geometry(str(config).encode(), nx_ * nz_,
+                                    mask.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), _dp(volt),
+                                    ctypes.byref(nx), ctypes.byref(nz)))
+    return mask, volt
+
+
+def config_species(config, species_conf, index: int):
+    """(info dict, rates array) of species 'index' (host-only, no GPU)."""
+    info = MagSpeciesInfo()
+    rates = np.zeros(64)
+    n = check(lib().mag_config_species(str(config).encode(), str(species_conf).encode(), index,
+                                       ctypes.byref(info), _dp(rates)))
+    d = {k: (getattr(info, k).decode() if k == "name" else getattr(info, k)) for k, _ in info._fields_}
+    return d, rates[:n]

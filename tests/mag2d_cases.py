@@ -55,8 +55,10 @@ def write_config(cfg: dict, path) -> Path:
     path = Path(path)
     lines = ["# generated test configuration"]
     for k, v in cfg.items():
-        if isinstance(v, float):
-            v = repr(v)
+        if isinstance(v, (float, np.floating)):
+            v = repr(float(v))
+        elif isinstance(v, (np.integer,)):
+            v = int(v)
         lines.append(f"{k} = {v}")
     path.write_text("\n".join(lines) + "\n")
     return path
@@ -74,7 +76,7 @@ def write_species_conf(species: list, interactions: list, path) -> Path:
         for k, tag in keys:
             if k in s:
                 v = s[k]
-                out.append(f"    {tag} {v!r}" if isinstance(v, float) else f"    {tag} {v}")
+                out.append(f"    {tag} {float(v)!r}" if isinstance(v, (float, np.floating)) else f"    {tag} {v}")
         out.append("")
     for it in interactions:
         out.append("INTERACTION")
@@ -84,11 +86,11 @@ def write_species_conf(species: list, interactions: list, path) -> Path:
         out.append(f"    SECONDARY {it['secondary']}")
         for k, tag in (("DE", "DE"), ("rate", "RATE"), ("cutoff", "CUTOFF")):
             if k in it:
-                out.append(f"    {tag} {it[k]!r}")
+                out.append(f"    {tag} {float(it[k])!r}")
         if it.get("table"):
             out.append("    CROSS_SECTION")
             for e, sg in it["table"]:
-                out.append(f"        {e!r} {sg!r}")
+                out.append(f"        {float(e)!r} {float(sg)!r}")
             out.append("    END_CROSS_SECTION")
         out.append("")
     path.write_text("\n".join(out) + "\n")
@@ -101,7 +103,7 @@ def write_field_file(path, x, z, values) -> Path:
     with open(path, "w") as f:
         for i, xv in enumerate(x):
             for j, zv in enumerate(z):
-                f.write(f"{xv!r} {zv!r} {values[i, j]!r}\n")
+                f.write(f"{float(xv)!r} {float(zv)!r} {float(values[i, j])!r}\n")
     return path
 
 

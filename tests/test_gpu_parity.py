@@ -1,0 +1,188 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle port.
+
+Tolerances (from the spec bar of the project):
+  * deposit        — bit-exact against the oracle's fixed-point CIC deposit
+  * Poisson solve  — |u_gpu - u_oracle|_inf <= 1e-9 |u_oracle|_inf
+  * trajectories   — positions within 1e-5 of the domain size after 1000 steps
+                     with collisions off (FP32 state against the FP64 oracle)
+  * MCC            — collision counts within 3 sigma of the expected count and a
+                     two-sample KS test on energies at p > 0.01
+"""
+from __future__ import annotations
+
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def m(built):
+    import mag2d_gb300
+
+    return mag2d_gb300
+
+
+def _port_for(m, cfg, species, inter, cpath, seed=1, loaded=None):
+    from mag2d_cases import Port
+
+    mask, volt = m.config_geometry(cpath)
+    return Port(cfg, species, inter, mask, volt, seed=seed, loaded_fields=loaded)
+
+
+def _match(g, o):
+    """Map GPU particles (by id) onto oracle slots (slot i holds input i)."""
+    live = o[:, 7] == 0
+    ids = g["id"].astype(np.int64)
+    common = np.intersect1d(ids, np.flatnonzero(live))
+    pos = {int(k): i for i, k in enumerate(ids)}
+    sel = np.array([pos[int(k)] for k in common], dtype=np.int64)
+    return common, sel, live
+
+
+# ---------------------------------------------------------------------------
+# Poisson: FP32 multigrid + FP64 refinement against the oracle's direct solve
+@pytest.mark.parametrize("geom", [
+    dict(coord="CYLINDRICAL", geometry="PENNING_ENDCAP", r_max=5e-3, z_max=20e-3, r_sampl=65, z_sampl=129),
+    dict(coord="CYLINDRICAL", geometry="PENNING_SIMPLE", r_max=1.2e-2, z_max=7.5e-2, r_sampl=33, z_sampl=129),
+    dict(coord="CYLINDRICAL", geometry="PENNING", r_max=1.2e-2, z_max=7.5e-2, r_sampl=49, z_sampl=97),
+    dict(coord="CARTESIAN", geometry="RF_22PT", x_max=2e-2, z_max=2e-2, x_sampl=129, z_sampl=129),
+    dict(coord="CARTESIAN", geometry="PROBE", x_max=2e-2, z_max=2e-2, x_sampl=65, z_sampl=65, probe_radius=1e-3),
+    dict(coord="CARTESIAN", geometry="EMPTY", x_max=2e-2, z_max=2e-2, x_sampl=50, z_sampl=50, extern_field=300.0),
+], ids=["penning_endcap", "penning_simple", "penning", "rf22pt", "probe", "empty_sor"])
+def test_poisson_matches_direct_solve(m, tmp_path, geom):
+    from mag2d_cases import QE, write_config, write_species_conf
+
+    cfg = dict(selfconsistent=1, rf=0, do_plot=0, macroparticle_factor=100.0, **geom)
+    species = [dict(name="E", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11, temperature=1e4, density=1e13)]
+    cpath = write_config(cfg, tmp_path / "c.txt")
+    spath = write_species_conf(species, [], tmp_path / "s.txt")
+    pic = m.Pic(cpath, spath, seed=1)
+    port = _port_for(m, cfg, species, [], cpath)
+    rng = np.random.default_rng(5)
+    nx, nz = pic.shape
+    # a space charge of ~1e13 m^-3 electrons: -q * weights of ~10 macro particles per node
+    rho = -QE * 10 * rng.random((nx, nz))
+    info = pic.field.boundary_solve(rho)
+    u_gpu = pic.field.u
+    u_ref = port.solve(rho)
+    err = np.abs(u_gpu - u_ref).max() / np.abs(u_ref).max()
+    assert info["status"] == 0, info
+    assert err <= 1e-9, (err, info)
+    pic.close()
+
+
+# ---------------------------------------------------------------------------
+def test_deposit_bit_exact(m, tmp_path):
+    from cases import penning_rz
+    from mag2d_cases import deposit_fixed
+
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=50_000)
+    pic = m.Pic(cpath, spath, seed=1)
+    sp = pic.speclist[0]
+    sp.set_particles(*parts)
+    pic.deposit()
+    got = sp.rho_fixed()
+    xg = np.float32((parts[0] - pic.x_min) / pic.dx)
+    zg = np.float32((parts[1] - pic.z_min) / pic.dz)
+    want = deposit_fixed(pic.shape[0], pic.shape[1], xg, zg)
+    assert np.array_equal(got, want)
+    # every particle contributes exactly 2^40
+    assert got.sum() == len(xg) << 40
+    pic.close()
+
+
+# ---------------------------------------------------------------------------
+def _trajectory_case(m, tmp_path, make, nsteps, n, species_index, **kw):
+    out = make(tmp_path, n=n, **kw)
+    cfg, species, inter, cpath, spath, parts = out[:6]
+    loaded = out[6] if len(out) > 6 else None
+    pic = m.Pic(cpath, spath, seed=3)
+    pic.speclist[species_index].set_particles(*parts)
+    pic.advance_init()
+    pic.advance(nsteps)
+    pic.sync()
+    g = pic.speclist[species_index].particles()
+    port = _port_for(m, cfg, species, inter, cpath, seed=3, loaded=loaded)
+    port.set_particles(species_index, *parts)
+    port.advance_init()
+    port.advance(nsteps)
+    o = port.particles(species_index)
+    pic.close()
+    return g, o
+
+
+def test_penning_trajectories_1000_steps(m, tmp_path):
+    from cases import penning_rz
+
+    g, o = _trajectory_case(m, tmp_path, penning_rz, 1000, 2000, 0)
+    common, sel, live = _match(g, o)
+    assert len(common) >= live.sum() - 2
+    ex = np.abs(g["x"][sel] - o[common, 0]) / 5e-3
+    ez = np.abs(g["z"][sel] - o[common, 2]) / 20e-3
+    assert np.percentile(np.maximum(ex, ez), 99) < 1e-5, (ex.max(), ez.max())
+    assert max(ex.max(), ez.max()) < 1e-4
+
+
+def test_multipole_trajectories_1000_steps(m, tmp_path):
+    from cases import multipole_xy
+
+    g, o = _trajectory_case(m, tmp_path, multipole_xy, 1000, 2000, 1, collisions=False, n_nodes=129)
+    common, sel, live = _match(g, o)
+    assert len(common) >= live.sum() - 2
+    ex = np.abs(g["x"][sel] - o[common, 0]) / 10e-3
+    ez = np.abs(g["z"][sel] - o[common, 2]) / 10e-3
+    assert np.percentile(np.maximum(ex, ez), 99) < 1e-5, (ex.max(), ez.max())
+    assert max(ex.max(), ez.max()) < 1e-4
+
+
+# ---------------------------------------------------------------------------
+def _ks_2samp(a, b):
+    a, b = np.sort(a), np.sort(b)
+    allv = np.concatenate([a, b])
+    cdf_a = np.searchsorted(a, allv, side="right") / len(a)
+    cdf_b = np.searchsorted(b, allv, side="right") / len(b)
+    d = np.abs(cdf_a - cdf_b).max()
+    ne = len(a) * len(b) / (len(a) + len(b))
+    lam = (math.sqrt(ne) + 0.12 + 0.11 / math.sqrt(ne)) * d
+    p = 2 * sum((-1) ** (k - 1) * math.exp(-2 * k * k * lam * lam) for k in range(1, 101))
+    return d, min(max(p, 0.0), 1.0)
+
+
+def test_mcc_statistics_multipole(m, tmp_path):
+    """Collision counts within 3 sigma and energy distributions alike (KS p > 0.01)."""
+    from cases import multipole_xy
+    from mag2d_cases import AMU, QE
+
+    n, steps = 20_000, 200
+    cfg, species, inter, cpath, spath, parts, loaded = multipole_xy(tmp_path, n=n, n_nodes=129, pressure=5.0)
+    pic = m.Pic(cpath, spath, seed=11)
+    ion = pic.speclist[1]
+    ion.set_particles(*parts)
+    pic.advance_init()
+    pic.advance(steps)
+    d = ion.diag()
+    g = ion.particles()
+    port = _port_for(m, cfg, species, inter, cpath, seed=11, loaded=loaded)
+    port.set_particles(1, *parts)
+    port.advance_init()
+    port.advance(steps)
+    o = port.particles(1)
+    info = ion.info()
+    prob = 1.0 - math.exp(-info["dt"] / info["lifetime"])
+    # candidate count ~ Binomial(live * steps, prob); live changes little in this run
+    live_mean = 0.5 * (n + d["n_live"])
+    expect = live_mean * steps * prob
+    cand = d["collisions"] + d["null_collisions"]
+    assert abs(cand - expect) < 3 * math.sqrt(expect) + 0.01 * expect, (cand, expect)
+    ncoll_oracle = port.collisions(1)
+    assert abs(cand - ncoll_oracle) < 3 * math.sqrt(2 * expect), (cand, ncoll_oracle)
+    eg = 0.5 * 3 * AMU * (g["vx"] ** 2 + g["vy"] ** 2 + g["vz"] ** 2) / QE
+    lo = o[o[:, 7] == 0]
+    eo = 0.5 * 3 * AMU * (lo[:, 3] ** 2 + lo[:, 4] ** 2 + lo[:, 5] ** 2) / QE
+    _, p = _ks_2samp(eg, eo)
+    assert p > 0.01, p
+    pic.close()

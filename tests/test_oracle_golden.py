@@ -1,0 +1,181 @@
+"""The oracle port against golden vectors produced by the reference itself
+(tests/golden/make_golden.py): bit-exact random streams, particle states,
+potentials.  CPU only."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def port_lib(built):
+    from mag2d_cases import load_port
+
+    return load_port()
+
+
+def _meta(d):
+    return json.loads(str(d["meta"]))
+
+
+def test_rng_streams_match_reference(port_lib):
+    from mag2d_cases import Port
+
+    g = np.load(GOLDEN / "rng.npz")
+    cfg = dict(coord="CARTESIAN", geometry="EMPTY", x_sampl=5, z_sampl=5, selfconsistent=0, rf=0)
+    mask = np.zeros((5, 5), np.int8)
+    p = Port(cfg, [dict(name="E", mass=9.11e-31, charge=-1.6e-19, dt=1e-11, temperature=1e4)], [], mask,
+             np.zeros((5, 5)))
+    for seed in (1, 1234, 4242):
+        p.L.orc_seed(p.h, seed)
+        assert np.array_equal(p.rng(0, 1000), g[f"uni_{seed}"])
+        assert np.array_equal(p.rng(1, 4000), g[f"rnor_{seed}"])
+        assert np.array_equal(p.rng(2, 4000), g[f"rexp_{seed}"])
+        assert np.array_equal(p.rng(3, 500), g[f"iuni_{seed}"])
+        assert np.array_equal(p.rng(4, 500), g[f"rot_{seed}"])
+        assert np.array_equal(p.rng(5, 500, 0.75 * np.pi), g[f"deflect_{seed}"])
+
+
+def test_rng_distribution_kats(port_lib):
+    """Known-answer properties of the reference's generators (tests/test_deflect.cpp,
+    the isotropy and Maxwellian checks of tests/rot_test.cpp and tests/maxwell_test.cpp)."""
+    g = np.load(GOLDEN / "rng.npz")
+    rnor = g["rnor_1234"]
+    assert abs(rnor.mean()) < 4 / np.sqrt(len(rnor)) and abs(rnor.std() - 1) < 0.05
+    rexp = g["rexp_1234"]
+    assert abs(rexp.mean() - 1) < 0.05
+    rot = g["rot_1234"].reshape(-1, 3)
+    assert np.allclose(np.linalg.norm(rot, axis=1), 1.0, atol=1e-12)
+    assert np.abs(rot.mean(axis=0)).max() < 0.1
+    d = g["deflect_1234"].reshape(-1, 3)
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-9)  # deflect preserves |v|
+    assert np.allclose(d[:, 0], np.cos(0.75 * np.pi), atol=1e-9)  # by the requested angle
+
+
+STEP_CASES = sorted(p.name for p in GOLDEN.glob("step_*.npz"))
+
+
+@pytest.mark.parametrize("fname", STEP_CASES)
+def test_step_matches_reference(port_lib, fname, tmp_path):
+    from mag2d_cases import Port
+
+    d = np.load(GOLDEN / fname)
+    m = _meta(d)
+    loaded = None
+    if m["has_fields"]:
+        nx, nz, dx, dz = d["f_grid"]
+        loaded = (int(nx), int(nz), dx, dz, 0.0, 0.0, d["f_u"], d["f_urf"])
+    port = Port(m["cfg"], m["species"], m["inter"], d["mask"], d["voltage"], seed=m["seed"], loaded_fields=loaded)
+    ns = len(m["species"])
+    for s in range(ns):
+        if f"init_{s}" in d:
+            port.set_particles(s, *d[f"init_{s}"])
+    if m["initscript"]:
+        (tmp_path / "init.txt").write_text(m["initscript"])
+        port.run_initscript(tmp_path / "init.txt")
+    port.advance_init()
+    for s in range(ns):
+        assert np.array_equal(port.particles(s), d[f"p_init_{s}"]), (fname, "init", s)
+    done = 0
+    for k in m["snaps"]:
+        port.advance(k - done)
+        done = k
+        for s in range(ns):
+            got, want = port.particles(s), d[f"p_{k}_{s}"]
+            assert got.shape == want.shape, (fname, k, s)
+            assert np.array_equal(got, want), (fname, k, s, np.nanmax(np.abs(got - want)))
+    assert np.array_equal(port.field(0), d["u"])
+    if not m["has_fields"]:  # with loaded fields the reference leaves rho uninitialised (pic.cpp:163)
+        assert np.array_equal(port.field(2), d["rho"])
+
+
+@pytest.mark.parametrize("fname", sorted(p.name for p in GOLDEN.glob("solve_*.npz")))
+def test_poisson_solve_matches_reference(port_lib, fname):
+    from mag2d_cases import Port
+
+    d = np.load(GOLDEN / fname)
+    m = _meta(d)
+    port = Port(m["cfg"], m["species"], [], d["mask"], d["voltage"])
+    u = port.solve(d["rho"])
+    assert np.array_equal(u, d["u"])
+
+
+@pytest.mark.parametrize("fname", sorted(p.name for p in GOLDEN.glob("solve_*.npz")))
+def test_poisson_solve_independent_check(fname):
+    """The reference's linear system (fields.cpp:136-312) solved by SciPy's
+    SuperLU agrees with the golden potential to 1e-11 (pins the banded LU used
+    in place of UMFPACK)."""
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    from mag2d_cases import EPS0, full_config
+
+    d = np.load(GOLDEN / fname)
+    m = _meta(d)
+    c = full_config(m["cfg"])
+    mask, volt, rho = d["mask"], d["voltage"], d["rho"]
+    nx, nz = mask.shape
+    dx, dz = float(c["x_max"]) / (nx - 1), float(c["z_max"]) / (nz - 1)
+    cyl = c["coord"] == "CYLINDRICAL"
+    rows, cols, vals = [], [], []
+    b = np.zeros(nx * nz)
+    for i in range(nx):
+        for j in range(nz):
+            k = i * nz + j
+            if mask[i, j] in (0, 1):
+                rows.append(k), cols.append(k), vals.append(1.0)
+                b[k] = volt[i, j] if mask[i, j] == 0 else 0.0
+                continue
+            if cyl and i == 0:
+                k2, k3 = 1 / dz ** 2, 1 / (dx * dx * 0.25)
+                st = [(k - 1, k2), (k, -2 * k2 - k3), (k + 1, k2), (k + nz, k3)]
+                b[k] = rho[i, j] * (-1.0 / EPS0 / (np.pi * dx * dx * 0.25 * dz) * float(c["macroparticle_factor"]))
+            elif cyl:
+                k1, k2, k3 = (i - 0.5) / (dx * dx * i), 1 / dz ** 2, (i + 0.5) / (dx * dx * i)
+                st = [(k - nz, k1), (k - 1, k2), (k, -2 * k2 - k1 - k3), (k + 1, k2), (k + nz, k3)]
+                b[k] = rho[i, j] * (-1.0 / EPS0 / (np.pi * dx * dx * 2.0 * i * dz) * float(c["macroparticle_factor"]))
+            else:
+                V = float(c["n_particles_total"]) / float(c["density_total"])
+                dV = V / ((nx - 1) * (nz - 1))
+                st = [(k - nz, 1.0), (k - 1, 1.0), (k, -4.0), (k + 1, 1.0), (k + nz, 1.0)]
+                b[k] = rho[i, j] * (-dx * dx / EPS0 / dV)
+            for cc, v in st:
+                rows.append(k), cols.append(cc), vals.append(v)
+    A = sp.csc_matrix((vals, (rows, cols)), shape=(nx * nz, nx * nz))
+    lu = spl.splu(A)
+    u = lu.solve(b)
+    for _ in range(3):  # iterative refinement: SuperLU alone leaves ~1e-8 residuals on these systems
+        u = u + lu.solve(b - A @ u)
+    assert np.abs(u.reshape(nx, nz) - d["u"]).max() <= 1e-11 * np.abs(d["u"]).max()
+
+
+def test_fixed_point_deposit_properties(port_lib):
+    """The quantised CIC deposit conserves charge exactly (2^40 per particle)
+    and stays within 2^-20 per weight of the reference's FP64 weights."""
+    from mag2d_cases import deposit_fixed
+
+    rng = np.random.default_rng(1)
+    n, nx, nz = 5000, 17, 33
+    xg = (rng.random(n) * (nx - 1)).astype(np.float32)
+    zg = (rng.random(n) * (nz - 1)).astype(np.float32)
+    acc = deposit_fixed(nx, nz, xg, zg)
+    assert acc.sum() == n << 40
+    ref = np.zeros((nx, nz))
+    i, j = np.floor(xg).astype(int), np.floor(zg).astype(int)
+    u, v = xg.astype(np.float64) - i, zg.astype(np.float64) - j
+    np.add.at(ref, (i, j), (1 - u) * (1 - v))
+    np.add.at(ref, (i + 1, j), u * (1 - v))
+    np.add.at(ref, (i, j + 1), (1 - u) * v)
+    np.add.at(ref, (i + 1, j + 1), u * v)
+    counts = np.zeros((nx, nz))
+    for di in (0, 1):
+        for dj in (0, 1):
+            np.add.at(counts, (i + di, j + dj), 1)
+    assert np.all(np.abs(acc / 2.0 ** 40 - ref) <= counts * 2.0 ** -19)
+    # order independence: any permutation gives identical integers
+    perm = rng.permutation(n)
+    assert np.array_equal(deposit_fixed(nx, nz, xg[perm], zg[perm]), acc)
