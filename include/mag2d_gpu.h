@@ -50,7 +50,7 @@ typedef struct mag_sim mag_sim;
 typedef struct {
     int device;            /* CUDA device ordinal */
     uint64_t seed;         /* Philox key of every random draw */
-    int sort_interval;     /* counting sort of particles by cell every N steps (0 = never) */
+    int sort_interval;     /* counting sort of particles by cell every N steps (0 = 20, < 0 = never) */
     double poisson_tol;    /* Jacobi-scaled residual / max|u| at which the solve stops (0 = 1e-12) */
     int poisson_max_iter;  /* outer refinement iterations before MAG_ENOTCONV (0 = 200) */
     int64_t capacity_hint; /* particle slots to reserve per species (0 = grow as needed) */

@@ -35,7 +35,7 @@ def _sources():
 
 
 def _newest_header() -> float:
-    hs = list(CSRC.glob("*.hpp")) + list((ROOT / "include").glob("*.h"))
+    hs = list(CSRC.glob("*.hpp")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 

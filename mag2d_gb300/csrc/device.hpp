@@ -1,8 +1,11 @@
 // Data shared between the host orchestration and the sm_103a kernels.
 //
 // HBM layout of one species (SoA, one array per component, length = slots):
-//   x, z   float   position in grid units of the field grid, (x - x_min)/dx and
-//                  (z - z_min)/dz; a removed particle holds x = -1
+//   x, z   uint32  position in cells of the field grid as fixed point with
+//                  kFracBits fractional bits: x = round((x_SI - x_min)/dx * 2^20).
+//                  The cell index is x >> 20 and the CIC fraction (x & 0xFFFFF)
+//                  is exact; resolution 2^-20 cell everywhere on grids up to
+//                  4095 cells per axis.  A removed particle holds x = kDead.
 //   vx, vy, vz float  velocity [m/s]; (vx, vy, vz) = (radial/x, azimuthal/y, axial/z)
 //                  as in t_particle (src/particles.hpp:26-33)
 //   id     uint32  persistent particle id (key of its random stream)
@@ -13,6 +16,8 @@
 // which makes the staggered gradient of Field2D::grad (src/Field2D.hpp:80-168)
 // a plain bilinear interpolation of four face values per component.
 #pragma once
+#include <vector_types.h>
+
 #include <cstdint>
 
 namespace mag {
@@ -20,8 +25,11 @@ namespace mag {
 constexpr int kMaxSpecies = 16;
 constexpr int kMaxInteractions = 64;
 constexpr int kMaxLevels = 12;
-constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis
-constexpr float kDeadX = -1.0f;
+constexpr int kFracBits = 20;      // fixed-point fraction of a cell in the positions
+constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis (= kFracBits)
+constexpr uint32_t kFracMask = (1u << kFracBits) - 1u;
+constexpr uint32_t kDead = 0xFFFFFFFFu;
+constexpr int kMaxCellsPerAxis = 4095;
 
 // CollType of the species_conf INTERACTION blocks (src/parser.hpp:15)
 enum CollType { ELASTIC = 0, LANGEVIN = 1, CX = 2, COULOMB = 3, SUPERELASTIC = 4 };
@@ -37,44 +45,64 @@ struct Counters {
     unsigned long long nnull;      // null collisions
     unsigned long long partner_miss;
     unsigned long long done_blocks;
+    unsigned long long slots;      // slots in use on the device (shrinks when a sort compacts)
     int error;                     // first device error code (0 = none)
     int pad;
 };
 
+// Null-collision tables of one species (device copy), shared by the inline
+// collision path of the particle kernel and the candidate-list kernel.
+struct InterDev;
+struct MccSpecies {
+    double mass, inv_lifetime;
+    int nsp;
+    double rates[kMaxSpecies];
+    double t_mass[kMaxSpecies], t_density[kMaxSpecies], t_sigma_v[kMaxSpecies];
+    int inter_begin[kMaxSpecies], inter_end[kMaxSpecies];
+    const InterDev* inter;
+    const double* tables;
+};
+
 struct PushArgs {
-    float *x, *z, *vx, *vy, *vz;
+    uint32_t *x, *z;
+    float *vx, *vy, *vz;
     const uint32_t* id;
-    int64_t n;
+    int64_t n;                 // slots (upper bound; the live range may be shorter after a sort)
+    const unsigned long long* n_dev;  // current slot count on the device (null: use n)
     int nx, nz;
-    float xmaxg, zmaxg;   // domain extent in grid units
+    uint32_t xmaxf, zmaxf;     // domain extent in fixed point
     int periodic;
-    int check_mask;       // kill particles in cells with no FREE corner (t_grid::is_free)
-    const int8_t* mask;   // nx*nz
-    // electric field: 0 uniform (0, extern_ez), 1 from u, 2 from u and uRF
+    int check_mask;            // kill particles in cells with no FREE corner (t_grid::is_free)
+    const int8_t* mask;        // nx*nz
+    // electric field: 0 uniform (0, extern_ez), 1 from u faces, 2 from (u, uRF) face pairs
     int emode;
     const float* Exf;
     const float* Ezf;
-    const float* Exf_rf;
-    const float* Ezf_rf;
+    const float2* Exf2;
+    const float2* Ezf2;
     float extern_ez;
-    double rf_omega, rf_amp, rf_U0, dt;
+    float phase;                   // rf_amplitude cos(mod(rf_omega niter dt, 1e7 pi)) + rf_U0 (fields.hpp:135-145)
+    uint64_t step;                 // this species' step counter (niter), the counter of its random streams
     // magnetic field: constant Boris vectors, or tables Br/Bz (Field2D::interpolate)
     int btab;
     float tx, ty, tz, sx, sy, sz;
     const float* Br;
     const float* Bz;
     int bnx, bnz;
-    float b_x0, b_z0, b_ix, b_iz;  // table index = (xg*dx + x_min - b_xmin) * b_idx
+    float b_x0, b_z0, b_ix, b_iz;  // table index = (x_cells*dx + x_min - b_xmin) * b_idx
     float gdx, gdz, gx0, gz0;      // field grid dx, dz, x_min, z_min (for tables)
     float q_dt_2m;                 // charge*dt/(2*mass)
     float hq;                      // charge/mass*dt/2
-    float cx, cz;                  // dt/dx, dt/dz
+    float cx, cz;                  // dt/dx, dt/dz (cells per m/s)
     unsigned long long* rho;       // fixed-point deposit (nx*nz) or null
     uint32_t coll_threshold;       // collision probability * 2^32 (0: no test)
+    int coll_mode;                 // 0 none, 1 inline scatter (Maxwellian targets), 2 candidate list
     uint32_t* cand;
+    const MccSpecies* mcc;
     uint64_t seed;
     uint32_t species;
     Counters* cnt;
+    int close_step;                // the last block closes the step (no collide kernel follows)
 };
 
 struct InterDev {
@@ -93,23 +121,32 @@ struct CollideArgs {
     const uint32_t* id;
     const uint32_t* cand;
     Counters* cnt;
-    double mass, inv_lifetime;
-    int nsp;
-    double rates[kMaxSpecies];
-    double t_mass[kMaxSpecies], t_density[kMaxSpecies], t_sigma_v[kMaxSpecies];
+    const MccSpecies* mcc;
     int t_has_slots[kMaxSpecies];
-    float* t_x[kMaxSpecies];
+    const uint32_t* t_x[kMaxSpecies];
     float* t_vx[kMaxSpecies];
     float* t_vy[kMaxSpecies];
     float* t_vz[kMaxSpecies];
     int64_t t_n[kMaxSpecies];
-    int inter_begin[kMaxSpecies], inter_end[kMaxSpecies];
-    const InterDev* inter;
-    const double* tables;  // E_eV then sigma, per interaction
     uint64_t seed;
     uint32_t species;
-    // step-end bookkeeping done by the last block
-    unsigned long long* rho_unused;
+    uint64_t step;
+};
+
+struct SortArgs {
+    const uint32_t *x, *z;
+    const float *vx, *vy, *vz;
+    const uint32_t* id;
+    uint32_t *ox, *oz;
+    float *ovx, *ovy, *ovz;
+    uint32_t* oid;
+    int64_t n;
+    int nx, nz;
+    long long ncells;        // (nx-1)*(nz-1)
+    uint32_t* count;         // ncells, zero on entry and on exit
+    uint32_t* offset;        // ncells + 1
+    uint32_t* blocksum;      // ceil(ncells/1024)
+    Counters* cnt;
 };
 
 struct SolveStatus {

@@ -10,7 +10,8 @@ namespace {
 constexpr double kPi = 3.14159265358979323846;
 
 struct LoadArgs {
-    float *x, *z, *vx, *vy, *vz;
+    uint32_t *x, *z;
+    float *vx, *vy, *vz;
     uint32_t* id;
     int64_t n;
     uint32_t id0;
@@ -83,8 +84,10 @@ __global__ void k_load(const LoadArgs a)
         z = a.zlo + (a.zhi - a.zlo) * r.uni();
     }
     if (x < a.x0 || x > a.xmax || z < a.z0 || z > a.zmax) ok = false;
-    a.x[k] = ok ? (float)((x - a.x0) / a.dx) : kDeadX;
-    a.z[k] = (float)((z - a.z0) / a.dz);
+    const double fx = rint((x - a.x0) / a.dx * (double)(1u << kFracBits));
+    const double fz = rint((z - a.z0) / a.dz * (double)(1u << kFracBits));
+    a.x[k] = ok ? (uint32_t)fx : kDead;
+    a.z[k] = ok ? (uint32_t)fz : 0u;
     a.vx[k] = (float)(r.normal() * a.vsig);
     a.vz[k] = (float)(r.normal() * a.vsig);
     a.vy[k] = (float)(r.normal() * a.vsig);
@@ -97,13 +100,13 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t v0, int64_t n)
         p[k] = v0 + (uint32_t)k;
 }
 
-__global__ void k_energy(const float* x, const float* vx, const float* vy, const float* vz, int64_t n, double* sum,
+__global__ void k_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n, double* sum,
                          unsigned long long* cnt)
 {
     double s = 0.0;
     unsigned long long c = 0;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        if (!(x[k] >= 0.f)) continue;
+        if (x[k] == kDead) continue;
         const double a = vx[k], b = vy[k], d = vz[k];
         s += a * a + b * b + d * d;
         ++c;
@@ -118,9 +121,22 @@ __global__ void k_energy(const float* x, const float* vx, const float* vy, const
     }
 }
 
+__global__ void k_interleave(const float* a, const float* b, float2* out, long long n)
+{
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        out[k] = make_float2(a[k], b[k]);
+}
+
 }  // namespace
 
-int launch_load_disk(float* x, float* z, float* vx, float* vy, float* vz, uint32_t* id, int64_t n, uint32_t id0,
+int launch_interleave(const float* a, const float* b, float2* out, long long n, cudaStream_t s)
+{
+    if (n == 0) return 0;
+    k_interleave<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 8), 256, 0, s>>>(a, b, out, n);
+    return 1;
+}
+
+int launch_load_disk(uint32_t* x, uint32_t* z, float* vx, float* vy, float* vz, uint32_t* id, int64_t n, uint32_t id0,
                      int kind, double cx, double cz, double radius, double zlo, double zhi, double x0, double z0,
                      double dx, double dz, double xmax, double zmax, double vsig, uint64_t seed, uint32_t species,
                      int, cudaStream_t s)
@@ -138,7 +154,7 @@ int launch_fill_u32(uint32_t* p, uint32_t v0, int64_t n, cudaStream_t s)
     return 1;
 }
 
-int launch_energy(const float* x, const float* vx, const float* vy, const float* vz, int64_t n, double* out_sum_v2,
+int launch_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n, double* out_sum_v2,
                   unsigned long long* out_n, cudaStream_t s)
 {
     if (n == 0) return 0;

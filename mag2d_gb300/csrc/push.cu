@@ -1,28 +1,36 @@
-// Particle step kernel: field gather, Boris push, collision test, boundary,
-// mask test and fixed-point charge deposit, fused into one pass over the SoA.
+// Particle step kernel: field gather, Boris push, collision test (and, against
+// Maxwellian background targets, the collision itself), boundary, mask test
+// and fixed-point charge deposit, fused into one pass over the SoA.
 //
 // Replaces, per particle, the loop bodies of
 //   Species<CYLINDRICAL>::advance_boris   src/particles.cpp:539-621
 //   Species<CARTESIAN>::advance_boris     src/particles.cpp:924-995
 //   Fields::E / Fields::B                 src/fields.hpp:124-177
+//   BaseSpecies::scatter                  src/particles.cpp:208-365 (Maxwellian partners)
 //   Species::advance_boundary             src/particles.hpp:370-411
 //   t_grid::is_free                       src/fields.hpp:94-101
 //   Field2D::accumulate                   src/Field2D.hpp:45-62
-// The scatter itself (uni() < prob -> BaseSpecies::scatter) is deferred to
-// the collide kernel through a compacted candidate list; scattering changes
-// only velocities, so boundary and deposit, which read positions only, give
-// the same result as in the reference's order.
+// Scattering changes only velocities, so boundary and deposit, which read
+// positions only, give the same result as in the reference's order.
 //
 // HBM traffic per live particle and step: read x, z, vx, vy, vz (20 B) and,
 // when collisions are on, id (4 B); write x, z, vx, vy, vz (20 B).  Field
-// faces, mask and the charge grid are small and stay in L2.
+// faces, mask and the charge grid are small and stay in L1/L2 when the
+// particles are sorted by cell.
 #include "device.hpp"
 #include "kernels.hpp"
+#include "mcc_device.cuh"
 #include "philox.hpp"
 
 namespace mag {
 
 namespace {
+
+constexpr float kInvOne = 1.0f / (float)(1u << kFracBits);
+constexpr float kOne = (float)(1u << kFracBits);
+constexpr uint32_t kHalf = 1u << (kFracBits - 1);
+
+__device__ __forceinline__ float frac(uint32_t v) { return (float)(v & kFracMask) * kInvOne; }
 
 __device__ __forceinline__ float bilerp(const float* __restrict__ f, int stride, int i, int j, float fx, float fz)
 {
@@ -31,134 +39,200 @@ __device__ __forceinline__ float bilerp(const float* __restrict__ f, int stride,
     return (1.f - fx) * ((1.f - fz) * a + fz * b) + fx * ((1.f - fz) * c + fz * d);
 }
 
-// E at grid position (xg, zg) from face arrays (Field2D::grad with the sign of Fields::E)
-__device__ __forceinline__ void gather_faces(const float* __restrict__ Exf, const float* __restrict__ Ezf, int nx,
-                                             int nz, float xg, float zg, float& ex, float& ez)
+__device__ __forceinline__ float2 bilerp2(const float2* __restrict__ f, int stride, int i, int j, float fx, float fz)
 {
-    int ix = (int)(xg + 0.5f);
-    ix = max(0, min(ix, nx - 1));
-    int jz = max(0, min((int)zg, nz - 2));
-    ex = bilerp(Exf, nz, ix, jz, xg + 0.5f - (float)ix, zg - (float)jz);
-    int ix2 = max(0, min((int)xg, nx - 2));
-    int jz2 = (int)(zg + 0.5f);
-    jz2 = max(0, min(jz2, nz - 1));
-    ez = bilerp(Ezf, nz + 1, ix2, jz2, xg - (float)ix2, zg + 0.5f - (float)jz2);
+    const float2* p = f + (size_t)i * stride + j;
+    const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + stride), d = __ldg(p + stride + 1);
+    const float w00 = (1.f - fx) * (1.f - fz), w01 = (1.f - fx) * fz, w10 = fx * (1.f - fz), w11 = fx * fz;
+    return make_float2(w00 * a.x + w01 * b.x + w10 * c.x + w11 * d.x, w00 * a.y + w01 * b.y + w10 * c.y + w11 * d.y);
+}
+
+// Stencil of Field2D::grad at fixed-point position (x, z): the x component
+// interpolates faces (ix, ix+1) x (jz, jz+1) around the rounded x, the z
+// component faces (iz, iz+1) x (jz2, jz2+1) around the rounded z.
+struct GatherIdx {
+    int ix, jz, iz, jz2;
+    float fx, fz, gx, gz;
+};
+__device__ __forceinline__ GatherIdx gather_idx(uint32_t x, uint32_t z, int nx, int nz)
+{
+    GatherIdx g;
+    const uint32_t xr = x + kHalf, zr = z + kHalf;
+    g.ix = min((int)(xr >> kFracBits), nx - 1);
+    g.fx = frac(xr);
+    g.jz = min((int)(z >> kFracBits), nz - 2);
+    g.fz = (float)(z - ((uint32_t)g.jz << kFracBits)) * kInvOne;
+    g.iz = min((int)(x >> kFracBits), nx - 2);
+    g.gx = (float)(x - ((uint32_t)g.iz << kFracBits)) * kInvOne;
+    g.jz2 = min((int)(zr >> kFracBits), nz - 1);
+    g.gz = frac(zr);
+    return g;
 }
 
 // Field2D::interpolate of a B table at physical position (x, z)
 __device__ __forceinline__ float table_interp(const float* __restrict__ t, int bnx, int bnz, float xi, float zi)
 {
-    int i = max(0, min((int)xi, bnx - 2));
-    int j = max(0, min((int)zi, bnz - 2));
+    const int i = max(0, min((int)xi, bnx - 2));
+    const int j = max(0, min((int)zi, bnz - 2));
     return bilerp(t, bnz, i, j, xi - (float)i, zi - (float)j);
 }
 
-__device__ __forceinline__ double mod_phase(double x, double y)  // src/mymath.cpp:62-67
+template <int EMODE>
+__device__ __forceinline__ void gather_E(const PushArgs& a, uint32_t x, uint32_t z, float phase, float& ex, float& ez)
 {
-    if (x >= 0.0 && x <= y) return x;
-    return x - y * (double)(int)(x / y) + (x < 0 ? y : 0);
+    if (EMODE == 0) {
+        ex = 0.f;
+        ez = a.extern_ez;
+        return;
+    }
+    const GatherIdx g = gather_idx(x, z, a.nx, a.nz);
+    if (EMODE == 1) {
+        ex = bilerp(a.Exf, a.nz, g.ix, g.jz, g.fx, g.fz);
+        ez = bilerp(a.Ezf, a.nz + 1, g.iz, g.jz2, g.gx, g.gz);
+    } else {
+        const float2 px = bilerp2(a.Exf2, a.nz, g.ix, g.jz, g.fx, g.fz);
+        const float2 pz = bilerp2(a.Ezf2, a.nz + 1, g.iz, g.jz2, g.gx, g.gz);
+        ex = px.x + phase * px.y;
+        ez = pz.x + phase * pz.y;
+    }
+}
+
+__device__ __forceinline__ void boris_vectors(const PushArgs& a, uint32_t x, uint32_t z, float& tx, float& ty,
+                                              float& tz, float& sx, float& sy, float& sz)
+{
+    tx = a.tx, ty = a.ty, tz = a.tz, sx = a.sx, sy = a.sy, sz = a.sz;
+    if (a.btab) {
+        const float xc = (float)(x >> kFracBits) + frac(x), zc = (float)(z >> kFracBits) + frac(z);
+        const float xi = (xc * a.gdx + a.gx0 - a.b_x0) * a.b_ix;
+        const float zi = (zc * a.gdz + a.gz0 - a.b_z0) * a.b_iz;
+        tx = table_interp(a.Br, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
+        tz = table_interp(a.Bz, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
+        ty = 0.f;
+        const float f = 2.f / (1.f + tx * tx + ty * ty + tz * tz);
+        sx = tx * f;
+        sy = ty * f;
+        sz = tz * f;
+    }
+}
+
+template <int COORD>
+__device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float tx, float ty, float tz, float sx,
+                                       float sy, float sz)
+{
+    if (COORD == 1) {  // (r, theta, z) orientation, particles.cpp:581-592
+        const float vpr = vx + vy * tz - vz * ty;
+        const float vpt = vy + vz * tx - vx * tz;
+        const float vpz = vz + vx * ty - vy * tx;
+        vx += vpt * sz - vpz * sy;
+        vy += vpz * sx - vpr * sz;
+        vz += vpr * sy - vpt * sx;
+    } else {  // (x, y, z) ~ (r, z, theta), particles.cpp:968-979
+        const float vpr = vx - vy * tz + vz * ty;
+        const float vpz = vz - vx * ty + vy * tx;
+        const float vpt = vy - vz * tx + vx * tz;
+        vx += -vpt * sz + vpz * sy;
+        vy += -vpz * sx + vpr * sz;
+        vz += -vpr * sy + vpt * sx;
+    }
+}
+
+__device__ __forceinline__ bool wrap_or_keep(int64_t& p, uint32_t maxf, int periodic)
+{
+    if (p >= 0 && p <= (int64_t)maxf) return true;
+    if (!periodic || maxf == 0) return false;
+    p %= (int64_t)maxf;
+    if (p < 0) p += maxf;
+    return true;
+}
+
+__device__ __forceinline__ void close_step_if_last(Counters* c, unsigned long long coll, unsigned long long nnull)
+{
+    // one thread per block; the last block to arrive finishes the step
+    if (coll) atomicAdd(&c->ncoll, coll);
+    if (nnull) atomicAdd(&c->nnull, nnull);
+    __threadfence();
+    const unsigned long long ticket = atomicAdd(&c->done_blocks, 1ull);
+    if (ticket == gridDim.x - 1) {
+        __threadfence();
+        const unsigned long long live = *((volatile unsigned long long*)&c->live_step);
+        c->live_last = live;
+        c->live_sum += live;
+        c->live_step = 0;
+        c->ncand = 0;
+        c->done_blocks = 0;
+        c->niter += 1;
+        __threadfence();
+    }
 }
 
 template <int COORD, int EMODE>
-__global__ void __launch_bounds__(256) k_push(const PushArgs a)
+__global__ void __launch_bounds__(256, 8) k_push(const PushArgs a)
 {
-    __shared__ float s_phase;
-    if (EMODE == 2) {
-        if (threadIdx.x == 0) {
-            const double t = (double)a.cnt->niter * a.dt;
-            s_phase = (float)(a.rf_amp * cos(mod_phase(a.rf_omega * t, 10000000 * M_PI)) + a.rf_U0);
-        }
-        __syncthreads();
+    __shared__ unsigned long long s_coll, s_null;
+    __shared__ long long s_n;
+    if (threadIdx.x == 0) {
+        s_coll = 0;
+        s_null = 0;
+        s_n = a.n_dev ? (long long)min((unsigned long long)a.n, *a.n_dev) : a.n;
     }
+    __syncthreads();
+    const uint64_t step = a.step;
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in_range = k < a.n;
-    float xg = in_range ? a.x[k] : kDeadX;
-    const bool was_alive = xg >= 0.f;
+    const bool in_range = k < s_n;
+    uint32_t x = in_range ? a.x[k] : kDead;
+    const bool was_alive = x != kDead;
     bool alive = was_alive;
     bool cand = false;
     if (was_alive) {
-        float zg = a.z[k];
+        uint32_t z = a.z[k];
         float vx = a.vx[k], vy = a.vy[k], vz = a.vz[k];
         float ex, ez;
-        if (EMODE == 0) {
-            ex = 0.f;
-            ez = a.extern_ez;
-        } else {
-            gather_faces(a.Exf, a.Ezf, a.nx, a.nz, xg, zg, ex, ez);
-            if (EMODE == 2) {
-                float rx, rz;
-                gather_faces(a.Exf_rf, a.Ezf_rf, a.nx, a.nz, xg, zg, rx, rz);
-                ex += s_phase * rx;
-                ez += s_phase * rz;
-            }
-        }
-        float tx = a.tx, ty = a.ty, tz = a.tz, sx = a.sx, sy = a.sy, sz = a.sz;
-        if (a.btab) {
-            const float xi = (xg * a.gdx + a.gx0 - a.b_x0) * a.b_ix;
-            const float zi = (zg * a.gdz + a.gz0 - a.b_z0) * a.b_iz;
-            tx = table_interp(a.Br, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
-            tz = table_interp(a.Bz, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
-            ty = 0.f;
-            const float f = 2.f / (1.f + tx * tx + ty * ty + tz * tz);
-            sx = tx * f;
-            sy = ty * f;
-            sz = tz * f;
-        }
+        gather_E<EMODE>(a, x, z, a.phase, ex, ez);
+        float tx, ty, tz, sx, sy, sz;
+        boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
         // half acceleration, Boris rotation (Birdsall & Langdon), half acceleration
         vx += ex * a.hq;
         vz += ez * a.hq;
-        if (COORD == 1) {
-            const float vpr = vx + vy * tz - vz * ty;
-            const float vpt = vy + vz * tx - vx * tz;
-            const float vpz = vz + vx * ty - vy * tx;
-            vx += vpt * sz - vpz * sy;
-            vy += vpz * sx - vpr * sz;
-            vz += vpr * sy - vpt * sx;
-        } else {
-            const float vpr = vx - vy * tz + vz * ty;
-            const float vpz = vz - vx * ty + vy * tx;
-            const float vpt = vy - vz * tx + vx * tz;
-            vx += -vpt * sz + vpz * sy;
-            vy += -vpz * sx + vpr * sz;
-            vz += -vpr * sy + vpt * sx;
-        }
+        rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
         vx += ex * a.hq;
         vz += ez * a.hq;
+        int64_t px, pz;
+        const float dz = vz * a.cz;
         if (COORD == 1) {
-            // push in the local Cartesian frame, map back to r and rotate v (Birdsall p. 338)
-            const float x2 = xg + vx * a.cx;
-            const float y2 = vy * a.cx;
-            const float r = sqrtf(x2 * x2 + y2 * y2);
-            zg += vz * a.cz;
+            // push in the local Cartesian frame, map back to r and rotate v (Birdsall p. 338);
+            // dr = r' - r = (2 r a + a^2 + b^2) / (r' + r) keeps the fixed-point r exact
+            const float r = (float)(x >> kFracBits) + frac(x);
+            const float ax = vx * a.cx, by = vy * a.cx;
+            const float x2 = r + ax;
+            const float rn = sqrtf(x2 * x2 + by * by);
+            const float den = rn + r;
+            const float dr = den > 0.f ? (ax * (r + x2) + by * by) / den : 0.f;
             float sa = 0.f, ca = 1.f;
-            if (r != 0.f) {
-                const float ir = 1.f / r;
-                sa = y2 * ir;
+            if (rn != 0.f) {
+                const float ir = 1.f / rn;
+                sa = by * ir;
                 ca = x2 * ir;
             }
             const float t0 = vx;
             vx = ca * vx + sa * vy;
             vy = -sa * t0 + ca * vy;
-            xg = r;
+            px = isfinite(dr) ? (int64_t)x + __float2ll_rn(dr * kOne) : -1;
         } else {
-            xg += vx * a.cx;
-            zg += vz * a.cz;
+            const float dx = vx * a.cx;
+            px = isfinite(dx) ? (int64_t)x + __float2ll_rn(dx * kOne) : -1;
         }
+        pz = isfinite(dz) ? (int64_t)z + __float2ll_rn(dz * kOne) : -1;
         // boundary (advance_boundary): outside the box -> removed, or wrapped if PERIODIC
-        if (!(xg >= 0.f && xg <= a.xmaxg && zg >= 0.f && zg <= a.zmaxg)) {
-            if (a.periodic && isfinite(xg) && isfinite(zg)) {
-                xg = fmodf(xg, a.xmaxg);
-                if (xg < 0.f) xg += a.xmaxg;
-                zg = fmodf(zg, a.zmaxg);
-                if (zg < 0.f) zg += a.zmaxg;
-            } else {
-                alive = false;
-            }
+        alive = wrap_or_keep(px, a.xmaxf, a.periodic && isfinite(dz)) &&
+                wrap_or_keep(pz, a.zmaxf, a.periodic && isfinite(dz));
+        if (alive) {
+            x = (uint32_t)px;
+            z = (uint32_t)pz;
         }
         int ic = 0, jc = 0;
         if (alive) {
-            ic = min((int)xg, a.nx - 2);
-            jc = min((int)zg, a.nz - 2);
+            ic = min((int)(x >> kFracBits), a.nx - 2);
+            jc = min((int)(z >> kFracBits), a.nz - 2);
         }
         if (alive && a.check_mask) {
             const int8_t* m = a.mask + (size_t)ic * a.nz + jc;
@@ -167,8 +241,8 @@ __global__ void __launch_bounds__(256) k_push(const PushArgs a)
         }
         if (alive && a.rho != nullptr) {
             const unsigned long long one = 1ull << kDepositShift;
-            const unsigned long long U = (unsigned long long)((xg - (float)ic) * (float)(1 << kDepositShift));
-            const unsigned long long V = (unsigned long long)((zg - (float)jc) * (float)(1 << kDepositShift));
+            const unsigned long long U = x - ((uint32_t)ic << kFracBits);
+            const unsigned long long V = z - ((uint32_t)jc << kFracBits);
             unsigned long long* r0 = a.rho + (size_t)ic * a.nz + jc;
             atomicAdd(r0, (one - U) * (one - V));
             atomicAdd(r0 + a.nz, U * (one - V));
@@ -176,11 +250,19 @@ __global__ void __launch_bounds__(256) k_push(const PushArgs a)
             atomicAdd(r0 + a.nz + 1, U * V);
         }
         if (alive && a.coll_threshold != 0u) {
-            const U4 r = draw(a.seed, a.species, a.id[k], a.cnt->niter, TAG_COLLIDE_TEST, 0);
-            cand = r.x < a.coll_threshold;
+            const uint32_t pid = a.id[k];
+            const U4 r = draw(a.seed, a.species, pid, step, TAG_COLLIDE_TEST, 0);
+            if (r.x < a.coll_threshold) {
+                if (a.coll_mode == 1) {
+                    const int res = mcc_scatter_maxwell(a.mcc, a.seed, a.species, pid, step, vx, vy, vz);
+                    atomicAdd(res == MCC_HIT ? &s_coll : &s_null, 1ull);
+                } else {
+                    cand = true;
+                }
+            }
         }
-        a.x[k] = alive ? xg : kDeadX;
-        a.z[k] = zg;
+        a.x[k] = alive ? x : kDead;
+        a.z[k] = z;
         a.vx[k] = vx;
         a.vy[k] = vy;
         a.vz[k] = vz;
@@ -201,68 +283,29 @@ __global__ void __launch_bounds__(256) k_push(const PushArgs a)
         base = __shfl_sync(full, base, 0);
         if (cand) a.cand[base + __popc(cand_mask & ((1u << lane) - 1u))] = (uint32_t)k;
     }
+    if (a.close_step) {
+        __syncthreads();
+        if (threadIdx.x == 0) close_step_if_last(a.cnt, s_coll, s_null);
+    }
 }
 
 // Leapfrog start (advance_boris_init, src/particles.cpp:623-679, :997-1050):
-// a backward half rotation and a backward half acceleration, no move.
+// a backward half rotation and a backward half acceleration, no move.  The
+// caller passes the half-angle backward rotation vectors and hq = -q/m dt/2.
 template <int COORD, int EMODE>
 __global__ void __launch_bounds__(256) k_push_init(const PushArgs a)
 {
-    __shared__ float s_phase;
-    if (EMODE == 2) {
-        if (threadIdx.x == 0) {
-            const double t = (double)a.cnt->niter * a.dt;
-            s_phase = (float)(a.rf_amp * cos(mod_phase(a.rf_omega * t, 10000000 * M_PI)) + a.rf_U0);
-        }
-        __syncthreads();
-    }
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n) return;
-    const float xg = a.x[k];
-    if (!(xg >= 0.f)) return;
-    const float zg = a.z[k];
+    const uint32_t x = a.x[k];
+    if (x == kDead) return;
+    const uint32_t z = a.z[k];
     float vx = a.vx[k], vy = a.vy[k], vz = a.vz[k];
     float ex, ez;
-    if (EMODE == 0) {
-        ex = 0.f;
-        ez = a.extern_ez;
-    } else {
-        gather_faces(a.Exf, a.Ezf, a.nx, a.nz, xg, zg, ex, ez);
-        if (EMODE == 2) {
-            float rx, rz;
-            gather_faces(a.Exf_rf, a.Ezf_rf, a.nx, a.nz, xg, zg, rx, rz);
-            ex += s_phase * rx;
-            ez += s_phase * rz;
-        }
-    }
-    // here (tx..sz) hold the half-angle backward rotation vectors and hq = -q/m*dt/2
-    float tx = a.tx, ty = a.ty, tz = a.tz, sx = a.sx, sy = a.sy, sz = a.sz;
-    if (a.btab) {
-        const float xi = (xg * a.gdx + a.gx0 - a.b_x0) * a.b_ix;
-        const float zi = (zg * a.gdz + a.gz0 - a.b_z0) * a.b_iz;
-        tx = table_interp(a.Br, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
-        tz = table_interp(a.Bz, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
-        ty = 0.f;
-        const float f = 2.f / (1.f + tx * tx + ty * ty + tz * tz);
-        sx = tx * f;
-        sy = ty * f;
-        sz = tz * f;
-    }
-    if (COORD == 1) {
-        const float vpr = vx + vy * tz - vz * ty;
-        const float vpt = vy + vz * tx - vx * tz;
-        const float vpz = vz + vx * ty - vy * tx;
-        vx += vpt * sz - vpz * sy;
-        vy += vpz * sx - vpr * sz;
-        vz += vpr * sy - vpt * sx;
-    } else {
-        const float vpr = vx - vy * tz + vz * ty;
-        const float vpz = vz - vx * ty + vy * tx;
-        const float vpt = vy - vz * tx + vx * tz;
-        vx += -vpt * sz + vpz * sy;
-        vy += -vpz * sx + vpr * sz;
-        vz += -vpr * sy + vpt * sx;
-    }
+    gather_E<EMODE>(a, x, z, a.phase, ex, ez);
+    float tx, ty, tz, sx, sy, sz;
+    boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
+    rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
     vx += ex * a.hq;
     vz += ez * a.hq;
     a.vx[k] = vx;
@@ -275,14 +318,14 @@ __global__ void __launch_bounds__(256) k_deposit(const PushArgs a)
 {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n) return;
-    const float xg = a.x[k];
-    if (!(xg >= 0.f)) return;
-    const float zg = a.z[k];
-    const int ic = max(0, min((int)xg, a.nx - 2));
-    const int jc = max(0, min((int)zg, a.nz - 2));
+    const uint32_t x = a.x[k];
+    if (x == kDead) return;
+    const uint32_t z = a.z[k];
+    const int ic = min((int)(x >> kFracBits), a.nx - 2);
+    const int jc = min((int)(z >> kFracBits), a.nz - 2);
     const unsigned long long one = 1ull << kDepositShift;
-    const unsigned long long U = (unsigned long long)((xg - (float)ic) * (float)(1 << kDepositShift));
-    const unsigned long long V = (unsigned long long)((zg - (float)jc) * (float)(1 << kDepositShift));
+    const unsigned long long U = x - ((uint32_t)ic << kFracBits);
+    const unsigned long long V = z - ((uint32_t)jc << kFracBits);
     unsigned long long* r0 = a.rho + (size_t)ic * a.nz + jc;
     atomicAdd(r0, (one - U) * (one - V));
     atomicAdd(r0 + a.nz, U * (one - V));

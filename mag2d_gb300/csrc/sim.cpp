@@ -156,6 +156,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     seed = opts.seed;
     poisson_tol = opts.poisson_tol > 0 ? opts.poisson_tol : 1e-12;
     poisson_max_iter = opts.poisson_max_iter > 0 ? opts.poisson_max_iter : 200;
+    sort_interval = opts.sort_interval == 0 ? 20 : opts.sort_interval;
     p = make_param(KeyValueConfig::from_file(config));
     if (p.mover != ADVANCE_BORIS)
         throw Error(-1, "mover ADVANCE_MULTICOLL is not provided by this library (Boris mover only)");
@@ -207,6 +208,7 @@ int Sim::sync()
         Counters c;
         MAG_CK(cudaMemcpy(&c, s.cnt.p, sizeof c, cudaMemcpyDeviceToHost));
         if (c.error && !err) err = c.error;
+        if (s.n_slots > 0 && (int64_t)c.slots < s.n_slots) s.n_slots = (int64_t)c.slots;
     }
     if (err) {
         int zero = 0;
@@ -253,6 +255,8 @@ void Sim::setup_fields()
         urf64.zero(stream);
         check_mask = true;
     }
+    if (nx - 1 > kMaxCellsPerAxis || nz - 1 > kMaxCellsPerAxis || nx < 2 || nz < 2)
+        throw Error(-1, "field grid must have 2..4096 nodes per axis (fixed-point particle positions)");
     const size_t nn = (size_t)nx * nz;
     b64.alloc(std::max(nn, mask.size()));
     rho64.alloc(nn);
@@ -261,6 +265,12 @@ void Sim::setup_fields()
     Ezf.alloc((size_t)nx * (nz + 1));
     Exf_rf.alloc((size_t)(nx + 1) * nz);
     Ezf_rf.alloc((size_t)nx * (nz + 1));
+    Exf2.alloc((size_t)(nx + 1) * nz);
+    Ezf2.alloc((size_t)nx * (nz + 1));
+    sort_count.alloc((size_t)(nx - 1) * (nz - 1));
+    sort_count.zero(stream);
+    sort_offset.alloc((size_t)(nx - 1) * (nz - 1) + 1);
+    sort_blocksum.alloc(((size_t)(nx - 1) * (nz - 1) + 1023) / 1024 + 1);
     d_mask.upload(mask.data(), mask.size(), stream);
     d_volt.upload(voltage.data(), voltage.size(), stream);
     if (p.geometry == GEO_EMPTY && !p.selfconsistent) emode = 0;
@@ -288,6 +298,22 @@ void Sim::setup_fields()
         if (!p.selfconsistent) solve(false, 0, false, false);
         else launches += launch_faces(u64.p, nx, nz, dx, dz, Exf.p, Ezf.p, stream);
     }
+    refresh_rf_pairs();
+}
+
+// (u, uRF) face pairs for the RF gather
+void Sim::refresh_rf_pairs()
+{
+    if (emode != 2) return;
+    launches += launch_interleave(Exf.p, Exf_rf.p, Exf2.p, (long long)(nx + 1) * nz, stream);
+    launches += launch_interleave(Ezf.p, Ezf_rf.p, Ezf2.p, (long long)nx * (nz + 1), stream);
+}
+
+void Sim::upload_slots(int s)
+{
+    const unsigned long long v = (unsigned long long)sp[s].n_slots;
+    MAG_CK(cudaMemcpyAsync(&sp[s].cnt.p->slots, &v, sizeof v, cudaMemcpyHostToDevice, stream));
+    MAG_CK(cudaStreamSynchronize(stream));
 }
 
 void Sim::validate_operator() const
@@ -475,31 +501,56 @@ void Sim::setup_species()
     if (tab.empty()) tab.push_back(0.0);
     d_inter.upload(idev.data(), idev.size(), stream);
     d_tables.upload(tab.data(), tab.size(), stream);
+    for (int s = 0; s < ns; ++s) {
+        SpeciesState& S = sp[s];
+        MccSpecies m{};
+        m.mass = S.prm.mass;
+        m.inv_lifetime = std::isinf(S.lifetime) ? 0.0 : 1.0 / S.lifetime;
+        m.nsp = ns;
+        int pos = S.inter_off;
+        for (int t = 0; t < ns; ++t) {
+            m.rates[t] = S.rates[t];
+            m.t_mass[t] = species_prm[t].mass;
+            m.t_density[t] = species_prm[t].density;
+            m.t_sigma_v[t] = std::sqrt(2.0 * kKB * species_prm[t].temperature / species_prm[t].mass) * std::sqrt(0.5);
+            m.inter_begin[t] = pos;
+            pos += (int)S.by_target[t].size();
+            m.inter_end[t] = pos;
+        }
+        m.inter = d_inter.p;
+        m.tables = d_tables.p;
+        S.mcc.upload(&m, 1, stream);
+    }
+    MAG_CK(cudaStreamSynchronize(stream));
 }
 
 void Sim::ensure_capacity(int s, int64_t need)
 {
     SpeciesState& S = sp[s];
     if (need <= S.cap) return;
-    int64_t cap = std::max<int64_t>(need, (int64_t)(S.cap * 1.5) + 1024);
-    auto grow_f = [&](DevArray<float>& a) {
-        DevArray<float> b;
+    const int64_t cap = std::max<int64_t>(need, (int64_t)(S.cap * 1.5) + 1024);
+    MAG_CK(cudaStreamSynchronize(stream));
+    auto grow = [&](auto& a) {
+        typename std::remove_reference<decltype(a)>::type b;
         b.alloc(cap);
-        if (S.n_slots) MAG_CK(cudaMemcpyAsync(b.p, a.p, S.n_slots * sizeof(float), cudaMemcpyDeviceToDevice, stream));
+        if (S.n_slots)
+            MAG_CK(cudaMemcpyAsync(b.p, a.p, S.n_slots * sizeof(*a.p), cudaMemcpyDeviceToDevice, stream));
         MAG_CK(cudaStreamSynchronize(stream));
         a = std::move(b);
     };
-    grow_f(S.x);
-    grow_f(S.z);
-    grow_f(S.vx);
-    grow_f(S.vy);
-    grow_f(S.vz);
-    DevArray<uint32_t> nid;
-    nid.alloc(cap);
-    if (S.n_slots) MAG_CK(cudaMemcpyAsync(nid.p, S.id.p, S.n_slots * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
-    MAG_CK(cudaStreamSynchronize(stream));
-    S.id = std::move(nid);
+    grow(S.x);
+    grow(S.z);
+    grow(S.vx);
+    grow(S.vy);
+    grow(S.vz);
+    grow(S.id);
     S.cand.alloc(cap);
+    S.bx.release();  // sort buffers are re-made at the next sort
+    S.bz.release();
+    S.bvx.release();
+    S.bvy.release();
+    S.bvz.release();
+    S.bid.release();
     S.cap = cap;
 }
 
@@ -507,8 +558,6 @@ void Sim::add_loaded(int s, int64_t n, int kind, double cx, double cz, double ra
 {
     if (n <= 0) return;
     SpeciesState& S = sp[s];
-    if (S.n_slots == 0 && S.host_niter) MAG_CK(cudaMemcpyAsync(&S.cnt.p->niter, &S.host_niter, sizeof(uint64_t),
-                                                               cudaMemcpyHostToDevice, stream));
     ensure_capacity(s, S.n_slots + n);
     const double vsig = S.v_max * std::sqrt(0.5);
     const int64_t o = S.n_slots;
@@ -518,6 +567,8 @@ void Sim::add_loaded(int s, int64_t n, int kind, double cx, double cz, double ra
     MAG_CK(cudaGetLastError());
     S.n_slots += n;
     S.next_id += (uint32_t)n;
+    upload_slots(s);
+    sort_due = true;
 }
 
 void Sim::add_single(int s, double x, double z, double vx, double vy, double vz)
@@ -525,7 +576,9 @@ void Sim::add_single(int s, double x, double z, double vx, double vy, double vz)
     SpeciesState& S = sp[s];
     ensure_capacity(s, S.n_slots + 1);
     const int64_t o = S.n_slots;
-    float fx = (float)((x - x0) / dx), fz = (float)((z - z0) / dz);
+    const bool inside = x >= x0 && x <= xmax && z >= z0 && z <= zmax;
+    uint32_t fx = inside ? (uint32_t)std::llrint((x - x0) / dx * (double)(1u << kFracBits)) : kDead;
+    uint32_t fz = inside ? (uint32_t)std::llrint((z - z0) / dz * (double)(1u << kFracBits)) : 0u;
     float fvx = (float)vx, fvy = (float)vy, fvz = (float)vz;
     uint32_t pid = S.next_id;
     MAG_CK(cudaMemcpy(S.x.p + o, &fx, 4, cudaMemcpyHostToDevice));
@@ -536,6 +589,8 @@ void Sim::add_single(int s, double x, double z, double vx, double vy, double vz)
     MAG_CK(cudaMemcpy(S.id.p + o, &pid, 4, cudaMemcpyHostToDevice));
     S.n_slots += 1;
     S.next_id += 1;
+    upload_slots(s);
+    sort_due = true;
 }
 
 // Pic::run_initscript (src/pic.cpp:241-328) plus one r-z loader
@@ -597,23 +652,28 @@ PushArgs Sim::push_args(int s, bool init)
     a.vz = S.vz.p;
     a.id = S.id.p;
     a.n = S.n_slots;
+    a.n_dev = &S.cnt.p->slots;
     a.nx = nx;
     a.nz = nz;
-    a.xmaxg = (float)((xmax - x0) / dx);
-    a.zmaxg = (float)((zmax - z0) / dz);
+    a.xmaxf = (uint32_t)std::llrint((xmax - x0) / dx * (double)(1u << kFracBits));
+    a.zmaxf = (uint32_t)std::llrint((zmax - z0) / dz * (double)(1u << kFracBits));
     a.periodic = p.boundary == BND_PERIODIC ? 1 : 0;
     a.check_mask = check_mask ? 1 : 0;
     a.mask = d_mask.p;
     a.emode = emode;
     a.Exf = Exf.p;
     a.Ezf = Ezf.p;
-    a.Exf_rf = Exf_rf.p;
-    a.Ezf_rf = Ezf_rf.p;
+    a.Exf2 = Exf2.p;
+    a.Ezf2 = Ezf2.p;
     a.extern_ez = (float)p.extern_field;
-    a.rf_omega = p.rf_omega;
-    a.rf_amp = p.rf_amplitude;
-    a.rf_U0 = p.rf_U0;
-    a.dt = S.prm.dt;
+    a.step = S.niter;
+    {  // Fields::E phase at t = niter * dt, in FP64 as the reference (fields.hpp:135-145)
+        const double t = (double)S.niter * S.prm.dt;
+        double ph = p.rf_omega * t;
+        const double y = 10000000 * kPi;
+        if (!(ph >= 0.0 && ph <= y)) ph = ph - y * (double)(int)(ph / y) + (ph < 0 ? y : 0);
+        a.phase = (float)(p.rf_amplitude * std::cos(ph) + p.rf_U0);
+    }
     const double q = S.prm.charge, m = S.prm.mass, dt = S.prm.dt;
     const double rot = init ? -0.5 * q * dt / (2.0 * m) : q * dt / (2.0 * m);
     a.q_dt_2m = (float)rot;
@@ -643,11 +703,25 @@ PushArgs Sim::push_args(int s, bool init)
     a.cz = (float)(dt / dz);
     a.rho = p.selfconsistent ? S.rho.p : nullptr;
     a.coll_threshold = init ? 0u : S.threshold;
+    a.coll_mode = init ? 0 : coll_mode(s);
     a.cand = S.cand.p;
+    a.mcc = S.mcc.p;
     a.seed = seed;
     a.species = (uint32_t)s;
     a.cnt = S.cnt.p;
+    a.close_step = a.coll_mode == 2 ? 0 : 1;
     return a;
+}
+
+// 0: no collisions, 1: inline in the particle kernel (every target with a
+// non-zero rate is a Maxwellian background), 2: candidate list + k_collide
+int Sim::coll_mode(int s) const
+{
+    const SpeciesState& S = sp[s];
+    if (S.threshold == 0) return 0;
+    for (size_t t = 0; t < sp.size(); ++t)
+        if (S.rates[t] > 0.0 && sp[t].n_slots > 0) return 2;
+    return 1;
 }
 
 CollideArgs Sim::collide_args(int s)
@@ -660,30 +734,62 @@ CollideArgs Sim::collide_args(int s)
     a.id = S.id.p;
     a.cand = S.cand.p;
     a.cnt = S.cnt.p;
-    a.mass = S.prm.mass;
-    a.inv_lifetime = std::isinf(S.lifetime) ? 0.0 : 1.0 / S.lifetime;
-    a.nsp = (int)sp.size();
-    int pos = S.inter_off;
+    a.mcc = S.mcc.p;
     for (size_t t = 0; t < sp.size(); ++t) {
-        a.rates[t] = S.rates[t];
-        a.t_mass[t] = sp[t].prm.mass;
-        a.t_density[t] = sp[t].prm.density;
-        a.t_sigma_v[t] = sp[t].v_max * std::sqrt(0.5);
         a.t_has_slots[t] = sp[t].n_slots > 0 ? 1 : 0;
         a.t_x[t] = sp[t].x.p;
         a.t_vx[t] = sp[t].vx.p;
         a.t_vy[t] = sp[t].vy.p;
         a.t_vz[t] = sp[t].vz.p;
         a.t_n[t] = sp[t].n_slots;
-        a.inter_begin[t] = pos;
-        pos += (int)S.by_target[t].size();
-        a.inter_end[t] = pos;
     }
-    a.inter = d_inter.p;
-    a.tables = d_tables.p;
     a.seed = seed;
     a.species = (uint32_t)s;
+    a.step = S.niter;
     return a;
+}
+
+// Counting sort by cell into the double buffers, then swap (compacts removed particles).
+void Sim::sort_species(int s)
+{
+    SpeciesState& S = sp[s];
+    if (S.n_slots == 0) return;
+    if (!S.bx.p) {
+        S.bx.alloc(S.cap);
+        S.bz.alloc(S.cap);
+        S.bvx.alloc(S.cap);
+        S.bvy.alloc(S.cap);
+        S.bvz.alloc(S.cap);
+        S.bid.alloc(S.cap);
+    }
+    SortArgs a{};
+    a.x = S.x.p;
+    a.z = S.z.p;
+    a.vx = S.vx.p;
+    a.vy = S.vy.p;
+    a.vz = S.vz.p;
+    a.id = S.id.p;
+    a.ox = S.bx.p;
+    a.oz = S.bz.p;
+    a.ovx = S.bvx.p;
+    a.ovy = S.bvy.p;
+    a.ovz = S.bvz.p;
+    a.oid = S.bid.p;
+    a.n = S.n_slots;
+    a.nx = nx;
+    a.nz = nz;
+    a.ncells = (long long)(nx - 1) * (nz - 1);
+    a.count = sort_count.p;
+    a.offset = sort_offset.p;
+    a.blocksum = sort_blocksum.p;
+    a.cnt = S.cnt.p;
+    launches += launch_sort(a, S.n_slots, stream);
+    std::swap(S.x, S.bx);
+    std::swap(S.z, S.bz);
+    std::swap(S.vx, S.bvx);
+    std::swap(S.vy, S.bvy);
+    std::swap(S.vz, S.bvz);
+    std::swap(S.id, S.bid);
 }
 
 // One Pic::advance (src/pic.cpp:330-358).  With ev != nullptr, events
@@ -691,6 +797,11 @@ CollideArgs Sim::collide_args(int s)
 // kernels and after the collision kernels.
 void Sim::step(cudaEvent_t* ev)
 {
+    if (sort_interval > 0 && (sort_due || steps_done % (uint64_t)sort_interval == 0)) {
+        for (size_t s = 0; s < sp.size(); ++s) sort_species((int)s);
+        sort_due = false;
+    }
+    ++steps_done;
     if (ev) MAG_CK(cudaEventRecord(ev[0], stream));
     if (p.selfconsistent) solve(false, rho_override ? 2 : 1, true, false);
     rho_override = false;
@@ -704,13 +815,12 @@ void Sim::step(cudaEvent_t* ev)
     if (ev) MAG_CK(cudaEventRecord(ev[2], stream));
     for (size_t s = 0; s < sp.size(); ++s) {
         SpeciesState& S = sp[s];
-        if (S.n_slots == 0) {
-            S.host_niter++;
-            continue;
+        if (S.n_slots > 0 && coll_mode((int)s) == 2) {
+            const double expect = (double)S.n_slots * S.prob;
+            const int grid = (int)std::min<double>(304.0, std::ceil(4.0 * expect / 128.0) + 1.0);
+            launches += launch_collide(collide_args((int)s), grid, stream);
         }
-        const double expect = (double)S.n_slots * S.prob;
-        const int grid = (int)std::min<double>(304.0, std::ceil(4.0 * expect / 128.0) + 1.0);
-        launches += launch_collide(collide_args((int)s), grid, stream);
+        S.niter++;
     }
     if (ev) MAG_CK(cudaEventRecord(ev[3], stream));
 }
@@ -820,6 +930,7 @@ void Sim::set_field(int which, const double* in)
         throw Error(-1, "only u, uRF and rho can be set");
     if (which == 0) launches += launch_faces(u64.p, nx, nz, dx, dz, Exf.p, Ezf.p, stream);
     if (which == 1) launches += launch_faces(urf64.p, nx, nz, dx, dz, Exf_rf.p, Ezf_rf.p, stream);
+    if (which <= 1) refresh_rf_pairs();
     MAG_CK(cudaStreamSynchronize(stream));
 }
 
@@ -828,8 +939,8 @@ void Sim::get_particles(int s, int64_t cap, double* x, double* z, double* vx, do
 {
     SpeciesState& S = sp[s];
     const int64_t n = S.n_slots;
-    std::vector<float> hx(n), hz(n), hvx(n), hvy(n), hvz(n);
-    std::vector<uint32_t> hid(n);
+    std::vector<uint32_t> hx(n), hz(n), hid(n);
+    std::vector<float> hvx(n), hvy(n), hvz(n);
     S.x.download(hx.data(), n, stream);
     S.z.download(hz.data(), n, stream);
     S.vx.download(hvx.data(), n, stream);
@@ -838,10 +949,11 @@ void Sim::get_particles(int s, int64_t cap, double* x, double* z, double* vx, do
     S.id.download(hid.data(), n, stream);
     MAG_CK(cudaStreamSynchronize(stream));
     int64_t m = 0;
+    const double inv = 1.0 / (double)(1u << kFracBits);
     for (int64_t k = 0; k < n && m < cap; ++k) {
-        if (!(hx[k] >= 0.f)) continue;
-        if (x) x[m] = x0 + (double)hx[k] * dx;
-        if (z) z[m] = z0 + (double)hz[k] * dz;
+        if (hx[k] == kDead) continue;
+        if (x) x[m] = x0 + (double)hx[k] * inv * dx;
+        if (z) z[m] = z0 + (double)hz[k] * inv * dz;
         if (vx) vx[m] = hvx[k];
         if (vy) vy[m] = hvy[k];
         if (vz) vz[m] = hvz[k];
@@ -857,12 +969,14 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     SpeciesState& S = sp[s];
     MAG_CK(cudaStreamSynchronize(stream));
     S.n_slots = 0;
-    if (S.host_niter) MAG_CK(cudaMemcpy(&S.cnt.p->niter, &S.host_niter, sizeof(uint64_t), cudaMemcpyHostToDevice));
     ensure_capacity(s, std::max<int64_t>(n, 1));
-    std::vector<float> hx(n), hz(n), hvx(n), hvy(n), hvz(n);
+    std::vector<uint32_t> hx(n), hz(n);
+    std::vector<float> hvx(n), hvy(n), hvz(n);
+    const double one = (double)(1u << kFracBits);
     for (int64_t k = 0; k < n; ++k) {
-        hx[k] = (float)((x[k] - x0) / dx);
-        hz[k] = (float)((z[k] - z0) / dz);
+        const bool inside = x[k] >= x0 && x[k] <= xmax && z[k] >= z0 && z[k] <= zmax;
+        hx[k] = inside ? (uint32_t)std::llrint((x[k] - x0) / dx * one) : kDead;
+        hz[k] = inside ? (uint32_t)std::llrint((z[k] - z0) / dz * one) : 0u;
         hvx[k] = (float)vx[k];
         hvy[k] = (float)vy[k];
         hvz[k] = (float)vz[k];
@@ -876,6 +990,8 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     MAG_CK(cudaStreamSynchronize(stream));
     S.n_slots = n;
     S.next_id = (uint32_t)n;
+    upload_slots(s);
+    sort_due = true;
 }
 
 void Sim::get_rho_fixed(int s, int64_t* out)
@@ -893,11 +1009,7 @@ Counters Sim::counters(int s)
     return c;
 }
 
-uint64_t Sim::niter(int s)
-{
-    if (sp[s].n_slots == 0) return sp[s].host_niter;
-    return counters(s).niter;
-}
+uint64_t Sim::niter(int s) { return sp[s].niter; }
 
 void Sim::energy(int s, double& sum_v2, unsigned long long& n)
 {

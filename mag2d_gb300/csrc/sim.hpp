@@ -68,7 +68,7 @@ struct DevArray {
 struct SimOptions {
     int device = 0;
     uint64_t seed = 1;
-    int sort_interval = 0;
+    int sort_interval = 0;  // 0: default (20), < 0: never
     double poisson_tol = 1e-12;
     int poisson_max_iter = 200;
     int64_t capacity_hint = 0;
@@ -80,14 +80,17 @@ struct SpeciesState {
     uint32_t threshold = 0;
     std::vector<double> rates;              // rates_by_species
     std::vector<std::vector<int>> by_target;  // interaction indices per target species
-    // device particles
-    DevArray<float> x, z, vx, vy, vz;
-    DevArray<uint32_t> id, cand;
+    // device particles (x, z fixed point, see device.hpp) and their sort double buffers
+    DevArray<uint32_t> x, z, id, cand;
+    DevArray<float> vx, vy, vz;
+    DevArray<uint32_t> bx, bz, bid;
+    DevArray<float> bvx, bvy, bvz;
+    DevArray<MccSpecies> mcc;
     int64_t cap = 0, n_slots = 0;
     uint32_t next_id = 0;
     DevArray<unsigned long long> rho;  // fixed-point charge grid
     DevArray<Counters> cnt;
-    uint64_t host_niter = 0;           // step counter of species without particle storage
+    uint64_t niter = 0;                // steps advanced (Species::advance niter++, particles.hpp:347)
     int inter_off = 0;                 // first entry of this species in the device interaction list
 };
 
@@ -125,6 +128,9 @@ public:
     int poisson_max_iter = 200;
     bool rho_override = false;
     SolveStatus last_solve{};
+    int sort_interval = 20;
+    uint64_t steps_done = 0;
+    bool sort_due = true;
 
     void get_field(int which, double* out);
     void set_field(int which, const double* in);
@@ -146,6 +152,8 @@ private:
     DevArray<int8_t> d_mask;
     DevArray<double> d_volt, u64, urf64, b64, rho64, red;
     DevArray<float> Exf, Ezf, Exf_rf, Ezf_rf, d_Br, d_Bz;
+    DevArray<float2> Exf2, Ezf2;
+    DevArray<uint32_t> sort_count, sort_offset, sort_blocksum;
     int bnx = 0, bnz = 0;
     double b_x0 = 0, b_z0 = 0, b_dx = 1, b_dz = 1;
     DevArray<SolveStatus> d_status;
@@ -167,6 +175,10 @@ private:
     PushArgs push_args(int s, bool init);
     CollideArgs collide_args(int s);
     void step(cudaEvent_t* ev = nullptr);
+    void sort_species(int s);
+    void refresh_rf_pairs();
+    void upload_slots(int s);
+    int coll_mode(int s) const;
 };
 
 }  // namespace mag

@@ -1,0 +1,139 @@
+// Counting sort of a species' particles by cell, with compaction of removed
+// particles (north-star layout: "SoA, counting-sorted by cell every few
+// steps").  After a sort, consecutive threads of the particle kernel touch the
+// same few cells, so the field gather and the deposit atomics hit L1/L2
+// instead of scattering over the grid.  The order inside a cell is not
+// deterministic; nothing depends on it (random streams are keyed by particle
+// id, the deposit is an integer sum).
+//
+//   k_cell_count   count[cell] += 1 per live particle
+//   k_scan_*       offset = exclusive prefix sum of count (3-phase block scan)
+//   k_cell_scatter position = offset[cell] + (atomicSub(count[cell]) - 1);
+//                  count returns to zero for the next sort
+#include "device.hpp"
+#include "kernels.hpp"
+
+namespace mag {
+
+namespace {
+
+__device__ __forceinline__ int cell_of(uint32_t x, uint32_t z, int nx, int nz)
+{
+    const int i = min((int)(x >> kFracBits), nx - 2);
+    const int j = min((int)(z >> kFracBits), nz - 2);
+    return i * (nz - 1) + j;
+}
+
+__global__ void k_cell_count(const SortArgs a)
+{
+    const long long n = min((long long)a.n, (long long)a.cnt->slots);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const uint32_t x = a.x[k];
+        if (x == kDead) continue;
+        atomicAdd(&a.count[cell_of(x, a.z[k], a.nx, a.nz)], 1u);
+    }
+}
+
+// exclusive scan of one 1024-element chunk per block; returns the block total
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t& excl)
+{
+    __shared__ uint32_t warp_tot[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0u;
+        uint32_t ti = t;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= o) ti += u;
+        }
+        warp_tot[lane] = ti - t;  // exclusive warp offsets
+    }
+    __syncthreads();
+    excl = warp_tot[w] + inc - v;
+    // block total = last thread's inclusive value
+    __shared__ uint32_t total;
+    if (threadIdx.x == blockDim.x - 1) total = excl + v;
+    __syncthreads();
+    const uint32_t t = total;
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_local(const SortArgs a)
+{
+    const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
+    const uint32_t v = i < a.ncells ? a.count[i] : 0u;
+    uint32_t excl;
+    const uint32_t tot = block_exclusive_scan(v, excl);
+    if (i < a.ncells) a.offset[i] = excl;
+    if (threadIdx.x == 0) a.blocksum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(const SortArgs a, int nblocks)
+{
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nblocks; base += 1024) {
+        const int i = base + threadIdx.x;
+        const uint32_t v = i < nblocks ? a.blocksum[i] : 0u;
+        uint32_t excl;
+        const uint32_t tot = block_exclusive_scan(v, excl);
+        if (i < nblocks) a.blocksum[i] = excl + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.offset[a.ncells] = carry;
+        a.cnt->slots = carry;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_add(const SortArgs a)
+{
+    const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
+    if (i < a.ncells) a.offset[i] += a.blocksum[blockIdx.x];
+}
+
+__global__ void k_cell_scatter(const SortArgs a, long long n_src)
+{
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n_src;
+         k += (long long)gridDim.x * blockDim.x) {
+        const uint32_t x = a.x[k];
+        if (x == kDead) continue;
+        const uint32_t z = a.z[k];
+        const int c = cell_of(x, z, a.nx, a.nz);
+        const uint32_t pos = a.offset[c] + atomicSub(&a.count[c], 1u) - 1u;
+        a.ox[pos] = x;
+        a.oz[pos] = z;
+        a.ovx[pos] = a.vx[k];
+        a.ovy[pos] = a.vy[k];
+        a.ovz[pos] = a.vz[k];
+        a.oid[pos] = a.id[k];
+    }
+}
+
+}  // namespace
+
+int launch_sort(const SortArgs& a, long long n_src, cudaStream_t s)
+{
+    if (a.n == 0) return 0;
+    const int grid = (int)std::min<long long>((a.n + 255) / 256, 152 * 16);
+    k_cell_count<<<grid, 256, 0, s>>>(a);
+    const int nb = (int)((a.ncells + 1023) / 1024);
+    k_scan_local<<<nb, 1024, 0, s>>>(a);
+    k_scan_top<<<1, 1024, 0, s>>>(a, nb);
+    k_scan_add<<<nb, 1024, 0, s>>>(a);
+    k_cell_scatter<<<grid, 256, 0, s>>>(a, n_src);
+    return 5;
+}
+
+}  // namespace mag

@@ -155,8 +155,9 @@ class Pic:
     """Pic<D> of the reference, on the GPU."""
 
     def __init__(self, config, species_conf, initscript=None, *, seed: int = 1, device: int = 0,
-                 poisson_tol: float = 0.0, poisson_max_iter: int = 0, capacity_hint: int = 0):
-        opts = MagOpts(device=device, seed=seed, sort_interval=0, poisson_tol=poisson_tol,
+                 poisson_tol: float = 0.0, poisson_max_iter: int = 0, capacity_hint: int = 0,
+                 sort_interval: int = 0):
+        opts = MagOpts(device=device, seed=seed, sort_interval=sort_interval, poisson_tol=poisson_tol,
                        poisson_max_iter=poisson_max_iter, capacity_hint=capacity_hint)
         h = ctypes.c_void_p()
         ini = str(initscript).encode() if initscript else None

@@ -1288,20 +1288,18 @@ int orc_rng(orc_sim* s, int kind, int n, double arg, double* out)
 
 int64_t orc_collisions(orc_sim* s, int sp) { return s->sp[sp]->ncoll; }
 
-int64_t orc_deposit_fixed(int nx, int nz, int64_t n, const float* xg, const float* zg, const uint8_t* alive,
+int64_t orc_deposit_fixed(int nx, int nz, int64_t n, const uint32_t* xf, const uint32_t* zf, const uint8_t* alive,
                           int64_t* acc)
 {
     const int64_t one = (int64_t)1 << 20;
     int64_t cnt = 0;
     for (int64_t k = 0; k < n; ++k) {
         if (alive && !alive[k]) continue;
-        const float x = xg[k], z = zg[k];
-        int i = (int)floorf(x), j = (int)floorf(z);
-        if (i > nx - 2) i = nx - 2;  // a particle exactly on the last node line
+        int i = (int)(xf[k] >> 20), j = (int)(zf[k] >> 20);
+        if (i > nx - 2) i = nx - 2;  // a particle on the last node line
         if (j > nz - 2) j = nz - 2;
-        if (i < 0 || j < 0) continue;
-        const int64_t U = (int64_t)floorf((x - (float)i) * 1048576.0f);
-        const int64_t V = (int64_t)floorf((z - (float)j) * 1048576.0f);
+        const int64_t U = (int64_t)xf[k] - ((int64_t)i << 20);
+        const int64_t V = (int64_t)zf[k] - ((int64_t)j << 20);
         const size_t b = (size_t)i * nz + j;
         acc[b] += (one - U) * (one - V);
         acc[b + nz] += U * (one - V);

@@ -75,12 +75,14 @@ int orc_rng(orc_sim* s, int kind, int n, double arg, double* out);
 /* Collision counter: number of scatter() calls per species since creation */
 int64_t orc_collisions(orc_sim* s, int sp);
 
-/* Fixed-point CIC deposit (Field2D.hpp:45-62 with quantised weights): each
- * particle at grid coordinates (xg, zg) adds (2^20-U)(2^20-V), U(2^20-V),
- * (2^20-U)V, UV to the four surrounding nodes, U = floor(frac(xg) * 2^20).
- * acc is nx*nz int64 (row-major, z fastest), accumulated into.  Particles with
- * alive[i]==0 are skipped.  Returns the number deposited. */
-int64_t orc_deposit_fixed(int nx, int nz, int64_t n, const float* xg, const float* zg,
+/* Fixed-point CIC deposit (Field2D.hpp:45-62 with quantised weights): a
+ * particle at fixed-point grid position (xf, zf) -- cells times 2^20 -- in
+ * cell i = xf >> 20, j = zf >> 20 (clamped to the last cell) adds
+ * (2^20-U)(2^20-V), U(2^20-V), (2^20-U)V, UV to the four corners of the cell,
+ * U = xf - i*2^20, V = zf - j*2^20.  acc is nx*nz int64 (row-major, z
+ * fastest), accumulated into.  Particles with alive[i]==0 are skipped.
+ * Returns the number deposited. */
+int64_t orc_deposit_fixed(int nx, int nz, int64_t n, const uint32_t* xf, const uint32_t* zf,
                           const uint8_t* alive, int64_t* acc);
 
 #ifdef __cplusplus

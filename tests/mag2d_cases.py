@@ -285,11 +285,17 @@ class Port:
         return int(self.L.orc_collisions(self.h, sp))
 
 
-def deposit_fixed(nx: int, nz: int, xg: np.ndarray, zg: np.ndarray, alive=None) -> np.ndarray:
-    """Fixed-point CIC deposit of the oracle (int64, units of 2^-40 per particle)."""
+def to_fixed(v: np.ndarray) -> np.ndarray:
+    """Grid-unit positions to the library's fixed point (cells times 2^20, round to nearest)."""
+    return np.rint(np.asarray(v, dtype=np.float64) * 1048576.0).astype(np.uint32)
+
+
+def deposit_fixed(nx: int, nz: int, xf: np.ndarray, zf: np.ndarray, alive=None) -> np.ndarray:
+    """Fixed-point CIC deposit of the oracle (int64, units of 2^-40 per particle)
+    of particles at fixed-point positions xf, zf (cells times 2^20)."""
     L = load_port()
-    xg = np.ascontiguousarray(xg, dtype=np.float32)
-    zg = np.ascontiguousarray(zg, dtype=np.float32)
+    xg = np.ascontiguousarray(xf, dtype=np.uint32)
+    zg = np.ascontiguousarray(zf, dtype=np.uint32)
     acc = np.zeros((nx, nz), dtype=np.int64)
     al = None if alive is None else np.ascontiguousarray(alive, dtype=np.uint8)
     L.orc_deposit_fixed(nx, nz, len(xg), xg.ctypes.data, zg.ctypes.data,

@@ -78,7 +78,7 @@ def test_poisson_matches_direct_solve(m, tmp_path, geom):
 # ---------------------------------------------------------------------------
 def test_deposit_bit_exact(m, tmp_path):
     from cases import penning_rz
-    from mag2d_cases import deposit_fixed
+    from mag2d_cases import deposit_fixed, to_fixed
 
     cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=50_000)
     pic = m.Pic(cpath, spath, seed=1)
@@ -86,8 +86,8 @@ def test_deposit_bit_exact(m, tmp_path):
     sp.set_particles(*parts)
     pic.deposit()
     got = sp.rho_fixed()
-    xg = np.float32((parts[0] - pic.x_min) / pic.dx)
-    zg = np.float32((parts[1] - pic.z_min) / pic.dz)
+    xg = to_fixed((parts[0] - pic.x_min) / pic.dx)
+    zg = to_fixed((parts[1] - pic.z_min) / pic.dz)
     want = deposit_fixed(pic.shape[0], pic.shape[1], xg, zg)
     assert np.array_equal(got, want)
     # every particle contributes exactly 2^40
@@ -185,4 +185,69 @@ def test_mcc_statistics_multipole(m, tmp_path):
     eo = 0.5 * 3 * AMU * (lo[:, 3] ** 2 + lo[:, 4] ** 2 + lo[:, 5] ** 2) / QE
     _, p = _ks_2samp(eg, eo)
     assert p > 0.01, p
+    pic.close()
+
+
+def test_sort_does_not_change_results(m, tmp_path):
+    """Random streams are keyed by particle id and the deposit is an integer sum,
+    so sorting by cell every step or never gives bit-identical particles."""
+    from cases import penning_rz
+
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=5000)
+    out = []
+    for si in (1, -1):
+        pic = m.Pic(cpath, spath, seed=5, sort_interval=si)
+        pic.speclist[0].set_particles(*parts)
+        pic.advance_init()
+        pic.advance(200)
+        g = pic.speclist[0].particles()
+        order = np.argsort(g["id"])
+        out.append({k: v[order] for k, v in g.items()})
+        pic.close()
+    for k in ("id", "x", "z", "vx", "vy", "vz"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_mcc_candidate_list_path(m, tmp_path):
+    """Charge exchange with a neutral background and Coulomb collisions with a
+    second ion species that holds particles (partner = random live particle):
+    collision counts against the oracle within 3 sigma."""
+    from mag2d_cases import AMU, QE, write_config, write_species_conf
+
+    cfg = dict(coord="CARTESIAN", boundary="PERIODIC", geometry="EMPTY", x_max=1e-2, z_max=1e-2, x_sampl=9,
+               z_sampl=9, selfconsistent=0, rf=0, extern_field=50.0, do_plot=0)
+    sp = [dict(name="AR", type="NEUTRAL", mass=40 * AMU, density=5e21, temperature=300.0),
+          dict(name="ARP", type="ION", mass=40 * AMU, charge=QE, dt=1e-8, density=1e16, temperature=3000.0,
+               emax=5.0),
+          dict(name="HEP", type="ION", mass=4 * AMU, charge=QE, dt=1e-8, density=1e16, temperature=3000.0,
+               emax=5.0)]
+    inter = [dict(name="cx", type="CX", primary="ARP", secondary="AR", rate=5e-16),
+             dict(name="coul", type="COULOMB", primary="ARP", secondary="HEP"),
+             dict(name="hel", type="ELASTIC", primary="HEP", secondary="AR", rate=3e-16)]
+    cpath = write_config(cfg, tmp_path / "c.txt")
+    spath = write_species_conf(sp, inter, tmp_path / "s.txt")
+    rng = np.random.default_rng(4)
+    n, steps = 20000, 50
+    vth = np.sqrt(1.380662e-23 * 3000.0 / (40 * AMU))
+    def parts(mass):
+        v = np.sqrt(1.380662e-23 * 3000.0 / mass)
+        return (1e-2 * rng.random(n), 1e-2 * rng.random(n), v * rng.standard_normal(n), v * rng.standard_normal(n),
+                v * rng.standard_normal(n))
+    pa, ph = parts(40 * AMU), parts(4 * AMU)
+    pic = m.Pic(cpath, spath, seed=9)
+    pic.speclist[1].set_particles(*pa)
+    pic.speclist[2].set_particles(*ph)
+    pic.advance_init()
+    pic.advance(steps)
+    d1, d2 = pic.speclist[1].diag(), pic.speclist[2].diag()
+    port = _port_for(m, cfg, sp, inter, cpath, seed=9)
+    port.set_particles(1, *pa)
+    port.set_particles(2, *ph)
+    port.advance_init()
+    port.advance(steps)
+    for s, d in ((1, d1), (2, d2)):
+        cand = d["collisions"] + d["null_collisions"]
+        ref = port.collisions(s)
+        assert ref > 100
+        assert abs(cand - ref) < 3 * math.sqrt(2 * ref), (s, cand, ref)
     pic.close()

@@ -156,17 +156,18 @@ def test_poisson_solve_independent_check(fname):
 def test_fixed_point_deposit_properties(port_lib):
     """The quantised CIC deposit conserves charge exactly (2^40 per particle)
     and stays within 2^-20 per weight of the reference's FP64 weights."""
-    from mag2d_cases import deposit_fixed
+    from mag2d_cases import deposit_fixed, to_fixed
 
     rng = np.random.default_rng(1)
     n, nx, nz = 5000, 17, 33
-    xg = (rng.random(n) * (nx - 1)).astype(np.float32)
-    zg = (rng.random(n) * (nz - 1)).astype(np.float32)
-    acc = deposit_fixed(nx, nz, xg, zg)
+    xf = to_fixed(rng.random(n) * (nx - 1))
+    zf = to_fixed(rng.random(n) * (nz - 1))
+    xg, zg = xf / 2.0 ** 20, zf / 2.0 ** 20
+    acc = deposit_fixed(nx, nz, xf, zf)
     assert acc.sum() == n << 40
     ref = np.zeros((nx, nz))
-    i, j = np.floor(xg).astype(int), np.floor(zg).astype(int)
-    u, v = xg.astype(np.float64) - i, zg.astype(np.float64) - j
+    i, j = np.minimum(np.floor(xg).astype(int), nx - 2), np.minimum(np.floor(zg).astype(int), nz - 2)
+    u, v = xg - i, zg - j
     np.add.at(ref, (i, j), (1 - u) * (1 - v))
     np.add.at(ref, (i + 1, j), u * (1 - v))
     np.add.at(ref, (i, j + 1), (1 - u) * v)
@@ -178,4 +179,4 @@ def test_fixed_point_deposit_properties(port_lib):
     assert np.all(np.abs(acc / 2.0 ** 40 - ref) <= counts * 2.0 ** -19)
     # order independence: any permutation gives identical integers
     perm = rng.permutation(n)
-    assert np.array_equal(deposit_fixed(nx, nz, xg[perm], zg[perm]), acc)
+    assert np.array_equal(deposit_fixed(nx, nz, xf[perm], zf[perm]), acc)
