@@ -10,6 +10,8 @@
 //   k_scan_*       offset = exclusive prefix sum of count (3-phase block scan)
 //   k_cell_scatter position = offset[cell] + (atomicSub(count[cell]) - 1);
 //                  count returns to zero for the next sort
+// Invariant kept for all other kernels: every slot below the host's slot
+// count holds a live particle or the removed marker.
 #include "device.hpp"
 #include "kernels.hpp"
 
@@ -26,7 +28,7 @@ __device__ __forceinline__ int cell_of(uint32_t x, uint32_t z, int nx, int nz)
 
 __global__ void k_cell_count(const SortArgs a)
 {
-    const long long n = min((long long)a.n, (long long)a.cnt->slots);
+    const long long n = a.n;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
         const uint32_t x = a.x[k];
         if (x == kDead) continue;
@@ -103,10 +105,14 @@ __global__ void __launch_bounds__(1024) k_scan_add(const SortArgs a)
     if (i < a.ncells) a.offset[i] += a.blocksum[blockIdx.x];
 }
 
+// Every slot k >= total of the destination is marked removed, so all slots
+// below the host's slot count are either live or removed in both buffers.
 __global__ void k_cell_scatter(const SortArgs a, long long n_src)
 {
+    const long long total = a.offset[a.ncells];
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n_src;
          k += (long long)gridDim.x * blockDim.x) {
+        if (k >= total) a.ox[k] = kDead;
         const uint32_t x = a.x[k];
         if (x == kDead) continue;
         const uint32_t z = a.z[k];
