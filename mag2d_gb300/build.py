@@ -74,6 +74,15 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    drv_src = CSRC / "driver" / "plasma2d_gpu.cpp"
+    drv = LIBDIR / "plasma2d_gpu"
+    if not drv.exists() or drv.stat().st_mtime < max(drv_src.stat().st_mtime, LIB.stat().st_mtime):
+        cxx = os.environ.get("CXX", "g++")
+        cmd = [cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(drv_src), "-L", str(LIBDIR),
+               "-lmag2d_gpu", "-Wl,-rpath,$ORIGIN", "-o", str(drv)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

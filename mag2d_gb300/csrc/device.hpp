@@ -96,7 +96,7 @@ struct PushArgs {
     float cx, cz;                  // dt/dx, dt/dz (cells per m/s)
     unsigned long long* rho;       // fixed-point deposit (nx*nz) or null
     uint32_t coll_threshold;       // collision probability * 2^32 (0: no test)
-    int coll_mode;                 // 0 none, 1 inline scatter (Maxwellian targets), 2 candidate list
+    int coll_mode;                 // 0 none, 2 candidate list (k_collide)
     uint32_t* cand;
     const MccSpecies* mcc;
     uint64_t seed;

@@ -217,23 +217,4 @@ __device__ inline int mcc_collide(const MccSpecies& m, int s, Stream& rs, double
     return MCC_HIT;
 }
 
-// Inline scatter against a slot-less (Maxwellian) target: the whole of
-// scatter() for one particle.  noinline keeps its FP64 registers out of the
-// particle kernel's register budget.
-static __device__ __noinline__ int mcc_scatter_maxwell(const MccSpecies* __restrict__ m, uint64_t seed, uint32_t sp,
-                                                uint32_t id, uint64_t step, float& fvx, float& fvy, float& fvz)
-{
-    Stream rs(seed, sp, id, TAG_COLLIDE, step);
-    const int s = mcc_pick_target(*m, rs);
-    const double sig = m->t_sigma_v[s];
-    const double vr2 = rs.normalf() * sig, vz2 = rs.normalf() * sig, vt2 = rs.normalf() * sig;
-    double vx = fvx, vy = fvy, vz = fvz, pvx, pvy, pvz;
-    bool pu;
-    const int r = mcc_collide(*m, s, rs, vx, vy, vz, vr2, vz2, vt2, pu, pvx, pvy, pvz);
-    fvx = (float)vx;
-    fvy = (float)vy;
-    fvz = (float)vz;
-    return r;
-}
-
 }  // namespace mag

@@ -1,12 +1,10 @@
-// Particle step kernel: field gather, Boris push, collision test (and, against
-// Maxwellian background targets, the collision itself), boundary, mask test
-// and fixed-point charge deposit, fused into one pass over the SoA.
+// Particle step kernel: field gather, Boris push, collision test, boundary,
+// mask test and fixed-point charge deposit, fused into one pass over the SoA.
 //
 // Replaces, per particle, the loop bodies of
 //   Species<CYLINDRICAL>::advance_boris   src/particles.cpp:539-621
 //   Species<CARTESIAN>::advance_boris     src/particles.cpp:924-995
 //   Fields::E / Fields::B                 src/fields.hpp:124-177
-//   BaseSpecies::scatter                  src/particles.cpp:208-365 (Maxwellian partners)
 //   Species::advance_boundary             src/particles.hpp:370-411
 //   t_grid::is_free                       src/fields.hpp:94-101
 //   Field2D::accumulate                   src/Field2D.hpp:45-62
@@ -19,7 +17,6 @@
 // particles are sorted by cell.
 #include "device.hpp"
 #include "kernels.hpp"
-#include "mcc_device.cuh"
 #include "philox.hpp"
 
 namespace mag {
@@ -165,127 +162,157 @@ __device__ __forceinline__ void close_step_if_last(Counters* c, unsigned long lo
     }
 }
 
+// One particle of the step.  Returns the new state through the references;
+// alive / removed / candidate flags drive the counters.
 template <int COORD, int EMODE>
-__global__ void __launch_bounds__(256, 8) k_push(const PushArgs a)
+__device__ __forceinline__ void step_particle(const PushArgs& a, int64_t k, uint32_t& x, uint32_t& z, float& vx,
+                                              float& vy, float& vz, bool& alive, bool& cand)
 {
-    __shared__ unsigned long long s_coll, s_null;
-    __shared__ long long s_n;
-    if (threadIdx.x == 0) {
-        s_coll = 0;
-        s_null = 0;
-        s_n = a.n_dev ? (long long)min((unsigned long long)a.n, *a.n_dev) : a.n;
+    float ex, ez;
+    gather_E<EMODE>(a, x, z, a.phase, ex, ez);
+    float tx, ty, tz, sx, sy, sz;
+    boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
+    // half acceleration, Boris rotation (Birdsall & Langdon), half acceleration
+    vx += ex * a.hq;
+    vz += ez * a.hq;
+    rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
+    vx += ex * a.hq;
+    vz += ez * a.hq;
+    int64_t px, pz;
+    const float dz = vz * a.cz;
+    if (COORD == 1) {
+        // push in the local Cartesian frame, map back to r and rotate v (Birdsall p. 338);
+        // dr = r' - r = (2 r a + a^2 + b^2) / (r' + r) keeps the fixed-point r exact
+        const float r = (float)(x >> kFracBits) + frac(x);
+        const float ax = vx * a.cx, by = vy * a.cx;
+        const float x2 = r + ax;
+        const float rn = sqrtf(x2 * x2 + by * by);
+        const float den = rn + r;
+        const float dr = den > 0.f ? (ax * (r + x2) + by * by) / den : 0.f;
+        float sa = 0.f, ca = 1.f;
+        if (rn != 0.f) {
+            const float ir = 1.f / rn;
+            sa = by * ir;
+            ca = x2 * ir;
+        }
+        const float t0 = vx;
+        vx = ca * vx + sa * vy;
+        vy = -sa * t0 + ca * vy;
+        px = isfinite(dr) ? (int64_t)x + __float2ll_rn(dr * kOne) : -1;
+    } else {
+        const float dx = vx * a.cx;
+        px = isfinite(dx) ? (int64_t)x + __float2ll_rn(dx * kOne) : -1;
     }
-    __syncthreads();
-    const uint64_t step = a.step;
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in_range = k < s_n;
-    uint32_t x = in_range ? a.x[k] : kDead;
-    const bool was_alive = x != kDead;
-    bool alive = was_alive;
-    bool cand = false;
-    if (was_alive) {
-        uint32_t z = a.z[k];
-        float vx = a.vx[k], vy = a.vy[k], vz = a.vz[k];
-        float ex, ez;
-        gather_E<EMODE>(a, x, z, a.phase, ex, ez);
-        float tx, ty, tz, sx, sy, sz;
-        boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
-        // half acceleration, Boris rotation (Birdsall & Langdon), half acceleration
-        vx += ex * a.hq;
-        vz += ez * a.hq;
-        rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
-        vx += ex * a.hq;
-        vz += ez * a.hq;
-        int64_t px, pz;
-        const float dz = vz * a.cz;
-        if (COORD == 1) {
-            // push in the local Cartesian frame, map back to r and rotate v (Birdsall p. 338);
-            // dr = r' - r = (2 r a + a^2 + b^2) / (r' + r) keeps the fixed-point r exact
-            const float r = (float)(x >> kFracBits) + frac(x);
-            const float ax = vx * a.cx, by = vy * a.cx;
-            const float x2 = r + ax;
-            const float rn = sqrtf(x2 * x2 + by * by);
-            const float den = rn + r;
-            const float dr = den > 0.f ? (ax * (r + x2) + by * by) / den : 0.f;
-            float sa = 0.f, ca = 1.f;
-            if (rn != 0.f) {
-                const float ir = 1.f / rn;
-                sa = by * ir;
-                ca = x2 * ir;
-            }
-            const float t0 = vx;
-            vx = ca * vx + sa * vy;
-            vy = -sa * t0 + ca * vy;
-            px = isfinite(dr) ? (int64_t)x + __float2ll_rn(dr * kOne) : -1;
-        } else {
-            const float dx = vx * a.cx;
-            px = isfinite(dx) ? (int64_t)x + __float2ll_rn(dx * kOne) : -1;
+    pz = isfinite(dz) ? (int64_t)z + __float2ll_rn(dz * kOne) : -1;
+    // boundary (advance_boundary): outside the box -> removed, or wrapped if PERIODIC
+    alive = wrap_or_keep(px, a.xmaxf, a.periodic && isfinite(dz)) &&
+            wrap_or_keep(pz, a.zmaxf, a.periodic && isfinite(dz));
+    cand = false;
+    if (!alive) return;
+    x = (uint32_t)px;
+    z = (uint32_t)pz;
+    const int ic = min((int)(x >> kFracBits), a.nx - 2);
+    const int jc = min((int)(z >> kFracBits), a.nz - 2);
+    if (a.check_mask) {
+        const int8_t* m = a.mask + (size_t)ic * a.nz + jc;
+        const bool fr = m[0] == 2 || m[a.nz] == 2 || m[1] == 2 || m[a.nz + 1] == 2;  // FREE
+        if (!fr) {
+            alive = false;
+            return;
         }
-        pz = isfinite(dz) ? (int64_t)z + __float2ll_rn(dz * kOne) : -1;
-        // boundary (advance_boundary): outside the box -> removed, or wrapped if PERIODIC
-        alive = wrap_or_keep(px, a.xmaxf, a.periodic && isfinite(dz)) &&
-                wrap_or_keep(pz, a.zmaxf, a.periodic && isfinite(dz));
-        if (alive) {
-            x = (uint32_t)px;
-            z = (uint32_t)pz;
-        }
-        int ic = 0, jc = 0;
-        if (alive) {
-            ic = min((int)(x >> kFracBits), a.nx - 2);
-            jc = min((int)(z >> kFracBits), a.nz - 2);
-        }
-        if (alive && a.check_mask) {
-            const int8_t* m = a.mask + (size_t)ic * a.nz + jc;
-            const bool fr = m[0] == 2 || m[a.nz] == 2 || m[1] == 2 || m[a.nz + 1] == 2;  // FREE
-            if (!fr) alive = false;
-        }
-        if (alive && a.rho != nullptr) {
-            const unsigned long long one = 1ull << kDepositShift;
-            const unsigned long long U = x - ((uint32_t)ic << kFracBits);
-            const unsigned long long V = z - ((uint32_t)jc << kFracBits);
-            unsigned long long* r0 = a.rho + (size_t)ic * a.nz + jc;
-            atomicAdd(r0, (one - U) * (one - V));
-            atomicAdd(r0 + a.nz, U * (one - V));
-            atomicAdd(r0 + 1, (one - U) * V);
-            atomicAdd(r0 + a.nz + 1, U * V);
-        }
-        if (alive && a.coll_threshold != 0u) {
-            const uint32_t pid = a.id[k];
-            const U4 r = draw(a.seed, a.species, pid, step, TAG_COLLIDE_TEST, 0);
-            if (r.x < a.coll_threshold) {
-                if (a.coll_mode == 1) {
-                    const int res = mcc_scatter_maxwell(a.mcc, a.seed, a.species, pid, step, vx, vy, vz);
-                    atomicAdd(res == MCC_HIT ? &s_coll : &s_null, 1ull);
-                } else {
-                    cand = true;
-                }
-            }
-        }
-        a.x[k] = alive ? x : kDead;
-        a.z[k] = z;
-        a.vx[k] = vx;
-        a.vy[k] = vy;
-        a.vz[k] = vz;
     }
-    // warp-aggregated counters and candidate append
+    if (a.rho != nullptr) {
+        const unsigned long long one = 1ull << kDepositShift;
+        const unsigned long long U = x - ((uint32_t)ic << kFracBits);
+        const unsigned long long V = z - ((uint32_t)jc << kFracBits);
+        unsigned long long* r0 = a.rho + (size_t)ic * a.nz + jc;
+        atomicAdd(r0, (one - U) * (one - V));
+        atomicAdd(r0 + a.nz, U * (one - V));
+        atomicAdd(r0 + 1, (one - U) * V);
+        atomicAdd(r0 + a.nz + 1, U * V);
+    }
+    if (a.coll_threshold != 0u) {
+        const U4 r = draw(a.seed, a.species, a.id[k], a.step, TAG_COLLIDE_TEST, 0);
+        cand = r.x < a.coll_threshold;
+    }
+}
+
+__device__ __forceinline__ void append_candidate(const PushArgs& a, bool cand, int64_t k)
+{
     const unsigned full = 0xffffffffu;
-    const unsigned live_mask = __ballot_sync(full, alive);
-    const unsigned rem_mask = __ballot_sync(full, was_alive && !alive);
     const unsigned cand_mask = __ballot_sync(full, cand);
-    const int lane = threadIdx.x & 31;
-    if (lane == 0) {
-        if (live_mask) atomicAdd(&a.cnt->live_step, (unsigned long long)__popc(live_mask));
-        if (rem_mask) atomicAdd(&a.cnt->removed, (unsigned long long)__popc(rem_mask));
-    }
     if (cand_mask) {
+        const int lane = threadIdx.x & 31;
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(&a.cnt->ncand, (unsigned long long)__popc(cand_mask));
         base = __shfl_sync(full, base, 0);
         if (cand) a.cand[base + __popc(cand_mask & ((1u << lane) - 1u))] = (uint32_t)k;
     }
+}
+
+// Persistent grid-stride kernel, two particles per thread and iteration (two
+// independent load streams in flight), counters kept in registers and added
+// once per warp at the end.  Collision candidates go to a compacted list that
+// k_collide processes; without collisions this kernel closes the step.
+template <int COORD, int EMODE>
+__global__ void __launch_bounds__(256, 4) k_push(const PushArgs a)
+{
+    const int64_t n = a.n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned live = 0, removed = 0;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += 2 * stride) {
+        const int64_t k0 = base + threadIdx.x, k1 = k0 + stride;
+        uint32_t x0 = k0 < n ? a.x[k0] : kDead, x1 = k1 < n ? a.x[k1] : kDead;
+        uint32_t z0 = 0, z1 = 0;
+        float vx0 = 0.f, vy0 = 0.f, vz0 = 0.f, vx1 = 0.f, vy1 = 0.f, vz1 = 0.f;
+        if (x0 != kDead) {
+            z0 = a.z[k0];
+            vx0 = a.vx[k0];
+            vy0 = a.vy[k0];
+            vz0 = a.vz[k0];
+        }
+        if (x1 != kDead) {
+            z1 = a.z[k1];
+            vx1 = a.vx[k1];
+            vy1 = a.vy[k1];
+            vz1 = a.vz[k1];
+        }
+        bool al0 = false, c0 = false, al1 = false, c1 = false;
+        if (x0 != kDead) {
+            step_particle<COORD, EMODE>(a, k0, x0, z0, vx0, vy0, vz0, al0, c0);
+            a.x[k0] = al0 ? x0 : kDead;
+            a.z[k0] = z0;
+            a.vx[k0] = vx0;
+            a.vy[k0] = vy0;
+            a.vz[k0] = vz0;
+            live += al0;
+            removed += !al0;
+        }
+        if (x1 != kDead) {
+            step_particle<COORD, EMODE>(a, k1, x1, z1, vx1, vy1, vz1, al1, c1);
+            a.x[k1] = al1 ? x1 : kDead;
+            a.z[k1] = z1;
+            a.vx[k1] = vx1;
+            a.vy[k1] = vy1;
+            a.vz[k1] = vz1;
+            live += al1;
+            removed += !al1;
+        }
+        if (a.coll_threshold != 0u) {
+            append_candidate(a, c0, k0);
+            append_candidate(a, c1, k1);
+        }
+    }
+    const unsigned full = 0xffffffffu;
+    live = __reduce_add_sync(full, live);
+    removed = __reduce_add_sync(full, removed);
+    if ((threadIdx.x & 31) == 0) {
+        if (live) atomicAdd(&a.cnt->live_step, (unsigned long long)live);
+        if (removed) atomicAdd(&a.cnt->removed, (unsigned long long)removed);
+    }
     if (a.close_step) {
         __syncthreads();
-        if (threadIdx.x == 0) close_step_if_last(a.cnt, s_coll, s_null);
+        if (threadIdx.x == 0) close_step_if_last(a.cnt, 0, 0);
     }
 }
 
@@ -338,10 +365,12 @@ void launch_push_t(const PushArgs& a, cudaStream_t s, bool init)
 {
     const unsigned grid = (unsigned)((a.n + 255) / 256);
     if (grid == 0) return;
+    // the step kernel runs a persistent grid: at most 8 blocks per SM of the 152
+    const unsigned pgrid = (unsigned)std::min<int64_t>((a.n + 511) / 512, 152 * 8);
     switch (a.emode) {
-    case 0: init ? k_push_init<COORD, 0><<<grid, 256, 0, s>>>(a) : k_push<COORD, 0><<<grid, 256, 0, s>>>(a); break;
-    case 1: init ? k_push_init<COORD, 1><<<grid, 256, 0, s>>>(a) : k_push<COORD, 1><<<grid, 256, 0, s>>>(a); break;
-    default: init ? k_push_init<COORD, 2><<<grid, 256, 0, s>>>(a) : k_push<COORD, 2><<<grid, 256, 0, s>>>(a); break;
+    case 0: init ? k_push_init<COORD, 0><<<grid, 256, 0, s>>>(a) : k_push<COORD, 0><<<pgrid, 256, 0, s>>>(a); break;
+    case 1: init ? k_push_init<COORD, 1><<<grid, 256, 0, s>>>(a) : k_push<COORD, 1><<<pgrid, 256, 0, s>>>(a); break;
+    default: init ? k_push_init<COORD, 2><<<grid, 256, 0, s>>>(a) : k_push<COORD, 2><<<pgrid, 256, 0, s>>>(a); break;
     }
 }
 

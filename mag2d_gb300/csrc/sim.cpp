@@ -713,16 +713,9 @@ PushArgs Sim::push_args(int s, bool init)
     return a;
 }
 
-// 0: no collisions, 1: inline in the particle kernel (every target with a
-// non-zero rate is a Maxwellian background), 2: candidate list + k_collide
-int Sim::coll_mode(int s) const
-{
-    const SpeciesState& S = sp[s];
-    if (S.threshold == 0) return 0;
-    for (size_t t = 0; t < sp.size(); ++t)
-        if (S.rates[t] > 0.0 && sp[t].n_slots > 0) return 2;
-    return 1;
-}
+// 0: no collisions (the particle kernel closes the step), 2: candidate list
+// processed by k_collide, which closes the step
+int Sim::coll_mode(int s) const { return sp[s].threshold == 0 ? 0 : 2; }
 
 CollideArgs Sim::collide_args(int s)
 {
