@@ -57,6 +57,10 @@ int device_status(mag_sim* sim)
 
 }  // namespace
 
+namespace mag {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace mag
+
 extern "C" {
 
 const char* mag_last_error(void) { return g_last_error.c_str(); }

@@ -1,10 +1,10 @@
-// Null-collision Monte Carlo collisions of the particles that the push kernel
-// listed as candidates (BaseSpecies::scatter, src/particles.cpp:208-365).
-// This path serves species with at least one target species that holds
-// particles (the partner is a random live particle of that species,
-// random_particle, src/particles.hpp:207-217, and COULOMB also updates the
-// partner); collisions against Maxwellian backgrounds are done inline by the
-// particle kernel.  Candidates are few, so the velocity algebra is FP64.
+// Null-collision Monte Carlo collisions of the particles that the particle
+// kernel listed as candidates (BaseSpecies::scatter, src/particles.cpp:208-365):
+// the target species by the null-collision rates, the partner velocity from a
+// Maxwellian background (rndv, src/particles.hpp:188-192) or from a random
+// live particle of the target species (random_particle, :207-217; COULOMB
+// also updates the partner), the interaction by sigma_v * density, and the
+// velocity update of its type.  Arithmetic is FP32 (see mcc_device.cuh).
 //
 // The last block to finish closes the step of the species: it moves the live
 // count into the running totals, clears the candidate counter and advances
@@ -34,12 +34,12 @@ __global__ void __launch_bounds__(128) k_collide(const CollideArgs a)
         const uint32_t p = a.cand[c];
         const uint32_t pid = a.id[p];
         Stream rs(a.seed, a.species, pid, TAG_COLLIDE, step);
-        double vx = a.vx[p], vy = a.vy[p], vz = a.vz[p];
+        float vx = a.vx[p], vy = a.vy[p], vz = a.vz[p];
         const int s = mcc_pick_target(m, rs);
-        double vr2, vz2, vt2;
+        float vr2, vz2, vt2;
         int partner = -1;
         if (!a.t_has_slots[s]) {
-            const double sig = m.t_sigma_v[s];
+            const float sig = (float)m.t_sigma_v[s];
             vr2 = rs.normalf() * sig;
             vz2 = rs.normalf() * sig;
             vt2 = rs.normalf() * sig;
@@ -63,19 +63,19 @@ __global__ void __launch_bounds__(128) k_collide(const CollideArgs a)
             vt2 = a.t_vy[s][partner];
         }
         bool pu;
-        double pvx, pvy, pvz;
+        float pvx, pvy, pvz;
         const int r = mcc_collide(m, s, rs, vx, vy, vz, vr2, vz2, vt2, pu, pvx, pvy, pvz);
         if (r != MCC_HIT) {
             atomicAdd(&s_null, 1ull);
             continue;
         }
-        a.vx[p] = (float)vx;
-        a.vy[p] = (float)vy;
-        a.vz[p] = (float)vz;
+        a.vx[p] = vx;
+        a.vy[p] = vy;
+        a.vz[p] = vz;
         if (pu && partner >= 0) {
-            a.t_vx[s][partner] = (float)pvx;
-            a.t_vy[s][partner] = (float)pvy;
-            a.t_vz[s][partner] = (float)pvz;
+            a.t_vx[s][partner] = pvx;
+            a.t_vy[s][partner] = pvy;
+            a.t_vz[s][partner] = pvz;
         }
         atomicAdd(&s_coll, 1ull);
     }

@@ -1,7 +1,8 @@
-// Device side of BaseSpecies::scatter (src/particles.cpp:208-365), shared by
-// the inline collision path of the particle kernel and the candidate-list
-// collision kernel.  Random variates come from the Philox stream of the
-// colliding particle; velocity algebra is FP64, variates FP32.
+// Device side of BaseSpecies::scatter (src/particles.cpp:208-365) for the
+// candidate-list collision kernel.  Random variates come from the Philox
+// stream of the colliding particle.  The arithmetic is FP32 (GB300 runs FP64
+// at 1/64 of the FP32 rate, and MCC parity is statistical); only the Coulomb
+// cross section, whose charge products sit near the FP32 range limit, is FP64.
 #pragma once
 #include "device.hpp"
 #include "philox.hpp"
@@ -42,63 +43,65 @@ struct Stream {
     }
 };
 
-__device__ inline double mcc_table(const double* E, const double* S, int n, double x)
+__device__ inline float mcc_table(const double* E, const double* S, int n, float x)
 {
-    if (x >= E[n - 1]) return S[n - 1];
-    if (x <= E[0]) return S[0];
+    if (x >= (float)E[n - 1]) return (float)S[n - 1];
+    if (x <= (float)E[0]) return (float)S[0];
     int j1 = 0, j2 = n - 1;
     while (j2 - j1 > 1) {
         const int j3 = (j1 + j2) / 2;
-        if (x < E[j3]) j2 = j3;
+        if (x < (float)E[j3]) j2 = j3;
         else j1 = j3;
     }
-    const double w = (x - E[j1]) / (E[j2] - E[j1]);
-    return S[j1] * (1 - w) + S[j2] * w;
+    const float e1 = (float)E[j1], e2 = (float)E[j2];
+    const float w = (x - e1) / (e2 - e1);
+    return (float)S[j1] * (1.f - w) + (float)S[j2] * w;
 }
 
 // Interaction::sigma_v (src/particles.hpp:61-70)
-__device__ inline double mcc_sigma_v(const InterDev& in, const double* tables, double v)
+__device__ inline float mcc_sigma_v(const InterDev& in, const double* tables, float v)
 {
-    const double EeV = 0.5 * in.mu * v * v / kQeD;
     if (in.type == COULOMB) {  // Interaction::coulomb_sigma, src/particles.cpp:19-26
-        const double E = EeV * kQeD;
+        const double vd = v;
+        const double E = 0.5 * in.mu * vd * vd;
         const double Lambda = in.coul_q1q2 / (4 * kPiD * kEps0D * E);
-        return kPiD * Lambda * Lambda * log(in.coul_lambda_D / Lambda) * v;
+        return (float)(kPiD * Lambda * Lambda * log(in.coul_lambda_D / Lambda) * vd);
     }
+    const float EeV = (float)(0.5 * in.mu / kQeD) * v * v;
     if (in.tab_n > 0) {
         const double* E = tables + in.tab_off;
         return mcc_table(E, E + in.tab_n, in.tab_n, EeV) * v;
     }
-    return in.rate;
+    return (float)in.rate;
 }
 
 // isotropic vector of length len (t_random::rot, src/random.cpp:103-115)
-__device__ inline void mcc_rot(Stream& r, double len, double& x, double& y, double& z)
+__device__ inline void mcc_rot(Stream& r, float len, float& x, float& y, float& z)
 {
     const float cs = 1.0f - 2.0f * r.unif();
     const float sn = sqrtf(fmaxf(0.0f, 1.0f - cs * cs));
     float sp, cp;
     sincospif(2.0f * r.unif(), &sp, &cp);
     x = len * cs;
-    y = len * (double)(sn * sp);
-    z = len * (double)(sn * cp);
+    y = len * sn * sp;
+    z = len * sn * cp;
 }
 
 // rotation of (x, y, z) by 'angle' about a random axis normal to it (t_random::deflect, src/random.cpp:133-175)
-__device__ inline void mcc_deflect(Stream& r, double angle, double& x, double& y, double& z)
+__device__ inline void mcc_deflect(Stream& r, float angle, float& x, float& y, float& z)
 {
-    const double len = tan(angle / 2.0);
-    double x1, y1, z1;
+    const float len = tanf(angle / 2.0f);
+    float x1, y1, z1;
     mcc_rot(r, len, x1, y1, z1);
-    double tx = y * z1 - z * y1, ty = z * x1 - x * z1, tz = x * y1 - y * x1;
-    double tmp = len / sqrt(tx * tx + ty * ty + tz * tz);
+    float tx = y * z1 - z * y1, ty = z * x1 - x * z1, tz = x * y1 - y * x1;
+    float tmp = len / sqrtf(tx * tx + ty * ty + tz * tz);
     tx *= tmp;
     ty *= tmp;
     tz *= tmp;
-    const double xp = x - y * tz + z * ty;
-    const double yp = y - z * tx + x * tz;
-    const double zp = z - x * ty + y * tx;
-    tmp = 2.0 / (1 + len * len);
+    const float xp = x - y * tz + z * ty;
+    const float yp = y - z * tx + x * tz;
+    const float zp = z - x * ty + y * tx;
+    tmp = 2.0f / (1 + len * len);
     x1 = tx * tmp;
     y1 = ty * tmp;
     z1 = tz * tmp;
@@ -109,15 +112,15 @@ __device__ inline void mcc_deflect(Stream& r, double angle, double& x, double& y
 
 // complete elliptic integral of the first kind K(k) by the arithmetic-geometric
 // mean (Gauss): K(k) = pi / (2 AGM(1, sqrt(1 - k^2)))
-__device__ inline double mcc_ellint_K(double k)
+__device__ inline float mcc_ellint_K(float k)
 {
-    double a = 1.0, b = sqrt(fmax(0.0, 1.0 - k * k));
-    for (int i = 0; i < 40 && fabs(a - b) > 1e-16 * a; ++i) {
-        const double an = 0.5 * (a + b);
-        b = sqrt(a * b);
+    float a = 1.0f, b = sqrtf(fmaxf(0.0f, 1.0f - k * k));
+    for (int i = 0; i < 30 && fabsf(a - b) > 1e-7f * a; ++i) {
+        const float an = 0.5f * (a + b);
+        b = sqrtf(a * b);
         a = an;
     }
-    return kPiD / (2.0 * a);
+    return 3.14159265358979f / (2.0f * a);
 }
 
 enum { MCC_NULL = 0, MCC_HIT = 1, MCC_NOPARTNER = 2 };
@@ -138,19 +141,20 @@ __device__ inline int mcc_pick_target(const MccSpecies& m, Stream& rs)
 // Everything of scatter() after the partner velocity (vr2, vz2, vt2) of
 // target species s is known (particles.cpp:241-360).  Updates (vx, vy, vz);
 // for COULOMB also returns the partner's new velocity in (pvx, pvy, pvz).
-__device__ inline int mcc_collide(const MccSpecies& m, int s, Stream& rs, double& vx, double& vy, double& vz,
-                                  double vr2, double vz2, double vt2, bool& partner_update, double& pvx,
-                                  double& pvy, double& pvz)
+__device__ inline int mcc_collide(const MccSpecies& m, int s, Stream& rs, float& vx, float& vy, float& vz,
+                                  float vr2, float vz2, float vt2, bool& partner_update, float& pvx, float& pvy,
+                                  float& pvz)
 {
     partner_update = false;
-    const double dvx = vx - vr2, dvz = vz - vz2, dvt = vy - vt2;
-    const double v_rel = sqrt(dvx * dvx + dvz * dvz + dvt * dvt);
-    const double m2 = m.t_mass[s];
-    const double g2 = rs.uni() * m.rates[s];
-    double acc = 0.0;
+    const float dvx = vx - vr2, dvz = vz - vz2, dvt = vy - vt2;
+    const float v_rel = sqrtf(dvx * dvx + dvz * dvz + dvt * dvt);
+    const float m2 = (float)(m.t_mass[s] / m.mass);  // masses relative to the primary's
+    const float g2 = (float)(rs.uni() * m.rates[s]);
+    const float dens = (float)m.t_density[s];
+    float acc = 0.0f;
     int hit = -1;
     for (int q = m.inter_begin[s]; q < m.inter_end[s]; ++q) {
-        acc += mcc_sigma_v(m.inter[q], m.tables, v_rel) * m.t_density[s];
+        acc += mcc_sigma_v(m.inter[q], m.tables, v_rel) * dens;
         if (acc > g2) {
             hit = q;
             break;
@@ -158,13 +162,13 @@ __device__ inline int mcc_collide(const MccSpecies& m, int s, Stream& rs, double
     }
     if (hit < 0) return MCC_NULL;
     const InterDev in = m.inter[hit];
-    const double mass = m.mass;
-    const double tmp = 1.0 / (mass + m2);
+    const float mass = 1.0f;
+    const float tmp = 1.0f / (mass + m2);
     switch (in.type) {
     case SUPERELASTIC: {
-        const double E = 0.5 * in.mu * v_rel * v_rel + in.DE;
-        const double vr = sqrt(2 * E / in.mu);
-        double rx, rz, ry;
+        const double E = 0.5 * in.mu * (double)v_rel * v_rel + in.DE;
+        const float vr = (float)sqrt(2 * E / in.mu);
+        float rx, rz, ry;
         mcc_rot(rs, vr, rx, rz, ry);
         vx = (rx * m2 + vx * mass + vr2 * m2) * tmp;
         vz = (ry * m2 + vz * mass + vz2 * m2) * tmp;
@@ -172,10 +176,10 @@ __device__ inline int mcc_collide(const MccSpecies& m, int s, Stream& rs, double
     } break;
     case COULOMB:
     case ELASTIC: {
-        const double cx = (vx * mass + vr2 * m2) * tmp;
-        const double cz = (vz * mass + vz2 * m2) * tmp;
-        const double cy = (vy * mass + vt2 * m2) * tmp;
-        double rx, ry, rz;
+        const float cx = (vx * mass + vr2 * m2) * tmp;
+        const float cz = (vz * mass + vz2 * m2) * tmp;
+        const float cy = (vy * mass + vt2 * m2) * tmp;
+        float rx, ry, rz;
         mcc_rot(rs, v_rel, rx, ry, rz);
         vx = rx * m2 * tmp + cx;
         vz = rz * m2 * tmp + cz;
@@ -193,18 +197,18 @@ __device__ inline int mcc_collide(const MccSpecies& m, int s, Stream& rs, double
         vy = vt2;
         break;
     case LANGEVIN: {
-        double v1x = (vx - vr2) * m2 * tmp;
-        double v1y = (vz - vz2) * m2 * tmp;
-        double v1z = (vy - vt2) * m2 * tmp;
-        const double beta = sqrt(rs.uni()) * in.cutoff;
-        if (beta > 1.0) {  // Nanbu & Kitatani, J. Phys. D 28 (1995) 324
-            const double b2 = beta * beta;
-            const double tt = sqrt(b2 * b2 - 1.0);
-            const double xi0 = sqrt(b2 - tt), xi1 = sqrt(b2 + tt);
-            const double theta = mcc_ellint_K(xi0 / xi1) * 1.41421356237309504880 * beta / xi1;
-            mcc_deflect(rs, kPiD - 2 * theta, v1x, v1y, v1z);
+        float v1x = (vx - vr2) * m2 * tmp;
+        float v1y = (vz - vz2) * m2 * tmp;
+        float v1z = (vy - vt2) * m2 * tmp;
+        const float beta = sqrtf(rs.unif()) * (float)in.cutoff;
+        if (beta > 1.0f) {  // Nanbu & Kitatani, J. Phys. D 28 (1995) 324
+            const float b2 = beta * beta;
+            const float tt = sqrtf(b2 * b2 - 1.0f);
+            const float xi0 = sqrtf(b2 - tt), xi1 = sqrtf(b2 + tt);
+            const float theta = mcc_ellint_K(xi0 / xi1) * 1.41421356f * beta / xi1;
+            mcc_deflect(rs, 3.14159265358979f - 2 * theta, v1x, v1y, v1z);
         } else {
-            const double len = sqrt(v1x * v1x + v1y * v1y + v1z * v1z);
+            const float len = sqrtf(v1x * v1x + v1y * v1y + v1z * v1z);
             mcc_rot(rs, len, v1x, v1y, v1z);
         }
         vx = v1x + (vx * mass + vr2 * m2) * tmp;

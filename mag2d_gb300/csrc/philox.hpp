@@ -50,6 +50,21 @@ MAG_HD U4 draw(uint64_t seed, uint32_t sp, uint32_t id, uint64_t step, uint32_t 
     return philox4x32_10(c, (uint32_t)seed ^ (sp * 0x85EBCA6Bu), (uint32_t)(seed >> 32));
 }
 
+// Per-step collision test: one 32-bit uniform per (seed, species, particle id,
+// step), from the 64-bit finaliser of SplitMix64 (Steele, Lea, Flood, "Fast
+// splittable pseudorandom number generators", OOPSLA 2014) applied to the
+// stream position seed + (id * 2^32 + step) * golden gamma.  Two 64-bit
+// multiplies instead of the ten rounds of Philox; the rarer draws of the
+// collisions themselves stay on Philox.
+MAG_HD uint32_t collision_test_u32(uint64_t seed, uint32_t sp, uint32_t id, uint64_t step)
+{
+    uint64_t z = (seed ^ ((uint64_t)sp << 56)) + (((uint64_t)id << 32) ^ step) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (uint32_t)(z >> 32);
+}
+
 // uniform in [0,1) with 24 random bits (float) / 53 random bits (double)
 MAG_HD float u01f(uint32_t a) { return (float)(a >> 8) * (1.0f / 16777216.0f); }
 MAG_HD double u01d(uint32_t a, uint32_t b)

@@ -133,13 +133,29 @@ __device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float tx
     }
 }
 
-__device__ __forceinline__ bool wrap_or_keep(int64_t& p, uint32_t maxf, int periodic)
+// Move a fixed-point coordinate by d fixed-point units; false when it leaves
+// [0, maxf] (advance_boundary, FREE), or wrapped into [0, maxf) (PERIODIC).
+__device__ __forceinline__ bool move_coord(uint32_t& x, int d, uint32_t maxf, bool periodic)
 {
-    if (p >= 0 && p <= (int64_t)maxf) return true;
+    const uint32_t nx = x + (uint32_t)d;
+    const bool out = d >= 0 ? (nx < x || nx > maxf) : (nx > x);
+    if (!out) {
+        x = nx;
+        return true;
+    }
     if (!periodic || maxf == 0) return false;
-    p %= (int64_t)maxf;
+    long long p = (long long)x + d;  // rare path
+    p %= (long long)maxf;
     if (p < 0) p += maxf;
+    x = (uint32_t)p;
     return true;
+}
+
+// displacement in fixed-point units, clamped so that a wild value is simply "out"
+__device__ __forceinline__ int to_fixed_disp(float cells)
+{
+    const float v = fminf(fmaxf(cells * kOne, -1.0e9f), 1.0e9f);
+    return __float2int_rn(v);
 }
 
 __device__ __forceinline__ void close_step_if_last(Counters* c, unsigned long long coll, unsigned long long nnull)
@@ -178,7 +194,7 @@ __device__ __forceinline__ void step_particle(const PushArgs& a, int64_t k, uint
     rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
     vx += ex * a.hq;
     vz += ez * a.hq;
-    int64_t px, pz;
+    int dpx;
     const float dz = vz * a.cz;
     if (COORD == 1) {
         // push in the local Cartesian frame, map back to r and rotate v (Birdsall p. 338);
@@ -198,19 +214,18 @@ __device__ __forceinline__ void step_particle(const PushArgs& a, int64_t k, uint
         const float t0 = vx;
         vx = ca * vx + sa * vy;
         vy = -sa * t0 + ca * vy;
-        px = isfinite(dr) ? (int64_t)x + __float2ll_rn(dr * kOne) : -1;
+        dpx = to_fixed_disp(dr);
+        alive = isfinite(dr);
     } else {
         const float dx = vx * a.cx;
-        px = isfinite(dx) ? (int64_t)x + __float2ll_rn(dx * kOne) : -1;
+        dpx = to_fixed_disp(dx);
+        alive = isfinite(dx);
     }
-    pz = isfinite(dz) ? (int64_t)z + __float2ll_rn(dz * kOne) : -1;
+    alive = alive && isfinite(dz);
     // boundary (advance_boundary): outside the box -> removed, or wrapped if PERIODIC
-    alive = wrap_or_keep(px, a.xmaxf, a.periodic && isfinite(dz)) &&
-            wrap_or_keep(pz, a.zmaxf, a.periodic && isfinite(dz));
+    alive = alive && move_coord(x, dpx, a.xmaxf, a.periodic) && move_coord(z, to_fixed_disp(dz), a.zmaxf, a.periodic);
     cand = false;
     if (!alive) return;
-    x = (uint32_t)px;
-    z = (uint32_t)pz;
     const int ic = min((int)(x >> kFracBits), a.nx - 2);
     const int jc = min((int)(z >> kFracBits), a.nz - 2);
     if (a.check_mask) {
@@ -231,10 +246,7 @@ __device__ __forceinline__ void step_particle(const PushArgs& a, int64_t k, uint
         atomicAdd(r0 + 1, (one - U) * V);
         atomicAdd(r0 + a.nz + 1, U * V);
     }
-    if (a.coll_threshold != 0u) {
-        const U4 r = draw(a.seed, a.species, a.id[k], a.step, TAG_COLLIDE_TEST, 0);
-        cand = r.x < a.coll_threshold;
-    }
+    if (a.coll_threshold != 0u) cand = collision_test_u32(a.seed, a.species, a.id[k], a.step) < a.coll_threshold;
 }
 
 __device__ __forceinline__ void append_candidate(const PushArgs& a, bool cand, int64_t k)

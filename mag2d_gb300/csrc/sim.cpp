@@ -9,6 +9,7 @@
 #include <sstream>
 
 #include "kernels.hpp"
+#include "multigrid_host.hpp"
 
 namespace mag {
 
@@ -22,106 +23,6 @@ namespace {
 constexpr double kPi = 3.14159265358979323846;
 
 bool fixed_node(int8_t m) { return m == FIXED || m == FIXED_RF; }
-
-// 9-point operator planes: plane (di+1)*3 + (dj+1) holds the coefficient of node (i+di, j+dj)
-inline int plane(int di, int dj) { return (di + 1) * 3 + (dj + 1); }
-
-// Fine-level operator of the correction equation: the reference's rows
-// (src/fields.cpp:149-238) on free nodes with the columns of Dirichlet nodes
-// removed; Dirichlet rows are identity.
-void fine_operator(int coord, int nx, int nz, double dx, double dz, const std::vector<int8_t>& mask,
-                   std::vector<double>& A)
-{
-    const size_t n = (size_t)nx * nz;
-    A.assign(9 * n, 0.0);
-    for (int i = 0; i < nx; ++i)
-        for (int j = 0; j < nz; ++j) {
-            const size_t k = (size_t)i * nz + j;
-            if (fixed_node(mask[k])) {
-                A[4 * n + k] = 1.0;
-                continue;
-            }
-            double w, e, s, nn, c;
-            if (coord == CYLINDRICAL) {
-                const double k2 = 1.0 / (dz * dz);
-                if (i == 0) {
-                    const double k3 = 1.0 / (dx * dx * 0.25);
-                    w = 0.0; e = k3; s = k2; nn = k2; c = -2.0 * k2 - k3;
-                } else {
-                    const double k1 = (i - 0.5) / (dx * dx * i), k3 = (i + 0.5) / (dx * dx * i);
-                    w = k1; e = k3; s = k2; nn = k2; c = -2.0 * k2 - k1 - k3;
-                }
-            } else {
-                w = e = s = nn = 1.0;
-                c = -4.0;
-            }
-            A[4 * n + k] = c;
-            if (i > 0 && !fixed_node(mask[k - nz])) A[(size_t)plane(-1, 0) * n + k] = w;
-            if (i < nx - 1 && !fixed_node(mask[k + nz])) A[(size_t)plane(1, 0) * n + k] = e;
-            if (j > 0 && !fixed_node(mask[k - 1])) A[(size_t)plane(0, -1) * n + k] = s;
-            if (j < nz - 1 && !fixed_node(mask[k + 1])) A[(size_t)plane(0, 1) * n + k] = nn;
-        }
-}
-
-// Galerkin coarse operator Ac = P^T Af P with bilinear P (rows of fixed fine
-// nodes are zero).  Coarse rows left without a diagonal become identity.
-void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int& nxc,
-              int& nzc, std::vector<double>& Ac)
-{
-    nxc = (nxf - 1) / 2 + 1;
-    nzc = (nzf - 1) / 2 + 1;
-    const size_t nf = (size_t)nxf * nzf, nc = (size_t)nxc * nzc;
-    Ac.assign(9 * nc, 0.0);
-    auto pw = [](int a) { return a == 0 ? 1.0 : 0.5; };
-    for (int J0 = 0; J0 < nxc; ++J0)
-        for (int J1 = 0; J1 < nzc; ++J1) {
-            double v[3][3] = {{0}};
-            for (int a = -1; a <= 1; ++a)
-                for (int b = -1; b <= 1; ++b) {
-                    const int i = 2 * J0 + a, j = 2 * J1 + b;
-                    if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
-                    if (fixed_f[(size_t)i * nzf + j]) continue;
-                    v[a + 1][b + 1] = pw(a) * pw(b);
-                }
-            double w[5][5] = {{0}};
-            for (int a = -2; a <= 2; ++a)
-                for (int b = -2; b <= 2; ++b) {
-                    const int i = 2 * J0 + a, j = 2 * J1 + b;
-                    if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
-                    const size_t f = (size_t)i * nzf + j;
-                    double acc = 0.0;
-                    for (int di = -1; di <= 1; ++di)
-                        for (int dj = -1; dj <= 1; ++dj) {
-                            const int ga = a + di, gb = b + dj;
-                            if (ga < -1 || ga > 1 || gb < -1 || gb > 1) continue;
-                            const double vv = v[ga + 1][gb + 1];
-                            if (vv == 0.0) continue;
-                            acc += Af[(size_t)plane(di, dj) * nf + f] * vv;
-                        }
-                    w[a + 2][b + 2] = acc;
-                }
-            for (int I0 = J0 - 1; I0 <= J0 + 1; ++I0)
-                for (int I1 = J1 - 1; I1 <= J1 + 1; ++I1) {
-                    if (I0 < 0 || I0 >= nxc || I1 < 0 || I1 >= nzc) continue;
-                    double acc = 0.0;
-                    for (int a = -1; a <= 1; ++a)
-                        for (int b = -1; b <= 1; ++b) {
-                            const int i = 2 * I0 + a, j = 2 * I1 + b;
-                            if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
-                            if (fixed_f[(size_t)i * nzf + j]) continue;
-                            const int wa = i - 2 * J0, wb = j - 2 * J1;
-                            if (wa < -2 || wa > 2 || wb < -2 || wb > 2) continue;
-                            acc += pw(a) * pw(b) * w[wa + 2][wb + 2];
-                        }
-                    Ac[(size_t)plane(J0 - I0, J1 - I1) * nc + (size_t)I0 * nzc + I1] = acc;
-                }
-        }
-    for (size_t k = 0; k < nc; ++k)
-        if (Ac[4 * nc + k] == 0.0) {
-            for (int q = 0; q < 9; ++q) Ac[q * nc + k] = 0.0;
-            Ac[4 * nc + k] = 1.0;
-        }
-}
 
 std::vector<std::string> tokens(const std::string& line)
 {
@@ -333,12 +234,8 @@ void Sim::setup_solver()
     if (solver_ready) return;
     validate_operator();
     const int coord = p.coord == CYLINDRICAL ? 1 : 0;
-    std::vector<int> lnx{nx}, lnz{nz};
-    while (lnx.size() < (size_t)kMaxLevels && (lnx.back() - 1) % 2 == 0 && (lnz.back() - 1) % 2 == 0 &&
-           lnx.back() >= 5 && lnz.back() >= 5) {
-        lnx.push_back((lnx.back() - 1) / 2 + 1);
-        lnz.push_back((lnz.back() - 1) / 2 + 1);
-    }
+    std::vector<int> lnx, lnz;
+    multigrid_levels(nx, nz, kMaxLevels, lnx, lnz);
     lv.nlev = (int)lnx.size();
     lv.nx = lnx;
     lv.nz = lnz;

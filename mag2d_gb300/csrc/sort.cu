@@ -26,13 +26,21 @@ __device__ __forceinline__ int cell_of(uint32_t x, uint32_t z, int nx, int nz)
     return i * (nz - 1) + j;
 }
 
+// Particles of a warp that share a cell add to its counter once (sorted
+// particles arrive in runs of the same cell).
 __global__ void k_cell_count(const SortArgs a)
 {
     const long long n = a.n;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-        const uint32_t x = a.x[k];
-        if (x == kDead) continue;
-        atomicAdd(&a.count[cell_of(x, a.z[k], a.nx, a.nz)], 1u);
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+        const long long k = base + threadIdx.x;
+        const uint32_t x = k < n ? a.x[k] : kDead;
+        const bool valid = x != kDead;
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        if (!valid) continue;
+        const int c = cell_of(x, a.z[k], a.nx, a.nz);
+        const unsigned peers = __match_any_sync(vm, c);
+        if (lane == __ffs(peers) - 1) atomicAdd(&a.count[c], (unsigned)__popc(peers));
     }
 }
 
@@ -110,14 +118,24 @@ __global__ void __launch_bounds__(1024) k_scan_add(const SortArgs a)
 __global__ void k_cell_scatter(const SortArgs a, long long n_src)
 {
     const long long total = a.offset[a.ncells];
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n_src;
-         k += (long long)gridDim.x * blockDim.x) {
-        if (k >= total) a.ox[k] = kDead;
-        const uint32_t x = a.x[k];
-        if (x == kDead) continue;
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n_src; base += (long long)gridDim.x * blockDim.x) {
+        const long long k = base + threadIdx.x;
+        if (k < n_src && k >= total) a.ox[k] = kDead;
+        const uint32_t x = k < n_src ? a.x[k] : kDead;
+        const bool valid = x != kDead;
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        if (!valid) continue;
         const uint32_t z = a.z[k];
         const int c = cell_of(x, z, a.nx, a.nz);
-        const uint32_t pos = a.offset[c] + atomicSub(&a.count[c], 1u) - 1u;
+        // one atomic per run of equal cells in the warp; lanes take the slots below the old count
+        const unsigned peers = __match_any_sync(vm, c);
+        const int leader = __ffs(peers) - 1;
+        uint32_t old = 0;
+        if (lane == leader) old = atomicSub(&a.count[c], (unsigned)__popc(peers));
+        old = __shfl_sync(peers, old, leader);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        const uint32_t pos = a.offset[c] + old - 1u - rank;
         a.ox[pos] = x;
         a.oz[pos] = z;
         a.ovx[pos] = a.vx[k];
