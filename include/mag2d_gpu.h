@@ -171,6 +171,31 @@ int mag_config_geometry(const char* config_path, int64_t cap, int8_t* mask, doub
 int mag_config_species(const char* config_path, const char* species_conf_path, int index,
                        mag_species_info* out, double* rates_out);
 
+/* ---- allocation-free Poisson solve ------------------------------------------
+ *
+ * No counterpart in the reference.  Fields::boundary_solve (src/fields.cpp:278-312)
+ * as a stateless call that allocates no device memory, for callers that cannot
+ * call cudaMalloc: code running under a fixed, pre-reserved device-memory budget
+ * or a caching allocator it does not own, or calling from a context where a
+ * device allocation would synchronise the device.  The caller owns rho_dev and
+ * u_dev (device memory, nx*nz doubles, z fastest); u_dev holds the initial guess
+ * on entry (zeros are fine) and the potential on return.  mask_host and
+ * voltage_host are host arrays (t_grid::mask / voltage).  coord: 0 Cartesian,
+ * 1 cylindrical; dV is used by the Cartesian scaling, macroparticle_factor by
+ * the cylindrical one.  stream may be NULL (default stream).  With info != NULL
+ * the call waits for the solve and reports it; otherwise it returns once queued.
+ *
+ * Working memory is one static device array of 4 MiB that every GPU loading the
+ * library holds until exit; grids above 257 x 257 nodes are rejected with
+ * MAG_EINVAL.  The first call on a device looks up the array's device address
+ * with that device current, so make it before any stream capture.  All calls
+ * share the array and it keeps the last call's contents: calls that overlap on
+ * the GPU race. */
+int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, double dz, double macroparticle_factor,
+                              double dV, const int8_t* mask_host, const double* voltage_host,
+                              const double* rho_dev, double* u_dev, double tol, int max_iter, void* stream,
+                              mag_solve_info* info);
+
 /* Device stream of the handle (a cudaStream_t) so callers can order their own
  * work and timing events with the simulation's. */
 void* mag_stream(mag_sim* sim);
