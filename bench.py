@@ -9,8 +9,10 @@ synthetic and seeded.  One bench step = one Pic::advance of all particles.
 
 Timing: W untimed warm-up steps, then K timed steps.  Between timed steps L2 is
 flushed by writing a 512 MB buffer on the simulation's stream (the particle
-state, 24 MB, would otherwise stay in the 129 MB L2); each step is bracketed by
-CUDA events on that stream and the step times are summed.  value = sum of live
+state, 24 MB, would otherwise stay in the 129 MB L2) and then reading a 256 MB
+one, so that the write-back of the flush's own dirty lines is not charged to
+the step; each step is bracketed by CUDA events on that stream and the step
+times are summed.  value = sum of live
 particles over the timed steps / summed step time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -51,10 +53,11 @@ def _env_rank():
     return r, w, lr
 
 
-def _config(n_gpus: int, n_ions: int = N_IONS) -> dict:
+def _config(n_gpus: int, n_ions: int = N_IONS, sort_interval: int = 100) -> dict:
     return {"workload": "multipole_xy: 22-pole RF ion trap, 257x257 x-y grid, 1e6 ions (3 amu, 0.1 eV), "
                         "He 1e-2 Pa elastic MCC, dt 2 ns", "grid": [GRID, GRID], "particles_per_gpu": n_ions,
-            "species": 2, "l2": "flushed between timed steps (512 MB write)",
+            "species": 2, "l2": "flushed between timed steps (512 MB write, then 256 MB read)",
+            "sort_interval": sort_interval,
             "parallelism": f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"}
 
 
@@ -168,13 +171,18 @@ class ClockSampler:
 
 
 def _load_profile_traffic():
-    p = ROOT / "profiles" / "push_multipole.json"
-    if p.exists():
-        try:
-            d = json.loads(p.read_text())
-            return d.get("dram_bytes_per_particle_step")
-        except Exception:
-            return None
+    """DRAM bytes per particle-step of k_push from the committed ncu summary
+    (dram__bytes_read.sum + dram__bytes_write.sum of one launch on 8e6 ions,
+    divided by the particles; traffic grows in proportion to the particles)."""
+    p = ROOT / "profiles" / "k_push_multipole_xy_8e6.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_particle_step:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
     return None
 
 
@@ -200,7 +208,8 @@ def run_ours(args) -> None:
     tmp = Path(tempfile.mkdtemp(prefix=f"mag2d_bench_{rank}_"))
     cfg, species, inter, cpath, spath, parts, loaded = multipole_xy(tmp, n=args.particles, n_nodes=GRID,
                                                                     seed=2 + rank)
-    pic = m.Pic(cpath, spath, seed=1000 + rank, device=local, capacity_hint=args.particles)
+    pic = m.Pic(cpath, spath, seed=1000 + rank, device=local, capacity_hint=args.particles, push_vec=args.push_vec,
+                sort_interval=args.sort_interval)
     ion = pic.speclist[1]
     ion.set_particles(*parts)
     pic.advance_init()
@@ -208,10 +217,15 @@ def run_ours(args) -> None:
 
     stream = torch.cuda.ExternalStream(pic.stream, device=local)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    clean = torch.ones(FLUSH_BYTES // 8, dtype=torch.float32, device=f"cuda:{local}")
+    sink = torch.empty((), dtype=torch.float32, device=f"cuda:{local}")
 
     def flush_l2():
+        # write 512 MB (evicts everything), then read 256 MB so that the dirty
+        # lines of that write are written back before the timed step starts
         with torch.cuda.stream(stream):
             flush.zero_()
+            torch.sum(clean, dim=0, out=sink)
 
     for _ in range(args.warmup):
         flush_l2()
@@ -240,12 +254,12 @@ def run_ours(args) -> None:
     psteps = d1["particle_steps"] - d0["particle_steps"]
 
     # per-kernel device time (events between the kernels of each step), L2 flushed
-    kern = np.zeros(3)
+    kern = np.zeros(4)
     nk = max(3, min(args.steps, 20))
     for _ in range(nk):
         flush_l2()
         kern += np.array(pic.advance_timed(1))
-    push_ms = kern[1] / nk
+    push_ms = kern[2] / nk
     live_now = ion.diag()["n_live"]
     alg_bytes = BYTES_PER_PARTICLE_STEP * live_now
     achieved = alg_bytes / (push_ms * 1e-3) / 1e9
@@ -291,7 +305,7 @@ def run_ours(args) -> None:
             "metric": METRIC, "value": psteps_all / total_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": _config(world, args.particles),
+            "config": _config(world, args.particles, args.sort_interval),
             "clocks": clk.summary(),
             "e2e": {"value": e2e_all, "unit": UNIT, "h2d_bytes_per_step": int(5 * 8 * n_host / e2e_chunk),
                     "d2h_bytes_per_step": int(64 / e2e_chunk) + 1,
@@ -300,10 +314,12 @@ def run_ours(args) -> None:
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": (traffic_ps * live_now) if traffic_ps else None,
-                         "kernel": "k_push<0,2> (gather + Boris + MCC test + boundary)",
+                         "traffic_source": "profiles/k_push_multipole_xy_8e6.md, scaled to the live ions",
+                         "kernel": "k_push<0,2,0,2> (gather + Boris + collision test + boundary)",
                          "alg_bytes_per_launch": alg_bytes, "kernel_ms": push_ms,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured" if peaks else "fallback"},
-            "kernel_ms_per_step": {"solve": kern[0] / nk, "particles": kern[1] / nk, "collide": kern[2] / nk},
+            "kernel_ms_per_step": {"sort": kern[0] / nk, "solve": kern[1] / nk, "particles": kern[2] / nk,
+                                   "collide": kern[3] / nk},
         }
         if base is not None:
             line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")}
@@ -322,6 +338,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--particles", type=int, default=N_IONS, help="ions per GPU (default: the workload's 1e6)")
+    ap.add_argument("--push-vec", type=int, default=0, help="slots per thread of the particle kernel (0: library default)")
+    ap.add_argument("--sort-interval", type=int, default=100, help="steps between particle sorts (0: library default, 20)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -54,6 +54,8 @@ typedef struct {
     double poisson_tol;    /* Jacobi-scaled residual / max|u| at which the solve stops (0 = 1e-12) */
     int poisson_max_iter;  /* outer refinement iterations before MAG_ENOTCONV (0 = 200) */
     int64_t capacity_hint; /* particle slots to reserve per species (0 = grow as needed) */
+    int push_vec;          /* consecutive slots per thread of the particle kernel: 1, 2 or 4 (0 = 2);
+                              results do not depend on it */
 } mag_opts;
 
 typedef struct {
@@ -107,8 +109,10 @@ int mag_advance_init(mag_sim* sim);
 int mag_advance(mag_sim* sim, uint64_t nsteps);
 
 /* mag_advance with CUDA events recorded on the handle's stream between the
- * kernels of every step; ms_out[0..2] receive the summed device time of the
- * Poisson solve, the particle kernel and the collision kernel.  Synchronises. */
+ * kernels of every step; ms_out[0..3] receive the summed device time of the
+ * particle sort (every sort_interval steps), the Poisson solve, the particle
+ * kernels and the collision kernels (timed after all particle kernels, so
+ * without their overlap).  Synchronises. */
 int mag_advance_timed(mag_sim* sim, uint64_t nsteps, double* ms_out);
 
 /* Wait for queued work and report any device-side error flag. */

@@ -30,23 +30,26 @@ constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis (=
 constexpr uint32_t kFracMask = (1u << kFracBits) - 1u;
 constexpr uint32_t kDead = 0xFFFFFFFFu;
 constexpr int kMaxCellsPerAxis = 4095;
+constexpr int64_t kSlotAlign = 64;  // particle arrays hold a multiple of this many slots (vector access)
 
 // CollType of the species_conf INTERACTION blocks (src/parser.hpp:15)
 enum CollType { ELASTIC = 0, LANGEVIN = 1, CX = 2, COULOMB = 3, SUPERELASTIC = 4 };
 
+// Per-species counters.  The particle kernel of launch i adds to slot i & 1
+// of the per-step counters; the next launch's first thread folds slot
+// (i - 1) & 1 into the running totals and clears it, so no kernel has to find
+// out which of its blocks finished last.  Host reads add the slot of the last
+// launch, which no kernel has folded yet.
 struct Counters {
-    unsigned long long niter;      // steps advanced by this species
-    unsigned long long live_step;  // live particles counted by the running step
-    unsigned long long live_last;  // live particles after the last completed step
-    unsigned long long live_sum;   // sum over completed steps of live particles
-    unsigned long long removed;    // particles removed at the boundary
-    unsigned long long ncand;      // collision candidates of the running step
-    unsigned long long ncoll;      // real collisions
-    unsigned long long nnull;      // null collisions
+    unsigned long long live_par[2];   // live particles after the step of that launch parity
+    unsigned long long ncand_par[2];  // collision candidates listed by the step of that parity
+    unsigned long long live_sum;      // sum over folded steps of live particles
+    unsigned long long removed;       // particles removed at the boundary
+    unsigned long long ncoll;         // real collisions
+    unsigned long long nnull;         // null collisions
     unsigned long long partner_miss;
-    unsigned long long done_blocks;
-    unsigned long long slots;      // slots in use on the device (shrinks when a sort compacts)
-    int error;                     // first device error code (0 = none)
+    unsigned long long slots;         // slots in use on the device (shrinks when a sort compacts)
+    int error;                        // first device error code (0 = none)
     int pad;
 };
 
@@ -74,6 +77,7 @@ struct PushArgs {
     int periodic;
     int check_mask;            // kill particles in cells with no FREE corner (t_grid::is_free)
     const int8_t* mask;        // nx*nz
+    const uint8_t* cellfree;   // (nx-1)*(nz-1): 1 when one of the cell's four nodes is FREE
     // electric field: 0 uniform (0, extern_ez), 1 from u faces, 2 from (u, uRF) face pairs
     int emode;
     const float* Exf;
@@ -84,6 +88,7 @@ struct PushArgs {
     float phase;                   // rf_amplitude cos(mod(rf_omega niter dt, 1e7 pi)) + rf_U0 (fields.hpp:135-145)
     uint64_t step;                 // this species' step counter (niter), the counter of its random streams
     // magnetic field: constant Boris vectors, or tables Br/Bz (Field2D::interpolate)
+    int has_b;                     // 0: B = 0 everywhere, the rotation is the identity
     int btab;
     float tx, ty, tz, sx, sy, sz;
     const float* Br;
@@ -96,13 +101,14 @@ struct PushArgs {
     float cx, cz;                  // dt/dx, dt/dz (cells per m/s)
     unsigned long long* rho;       // fixed-point deposit (nx*nz) or null
     uint32_t coll_threshold;       // collision probability * 2^32 (0: no test)
-    int coll_mode;                 // 0 none, 2 candidate list (k_collide)
-    uint32_t* cand;
+    uint32_t* cand;                // candidate slots (run by k_collide)
+    float4* cand_rec;              // candidate (vx, vy, vz, id bits) after the push
     const MccSpecies* mcc;
     uint64_t seed;
     uint32_t species;
     Counters* cnt;
-    int close_step;                // the last block closes the step (no collide kernel follows)
+    int slot;                      // parity of this launch (Counters::live_par, ncand_par)
+    int fold_slot;                 // slot of the previous launch to fold into the totals, or -1
 };
 
 struct InterDev {
@@ -118,11 +124,17 @@ struct InterDev {
 
 struct CollideArgs {
     float *vx, *vy, *vz;
-    const uint32_t* id;
     const uint32_t* cand;
+    const float4* cand_rec;    // (vx, vy, vz, id bits) of each candidate after the push
+    const InterDev* inter;     // the whole interaction list (MccSpecies::inter) and its tables,
+    int n_inter;               // staged in shared memory by the kernel
+    const double* tables;
+    int n_tables;
     Counters* cnt;
+    int slot;                  // parity of the particle kernel launch whose candidates these are
     const MccSpecies* mcc;
     int t_has_slots[kMaxSpecies];
+    int any_target_slots;      // some target species holds particles (partner = random particle)
     const uint32_t* t_x[kMaxSpecies];
     float* t_vx[kMaxSpecies];
     float* t_vy[kMaxSpecies];

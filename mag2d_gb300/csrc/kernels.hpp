@@ -7,7 +7,9 @@
 
 namespace mag {
 
-int launch_push(const PushArgs& a, int coord, bool init, cudaStream_t s);
+// particle step (init: leapfrog start).  vec = slots per thread (1, 2 or 4);
+// sm_count = multiprocessors of the device (sizes the persistent grid)
+int launch_push(const PushArgs& a, int coord, bool init, int vec, int sm_count, cudaStream_t s);
 int launch_deposit(const PushArgs& a, cudaStream_t s);
 int launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
 // counting sort by cell with compaction; n_src = slots of the source arrays

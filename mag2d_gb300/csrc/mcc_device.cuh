@@ -221,4 +221,109 @@ __device__ inline int mcc_collide(const MccSpecies& m, int s, Stream& rs, float&
     return MCC_HIT;
 }
 
+// Shared-memory copy of a species' MCC data (MccSpecies and the interaction
+// list) and, when small enough, its cross-section tables.
+constexpr int kStageTables = 4096;  // table doubles staged in shared memory (32 KB)
+
+struct MccStage {
+    MccSpecies m;
+    InterDev inter[kMaxInteractions];
+};
+
+// Block-wide copy into shared memory; the caller synchronises the block,
+// calls mcc_stage_pointers from one thread, and synchronises again.
+__device__ inline void mcc_stage(const CollideArgs& a, MccStage& st, double* s_tab)
+{
+    static_assert(sizeof(MccSpecies) % 8 == 0 && sizeof(InterDev) % 8 == 0, "word copies");
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(a.mcc);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&st.m);
+    for (int w = threadIdx.x; w < (int)(sizeof(MccSpecies) / 8); w += blockDim.x) dst[w] = src[w];
+    const int ni = min(a.n_inter, kMaxInteractions);
+    src = reinterpret_cast<const unsigned long long*>(a.inter);
+    dst = reinterpret_cast<unsigned long long*>(st.inter);
+    for (int w = threadIdx.x; w < ni * (int)(sizeof(InterDev) / 8); w += blockDim.x) dst[w] = src[w];
+    if (s_tab && a.n_tables <= kStageTables)
+        for (int w = threadIdx.x; w < a.n_tables; w += blockDim.x) s_tab[w] = a.tables[w];
+}
+
+__device__ inline void mcc_stage_pointers(const CollideArgs& a, MccStage& st, double* s_tab)
+{
+    st.m.inter = st.inter;
+    if (s_tab && a.n_tables <= kStageTables) st.m.tables = s_tab;
+}
+
+// Scatter of one particle against a target drawn from the null-collision
+// rates, when every target species is a Maxwellian background (no particles):
+// the partner velocity is rndv (src/particles.hpp:188-192).  Updates
+// (vx, vy, vz); returns MCC_HIT or MCC_NULL.
+static __device__ __forceinline__ int collide_background(const MccSpecies& m, uint64_t seed, uint32_t species,
+                                                      uint32_t pid, uint64_t step, float& vx, float& vy, float& vz)
+{
+    Stream rs(seed, species, pid, TAG_COLLIDE, step);
+    const int s = mcc_pick_target(m, rs);
+    const float sig = (float)m.t_sigma_v[s];
+    const float vr2 = rs.normalf() * sig;
+    const float vz2 = rs.normalf() * sig;
+    const float vt2 = rs.normalf() * sig;
+    bool pu;
+    float pvx, pvy, pvz;
+    return mcc_collide(m, s, rs, vx, vy, vz, vr2, vz2, vt2, pu, pvx, pvy, pvz);
+}
+
+// One candidate c of the list: the whole of BaseSpecies::scatter for it.
+// Returns MCC_HIT, MCC_NULL or MCC_NOPARTNER.  The list and the particle
+// arrays are read through L2 (ld.global.cg): the kernel that wrote them may
+// still have been running when this one started (programmatic launch).
+static __device__ __noinline__ int collide_one(const CollideArgs& a, const MccSpecies& m, unsigned long long c)
+{
+    const uint32_t p = __ldcg(a.cand + c);
+    const float4 rec = __ldcg(a.cand_rec + c);
+    const uint32_t pid = __float_as_uint(rec.w);
+    float vx = rec.x, vy = rec.y, vz = rec.z;
+    int r;
+    int64_t partner = -1;
+    int s = 0;
+    bool pu = false;
+    float pvx = 0.f, pvy = 0.f, pvz = 0.f;
+    if (!a.any_target_slots) {
+        r = collide_background(m, a.seed, a.species, pid, a.step, vx, vy, vz);
+    } else {
+        Stream rs(a.seed, a.species, pid, TAG_COLLIDE, a.step);
+        s = mcc_pick_target(m, rs);
+        float vr2, vz2, vt2;
+        if (!a.t_has_slots[s]) {
+            const float sig = (float)m.t_sigma_v[s];
+            vr2 = rs.normalf() * sig;
+            vz2 = rs.normalf() * sig;
+            vt2 = rs.normalf() * sig;
+        } else {
+            Stream ps(a.seed, a.species, pid, TAG_PARTNER, a.step);
+            const int64_t nt = a.t_n[s];
+            for (int tries = 0; tries < 256 && nt > 0; ++tries) {
+                const uint64_t hi = ps.next();
+                const int64_t q = (int64_t)(((hi << 32) | ps.next()) % (uint64_t)nt);
+                if (__ldcg(a.t_x[s] + q) != kDead) {  // any live particle, itself included (random_particle)
+                    partner = q;
+                    break;
+                }
+            }
+            if (partner < 0) return MCC_NOPARTNER;
+            vr2 = __ldcg(a.t_vx[s] + partner);
+            vz2 = __ldcg(a.t_vz[s] + partner);
+            vt2 = __ldcg(a.t_vy[s] + partner);
+        }
+        r = mcc_collide(m, s, rs, vx, vy, vz, vr2, vz2, vt2, pu, pvx, pvy, pvz);
+    }
+    if (r != MCC_HIT) return MCC_NULL;
+    a.vx[p] = vx;
+    a.vy[p] = vy;
+    a.vz[p] = vz;
+    if (pu && partner >= 0) {
+        a.t_vx[s][partner] = pvx;
+        a.t_vy[s][partner] = pvy;
+        a.t_vz[s][partner] = pvz;
+    }
+    return MCC_HIT;
+}
+
 }  // namespace mag

@@ -15,6 +15,8 @@
 // when collisions are on, id (4 B); write x, z, vx, vy, vz (20 B).  Field
 // faces, mask and the charge grid are small and stay in L1/L2 when the
 // particles are sorted by cell.
+#include <algorithm>
+
 #include "device.hpp"
 #include "kernels.hpp"
 #include "philox.hpp"
@@ -27,21 +29,37 @@ constexpr float kInvOne = 1.0f / (float)(1u << kFracBits);
 constexpr float kOne = (float)(1u << kFracBits);
 constexpr uint32_t kHalf = 1u << (kFracBits - 1);
 
-__device__ __forceinline__ float frac(uint32_t v) { return (float)(v & kFracMask) * kInvOne; }
+// Explicitly rounded arithmetic: a product that is added is an fmaf, every
+// other product and sum is rounded on its own (__fmul_rn, __fadd_rn, which the
+// compiler never contracts).  Every instantiation of the step (slots per
+// thread, field and B variants) then produces the same bits per particle.
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+
+__device__ __forceinline__ float frac(uint32_t v) { return mul((float)(v & kFracMask), kInvOne); }
+__device__ __forceinline__ float cells(uint32_t v) { return add((float)(v >> kFracBits), frac(v)); }
+
+// (1-fx) ((1-fz) a + fz b) + fx ((1-fz) c + fz d)
+__device__ __forceinline__ float lerp4(float a, float b, float c, float d, float fx, float fz)
+{
+    const float ofz = sub(1.f, fz);
+    const float lo = fmaf(fz, b, mul(ofz, a)), hi = fmaf(fz, d, mul(ofz, c));
+    return fmaf(fx, hi, mul(sub(1.f, fx), lo));
+}
 
 __device__ __forceinline__ float bilerp(const float* __restrict__ f, int stride, int i, int j, float fx, float fz)
 {
     const float* p = f + (size_t)i * stride + j;
     const float a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + stride), d = __ldg(p + stride + 1);
-    return (1.f - fx) * ((1.f - fz) * a + fz * b) + fx * ((1.f - fz) * c + fz * d);
+    return lerp4(a, b, c, d, fx, fz);
 }
 
 __device__ __forceinline__ float2 bilerp2(const float2* __restrict__ f, int stride, int i, int j, float fx, float fz)
 {
     const float2* p = f + (size_t)i * stride + j;
     const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + stride), d = __ldg(p + stride + 1);
-    const float w00 = (1.f - fx) * (1.f - fz), w01 = (1.f - fx) * fz, w10 = fx * (1.f - fz), w11 = fx * fz;
-    return make_float2(w00 * a.x + w01 * b.x + w10 * c.x + w11 * d.x, w00 * a.y + w01 * b.y + w10 * c.y + w11 * d.y);
+    return make_float2(lerp4(a.x, b.x, c.x, d.x, fx, fz), lerp4(a.y, b.y, c.y, d.y, fx, fz));
 }
 
 // Stencil of Field2D::grad at fixed-point position (x, z): the x component
@@ -58,9 +76,9 @@ __device__ __forceinline__ GatherIdx gather_idx(uint32_t x, uint32_t z, int nx, 
     g.ix = min((int)(xr >> kFracBits), nx - 1);
     g.fx = frac(xr);
     g.jz = min((int)(z >> kFracBits), nz - 2);
-    g.fz = (float)(z - ((uint32_t)g.jz << kFracBits)) * kInvOne;
+    g.fz = mul((float)(z - ((uint32_t)g.jz << kFracBits)), kInvOne);
     g.iz = min((int)(x >> kFracBits), nx - 2);
-    g.gx = (float)(x - ((uint32_t)g.iz << kFracBits)) * kInvOne;
+    g.gx = mul((float)(x - ((uint32_t)g.iz << kFracBits)), kInvOne);
     g.jz2 = min((int)(zr >> kFracBits), nz - 1);
     g.gz = frac(zr);
     return g;
@@ -71,7 +89,7 @@ __device__ __forceinline__ float table_interp(const float* __restrict__ t, int b
 {
     const int i = max(0, min((int)xi, bnx - 2));
     const int j = max(0, min((int)zi, bnz - 2));
-    return bilerp(t, bnz, i, j, xi - (float)i, zi - (float)j);
+    return bilerp(t, bnz, i, j, sub(xi, (float)i), sub(zi, (float)j));
 }
 
 template <int EMODE>
@@ -89,8 +107,8 @@ __device__ __forceinline__ void gather_E(const PushArgs& a, uint32_t x, uint32_t
     } else {
         const float2 px = bilerp2(a.Exf2, a.nz, g.ix, g.jz, g.fx, g.fz);
         const float2 pz = bilerp2(a.Ezf2, a.nz + 1, g.iz, g.jz2, g.gx, g.gz);
-        ex = px.x + phase * px.y;
-        ez = pz.x + phase * pz.y;
+        ex = fmaf(phase, px.y, px.x);
+        ez = fmaf(phase, pz.y, pz.x);
     }
 }
 
@@ -99,16 +117,15 @@ __device__ __forceinline__ void boris_vectors(const PushArgs& a, uint32_t x, uin
 {
     tx = a.tx, ty = a.ty, tz = a.tz, sx = a.sx, sy = a.sy, sz = a.sz;
     if (a.btab) {
-        const float xc = (float)(x >> kFracBits) + frac(x), zc = (float)(z >> kFracBits) + frac(z);
-        const float xi = (xc * a.gdx + a.gx0 - a.b_x0) * a.b_ix;
-        const float zi = (zc * a.gdz + a.gz0 - a.b_z0) * a.b_iz;
-        tx = table_interp(a.Br, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
-        tz = table_interp(a.Bz, a.bnx, a.bnz, xi, zi) * a.q_dt_2m;
+        const float xi = mul(sub(fmaf(cells(x), a.gdx, a.gx0), a.b_x0), a.b_ix);
+        const float zi = mul(sub(fmaf(cells(z), a.gdz, a.gz0), a.b_z0), a.b_iz);
+        tx = mul(table_interp(a.Br, a.bnx, a.bnz, xi, zi), a.q_dt_2m);
+        tz = mul(table_interp(a.Bz, a.bnx, a.bnz, xi, zi), a.q_dt_2m);
         ty = 0.f;
-        const float f = 2.f / (1.f + tx * tx + ty * ty + tz * tz);
-        sx = tx * f;
-        sy = ty * f;
-        sz = tz * f;
+        const float f = __fdiv_rn(2.f, fmaf(tz, tz, fmaf(tx, tx, 1.f)));
+        sx = mul(tx, f);
+        sy = 0.f;
+        sz = mul(tz, f);
     }
 }
 
@@ -117,19 +134,19 @@ __device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float tx
                                        float sy, float sz)
 {
     if (COORD == 1) {  // (r, theta, z) orientation, particles.cpp:581-592
-        const float vpr = vx + vy * tz - vz * ty;
-        const float vpt = vy + vz * tx - vx * tz;
-        const float vpz = vz + vx * ty - vy * tx;
-        vx += vpt * sz - vpz * sy;
-        vy += vpz * sx - vpr * sz;
-        vz += vpr * sy - vpt * sx;
+        const float vpr = fmaf(-vz, ty, fmaf(vy, tz, vx));
+        const float vpt = fmaf(-vx, tz, fmaf(vz, tx, vy));
+        const float vpz = fmaf(-vy, tx, fmaf(vx, ty, vz));
+        vx = fmaf(-vpz, sy, fmaf(vpt, sz, vx));
+        vy = fmaf(-vpr, sz, fmaf(vpz, sx, vy));
+        vz = fmaf(-vpt, sx, fmaf(vpr, sy, vz));
     } else {  // (x, y, z) ~ (r, z, theta), particles.cpp:968-979
-        const float vpr = vx - vy * tz + vz * ty;
-        const float vpz = vz - vx * ty + vy * tx;
-        const float vpt = vy - vz * tx + vx * tz;
-        vx += -vpt * sz + vpz * sy;
-        vy += -vpz * sx + vpr * sz;
-        vz += -vpr * sy + vpt * sx;
+        const float vpr = fmaf(vz, ty, fmaf(-vy, tz, vx));
+        const float vpz = fmaf(vy, tx, fmaf(-vx, ty, vz));
+        const float vpt = fmaf(vx, tz, fmaf(-vz, tx, vy));
+        vx = fmaf(vpz, sy, fmaf(-vpt, sz, vx));
+        vy = fmaf(vpr, sz, fmaf(-vpz, sx, vy));
+        vz = fmaf(vpt, sx, fmaf(-vpr, sy, vz));
     }
 }
 
@@ -152,89 +169,74 @@ __device__ __forceinline__ bool move_coord(uint32_t& x, int d, uint32_t maxf, bo
 }
 
 // displacement in fixed-point units, clamped so that a wild value is simply "out"
-__device__ __forceinline__ int to_fixed_disp(float cells)
+__device__ __forceinline__ int to_fixed_disp(float c)
 {
-    const float v = fminf(fmaxf(cells * kOne, -1.0e9f), 1.0e9f);
+    const float v = fminf(fmaxf(mul(c, kOne), -1.0e9f), 1.0e9f);
     return __float2int_rn(v);
 }
 
-__device__ __forceinline__ void close_step_if_last(Counters* c, unsigned long long coll, unsigned long long nnull)
+// One particle of the step, in registers.  Returns alive (false: removed at
+// the boundary or in a closed cell) and cand (the collision test fired).
+template <int COORD, int EMODE, bool BFIELD>
+__device__ __forceinline__ void step_particle(const PushArgs& a, uint32_t& x, uint32_t& z, float& vx, float& vy,
+                                              float& vz, uint32_t id, bool& alive, bool& cand)
 {
-    // one thread per block; the last block to arrive finishes the step
-    if (coll) atomicAdd(&c->ncoll, coll);
-    if (nnull) atomicAdd(&c->nnull, nnull);
-    __threadfence();
-    const unsigned long long ticket = atomicAdd(&c->done_blocks, 1ull);
-    if (ticket == gridDim.x - 1) {
-        __threadfence();
-        const unsigned long long live = *((volatile unsigned long long*)&c->live_step);
-        c->live_last = live;
-        c->live_sum += live;
-        c->live_step = 0;
-        c->ncand = 0;
-        c->done_blocks = 0;
-        c->niter += 1;
-        __threadfence();
-    }
-}
-
-// One particle of the step.  Returns the new state through the references;
-// alive / removed / candidate flags drive the counters.
-template <int COORD, int EMODE>
-__device__ __forceinline__ void step_particle(const PushArgs& a, int64_t k, uint32_t& x, uint32_t& z, float& vx,
-                                              float& vy, float& vz, bool& alive, bool& cand)
-{
+    // the test uses only (seed, species, id, step): computed first, off the dependency chain
+    cand = a.coll_threshold != 0u && collision_test_u32(a.seed, a.species, id, a.step) < a.coll_threshold;
     float ex, ez;
     gather_E<EMODE>(a, x, z, a.phase, ex, ez);
-    float tx, ty, tz, sx, sy, sz;
-    boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
     // half acceleration, Boris rotation (Birdsall & Langdon), half acceleration
-    vx += ex * a.hq;
-    vz += ez * a.hq;
-    rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
-    vx += ex * a.hq;
-    vz += ez * a.hq;
+    vx = fmaf(ex, a.hq, vx);
+    vz = fmaf(ez, a.hq, vz);
+    if (BFIELD) {
+        float tx, ty, tz, sx, sy, sz;
+        boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
+        rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
+    }
+    vx = fmaf(ex, a.hq, vx);
+    vz = fmaf(ez, a.hq, vz);
     int dpx;
-    const float dz = vz * a.cz;
+    const float dz = mul(vz, a.cz);
     if (COORD == 1) {
         // push in the local Cartesian frame, map back to r and rotate v (Birdsall p. 338);
         // dr = r' - r = (2 r a + a^2 + b^2) / (r' + r) keeps the fixed-point r exact
-        const float r = (float)(x >> kFracBits) + frac(x);
-        const float ax = vx * a.cx, by = vy * a.cx;
-        const float x2 = r + ax;
-        const float rn = sqrtf(x2 * x2 + by * by);
-        const float den = rn + r;
-        const float dr = den > 0.f ? (ax * (r + x2) + by * by) / den : 0.f;
+        const float r = cells(x);
+        const float ax = mul(vx, a.cx), by = mul(vy, a.cx);
+        const float x2 = add(r, ax);
+        const float b2 = mul(by, by);
+        const float rn = __fsqrt_rn(fmaf(x2, x2, b2));
+        const float den = add(rn, r);
+        const float dr = den > 0.f ? __fdiv_rn(fmaf(ax, add(r, x2), b2), den) : 0.f;
         float sa = 0.f, ca = 1.f;
         if (rn != 0.f) {
-            const float ir = 1.f / rn;
-            sa = by * ir;
-            ca = x2 * ir;
+            const float ir = __fdiv_rn(1.f, rn);
+            sa = mul(by, ir);
+            ca = mul(x2, ir);
         }
         const float t0 = vx;
-        vx = ca * vx + sa * vy;
-        vy = -sa * t0 + ca * vy;
+        vx = fmaf(sa, vy, mul(ca, vx));
+        vy = fmaf(-sa, t0, mul(ca, vy));
         dpx = to_fixed_disp(dr);
         alive = isfinite(dr);
     } else {
-        const float dx = vx * a.cx;
+        const float dx = mul(vx, a.cx);
         dpx = to_fixed_disp(dx);
         alive = isfinite(dx);
     }
     alive = alive && isfinite(dz);
     // boundary (advance_boundary): outside the box -> removed, or wrapped if PERIODIC
     alive = alive && move_coord(x, dpx, a.xmaxf, a.periodic) && move_coord(z, to_fixed_disp(dz), a.zmaxf, a.periodic);
-    cand = false;
-    if (!alive) return;
+    if (!alive) {
+        cand = false;
+        return;
+    }
     const int ic = min((int)(x >> kFracBits), a.nx - 2);
     const int jc = min((int)(z >> kFracBits), a.nz - 2);
-    if (a.check_mask) {
-        const int8_t* m = a.mask + (size_t)ic * a.nz + jc;
-        const bool fr = m[0] == 2 || m[a.nz] == 2 || m[1] == 2 || m[a.nz + 1] == 2;  // FREE
-        if (!fr) {
-            alive = false;
-            return;
-        }
+    // t_grid::is_free: at least one FREE corner, precomputed per cell
+    if (a.check_mask && __ldg(a.cellfree + (size_t)ic * (a.nz - 1) + jc) == 0) {
+        alive = false;
+        cand = false;
+        return;
     }
     if (a.rho != nullptr) {
         const unsigned long long one = 1ull << kDepositShift;
@@ -246,85 +248,140 @@ __device__ __forceinline__ void step_particle(const PushArgs& a, int64_t k, uint
         atomicAdd(r0 + 1, (one - U) * V);
         atomicAdd(r0 + a.nz + 1, U * V);
     }
-    if (a.coll_threshold != 0u) cand = collision_test_u32(a.seed, a.species, a.id[k], a.step) < a.coll_threshold;
 }
 
-__device__ __forceinline__ void append_candidate(const PushArgs& a, bool cand, int64_t k)
+// Warp-aggregated append of a collision candidate: slot index and a record
+// of (vx, vy, vz, id) after the push, so that k_collide needs one load per
+// candidate.
+__device__ __forceinline__ void append_candidate(const PushArgs& a, bool cand, int64_t k, float vx, float vy,
+                                                 float vz, uint32_t id)
 {
     const unsigned full = 0xffffffffu;
     const unsigned cand_mask = __ballot_sync(full, cand);
     if (cand_mask) {
         const int lane = threadIdx.x & 31;
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&a.cnt->ncand, (unsigned long long)__popc(cand_mask));
+        if (lane == 0) base = atomicAdd(&a.cnt->ncand_par[a.slot], (unsigned long long)__popc(cand_mask));
         base = __shfl_sync(full, base, 0);
-        if (cand) a.cand[base + __popc(cand_mask & ((1u << lane) - 1u))] = (uint32_t)k;
+        if (cand) {
+            const unsigned long long c = base + __popc(cand_mask & ((1u << lane) - 1u));
+            a.cand[c] = (uint32_t)k;
+            a.cand_rec[c] = make_float4(vx, vy, vz, __uint_as_float(id));
+        }
     }
 }
 
-// Persistent grid-stride kernel, two particles per thread and iteration (two
-// independent load streams in flight), counters kept in registers and added
-// once per warp at the end.  Collision candidates go to a compacted list that
-// k_collide processes; without collisions this kernel closes the step.
-template <int COORD, int EMODE>
-__global__ void __launch_bounds__(256, 4) k_push(const PushArgs a)
+// VEC consecutive slots as one vector access (slots are allocated in
+// multiples of kSlotAlign, so a group never runs past the arrays).
+template <int VEC> struct Vec;
+template <> struct Vec<1> {
+    using U = uint32_t;
+    using F = float;
+    static __device__ __forceinline__ U ldu(const uint32_t* p, int64_t g) { return __ldcs(p + g); }
+    static __device__ __forceinline__ F ldf(const float* p, int64_t g) { return __ldcs(p + g); }
+    static __device__ __forceinline__ void stu(uint32_t* p, int64_t g, U v) { __stcs(p + g, v); }
+    static __device__ __forceinline__ void stf(float* p, int64_t g, F v) { __stcs(p + g, v); }
+    static __device__ __forceinline__ uint32_t& at(U& v, int) { return v; }
+    static __device__ __forceinline__ float& at(F& v, int) { return v; }
+};
+template <> struct Vec<2> {
+    using U = uint2;
+    using F = float2;
+    static __device__ __forceinline__ U ldu(const uint32_t* p, int64_t g) { return __ldcs((const uint2*)p + g); }
+    static __device__ __forceinline__ F ldf(const float* p, int64_t g) { return __ldcs((const float2*)p + g); }
+    static __device__ __forceinline__ void stu(uint32_t* p, int64_t g, U v) { __stcs((uint2*)p + g, v); }
+    static __device__ __forceinline__ void stf(float* p, int64_t g, F v) { __stcs((float2*)p + g, v); }
+    static __device__ __forceinline__ uint32_t& at(U& v, int j) { return j == 0 ? v.x : v.y; }
+    static __device__ __forceinline__ float& at(F& v, int j) { return j == 0 ? v.x : v.y; }
+};
+template <> struct Vec<4> {
+    using U = uint4;
+    using F = float4;
+    static __device__ __forceinline__ U ldu(const uint32_t* p, int64_t g) { return __ldcs((const uint4*)p + g); }
+    static __device__ __forceinline__ F ldf(const float* p, int64_t g) { return __ldcs((const float4*)p + g); }
+    static __device__ __forceinline__ void stu(uint32_t* p, int64_t g, U v) { __stcs((uint4*)p + g, v); }
+    static __device__ __forceinline__ void stf(float* p, int64_t g, F v) { __stcs((float4*)p + g, v); }
+    static __device__ __forceinline__ uint32_t& at(U& v, int j)
+    {
+        return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
+    }
+    static __device__ __forceinline__ float& at(F& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+};
+
+template <int VEC> constexpr int push_min_blocks() { return VEC == 4 ? 2 : VEC == 2 ? 3 : 4; }
+
+// Persistent grid-stride kernel over groups of VEC consecutive slots: every
+// load of a group (x, z, vx, vy, vz and, with collisions, id) is issued before
+// any of its results is used, as streaming (evict-first) vector accesses, so
+// that each thread keeps 20-24 VEC bytes in flight and the field faces stay in
+// L1.  Collision candidates go to a compacted list (slot and post-push
+// velocity and id) for k_collide, which runs the scatter of each
+// (BaseSpecies::scatter after the push, as Species::advance does).  Counters
+// are reduced per warp and added once at the end; thread 0 of block 0 first
+// folds the previous launch's per-step counters into the totals.
+template <int COORD, int EMODE, bool BFIELD, int VEC>
+__global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __grid_constant__ PushArgs a)
 {
+    using V = Vec<VEC>;
+    // a dependent k_collide may be scheduled and stage its tables now; it
+    // waits for this whole grid before it reads any result
+    asm volatile("griddepcontrol.launch_dependents;");
+    if (a.fold_slot >= 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+        Counters* c = a.cnt;
+        c->live_sum += c->live_par[a.fold_slot];
+        c->live_par[a.fold_slot] = 0;
+        c->ncand_par[a.fold_slot] = 0;
+    }
     const int64_t n = a.n;
+    const int64_t ngroups = (n + VEC - 1) / VEC;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const bool coll = a.coll_threshold != 0u;
     unsigned live = 0, removed = 0;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += 2 * stride) {
-        const int64_t k0 = base + threadIdx.x, k1 = k0 + stride;
-        uint32_t x0 = k0 < n ? a.x[k0] : kDead, x1 = k1 < n ? a.x[k1] : kDead;
-        uint32_t z0 = 0, z1 = 0;
-        float vx0 = 0.f, vy0 = 0.f, vz0 = 0.f, vx1 = 0.f, vy1 = 0.f, vz1 = 0.f;
-        if (x0 != kDead) {
-            z0 = a.z[k0];
-            vx0 = a.vx[k0];
-            vy0 = a.vy[k0];
-            vz0 = a.vz[k0];
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g - threadIdx.x < ngroups; g += stride) {
+        const bool act = g < ngroups;
+        typename V::U X{}, Z{}, ID{};
+        typename V::F VX{}, VY{}, VZ{};
+        if (act) {
+            X = V::ldu(a.x, g);
+            Z = V::ldu(a.z, g);
+            VX = V::ldf(a.vx, g);
+            VY = V::ldf(a.vy, g);
+            VZ = V::ldf(a.vz, g);
+            if (coll) ID = V::ldu(a.id, g);
         }
-        if (x1 != kDead) {
-            z1 = a.z[k1];
-            vx1 = a.vx[k1];
-            vy1 = a.vy[k1];
-            vz1 = a.vz[k1];
+        bool cand[VEC];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            cand[j] = false;
+            const int64_t k = g * VEC + j;
+            uint32_t& x = V::at(X, j);
+            if (!act || k >= n || x == kDead) continue;
+            bool al;
+            step_particle<COORD, EMODE, BFIELD>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j), V::at(VZ, j),
+                                                V::at(ID, j), al, cand[j]);
+            if (!al) x = kDead;
+            live += al;
+            removed += !al;
         }
-        bool al0 = false, c0 = false, al1 = false, c1 = false;
-        if (x0 != kDead) {
-            step_particle<COORD, EMODE>(a, k0, x0, z0, vx0, vy0, vz0, al0, c0);
-            a.x[k0] = al0 ? x0 : kDead;
-            a.z[k0] = z0;
-            a.vx[k0] = vx0;
-            a.vy[k0] = vy0;
-            a.vz[k0] = vz0;
-            live += al0;
-            removed += !al0;
+        if (act) {
+            V::stu(a.x, g, X);
+            V::stu(a.z, g, Z);
+            V::stf(a.vx, g, VX);
+            V::stf(a.vy, g, VY);
+            V::stf(a.vz, g, VZ);
         }
-        if (x1 != kDead) {
-            step_particle<COORD, EMODE>(a, k1, x1, z1, vx1, vy1, vz1, al1, c1);
-            a.x[k1] = al1 ? x1 : kDead;
-            a.z[k1] = z1;
-            a.vx[k1] = vx1;
-            a.vy[k1] = vy1;
-            a.vz[k1] = vz1;
-            live += al1;
-            removed += !al1;
-        }
-        if (a.coll_threshold != 0u) {
-            append_candidate(a, c0, k0);
-            append_candidate(a, c1, k1);
+        if (coll) {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j)
+                append_candidate(a, cand[j], g * VEC + j, V::at(VX, j), V::at(VY, j), V::at(VZ, j), V::at(ID, j));
         }
     }
     const unsigned full = 0xffffffffu;
     live = __reduce_add_sync(full, live);
     removed = __reduce_add_sync(full, removed);
     if ((threadIdx.x & 31) == 0) {
-        if (live) atomicAdd(&a.cnt->live_step, (unsigned long long)live);
+        if (live) atomicAdd(&a.cnt->live_par[a.slot], (unsigned long long)live);
         if (removed) atomicAdd(&a.cnt->removed, (unsigned long long)removed);
-    }
-    if (a.close_step) {
-        __syncthreads();
-        if (threadIdx.x == 0) close_step_if_last(a.cnt, 0, 0);
     }
 }
 
@@ -345,8 +402,8 @@ __global__ void __launch_bounds__(256) k_push_init(const PushArgs a)
     float tx, ty, tz, sx, sy, sz;
     boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
     rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
-    vx += ex * a.hq;
-    vz += ez * a.hq;
+    vx = fmaf(ex, a.hq, vx);
+    vz = fmaf(ez, a.hq, vz);
     a.vx[k] = vx;
     a.vy[k] = vy;
     a.vz[k] = vz;
@@ -372,27 +429,67 @@ __global__ void __launch_bounds__(256) k_deposit(const PushArgs a)
     atomicAdd(r0 + a.nz + 1, U * V);
 }
 
-template <int COORD>
-void launch_push_t(const PushArgs& a, cudaStream_t s, bool init)
+// Persistent launch: as many blocks as fit on the device at once (occupancy of
+// this instantiation x SMs), reduced so that every thread runs the same number
+// of grid-stride iterations.
+template <int COORD, int EMODE, bool BFIELD, int VEC>
+void launch_step(const PushArgs& a, int sm_count, cudaStream_t s)
 {
-    const unsigned grid = (unsigned)((a.n + 255) / 256);
-    if (grid == 0) return;
-    // the step kernel runs a persistent grid: at most 8 blocks per SM of the 152
-    const unsigned pgrid = (unsigned)std::min<int64_t>((a.n + 511) / 512, 152 * 8);
+    static int per_sm = 0;  // resident blocks per SM of this instantiation
+    if (per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_push<COORD, EMODE, BFIELD, VEC>, 256, 0) !=
+                cudaSuccess ||
+            b < 1)
+            b = 1;
+        per_sm = b;
+    }
+    const int64_t groups = (a.n + VEC - 1) / VEC;
+    const int64_t resident = (int64_t)per_sm * std::max(sm_count, 1);
+    const int64_t needed = (groups + 255) / 256;
+    const int64_t iters = (needed + resident - 1) / resident;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, (needed + iters - 1) / iters);
+    k_push<COORD, EMODE, BFIELD, VEC><<<grid, 256, 0, s>>>(a);
+}
+
+template <int COORD, int EMODE, bool BFIELD>
+void launch_step_vec(const PushArgs& a, int vec, int sm_count, cudaStream_t s)
+{
+    switch (vec) {
+    case 1: launch_step<COORD, EMODE, BFIELD, 1>(a, sm_count, s); break;
+    case 2: launch_step<COORD, EMODE, BFIELD, 2>(a, sm_count, s); break;
+    default: launch_step<COORD, EMODE, BFIELD, 4>(a, sm_count, s); break;
+    }
+}
+
+template <int COORD, int EMODE>
+void launch_push_e(const PushArgs& a, bool init, int vec, int sm_count, cudaStream_t s)
+{
+    if (init) {
+        k_push_init<COORD, EMODE><<<(unsigned)((a.n + 255) / 256), 256, 0, s>>>(a);
+        return;
+    }
+    if (a.has_b) launch_step_vec<COORD, EMODE, true>(a, vec, sm_count, s);
+    else launch_step_vec<COORD, EMODE, false>(a, vec, sm_count, s);
+}
+
+template <int COORD>
+void launch_push_t(const PushArgs& a, bool init, int vec, int sm_count, cudaStream_t s)
+{
     switch (a.emode) {
-    case 0: init ? k_push_init<COORD, 0><<<grid, 256, 0, s>>>(a) : k_push<COORD, 0><<<pgrid, 256, 0, s>>>(a); break;
-    case 1: init ? k_push_init<COORD, 1><<<grid, 256, 0, s>>>(a) : k_push<COORD, 1><<<pgrid, 256, 0, s>>>(a); break;
-    default: init ? k_push_init<COORD, 2><<<grid, 256, 0, s>>>(a) : k_push<COORD, 2><<<pgrid, 256, 0, s>>>(a); break;
+    case 0: launch_push_e<COORD, 0>(a, init, vec, sm_count, s); break;
+    case 1: launch_push_e<COORD, 1>(a, init, vec, sm_count, s); break;
+    default: launch_push_e<COORD, 2>(a, init, vec, sm_count, s); break;
     }
 }
 
 }  // namespace
 
-int launch_push(const PushArgs& a, int coord, bool init, cudaStream_t s)
+int launch_push(const PushArgs& a, int coord, bool init, int vec, int sm_count, cudaStream_t s)
 {
     if (a.n == 0) return 0;
-    if (coord == 1) launch_push_t<1>(a, s, init);
-    else launch_push_t<0>(a, s, init);
+    if (coord == 1) launch_push_t<1>(a, init, vec, sm_count, s);
+    else launch_push_t<0>(a, init, vec, sm_count, s);
     return 1;
 }
 

@@ -58,6 +58,9 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     poisson_tol = opts.poisson_tol > 0 ? opts.poisson_tol : 1e-12;
     poisson_max_iter = opts.poisson_max_iter > 0 ? opts.poisson_max_iter : 200;
     sort_interval = opts.sort_interval == 0 ? 20 : opts.sort_interval;
+    push_vec = opts.push_vec == 1 || opts.push_vec == 2 || opts.push_vec == 4 ? opts.push_vec : 2;
+    if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sm_count < 1)
+        sm_count = 1;
     p = make_param(KeyValueConfig::from_file(config));
     if (p.mover != ADVANCE_BORIS)
         throw Error(-1, "mover ADVANCE_MULTICOLL is not provided by this library (Boris mover only)");
@@ -174,6 +177,16 @@ void Sim::setup_fields()
     sort_blocksum.alloc(((size_t)(nx - 1) * (nz - 1) + 1023) / 1024 + 1);
     d_mask.upload(mask.data(), mask.size(), stream);
     d_volt.upload(voltage.data(), voltage.size(), stream);
+    {  // t_grid::is_free per cell (src/fields.hpp:94-101): one of the four corner nodes is FREE
+        std::vector<uint8_t> cf((size_t)(nx - 1) * (nz - 1), 1);
+        if (check_mask)
+            for (int i = 0; i + 1 < nx; ++i)
+                for (int j = 0; j + 1 < nz; ++j) {
+                    const int8_t* m = mask.data() + (size_t)i * nz + j;
+                    cf[(size_t)i * (nz - 1) + j] = (m[0] == 2 || m[nz] == 2 || m[1] == 2 || m[nz + 1] == 2) ? 1 : 0;
+                }
+        d_cellfree.upload(cf.data(), cf.size(), stream);
+    }
     if (p.geometry == GEO_EMPTY && !p.selfconsistent) emode = 0;
     else emode = p.rf ? 2 : 1;
     if (!p.magnetic_field_const) {
@@ -425,7 +438,8 @@ void Sim::ensure_capacity(int s, int64_t need)
 {
     SpeciesState& S = sp[s];
     if (need <= S.cap) return;
-    const int64_t cap = std::max<int64_t>(need, (int64_t)(S.cap * 1.5) + 1024);
+    int64_t cap = std::max<int64_t>(need, (int64_t)(S.cap * 1.5) + 1024);
+    cap = (cap + kSlotAlign - 1) / kSlotAlign * kSlotAlign;  // whole vector groups
     MAG_CK(cudaStreamSynchronize(stream));
     auto grow = [&](auto& a) {
         typename std::remove_reference<decltype(a)>::type b;
@@ -442,6 +456,7 @@ void Sim::ensure_capacity(int s, int64_t need)
     grow(S.vz);
     grow(S.id);
     S.cand.alloc(cap);
+    S.cand_rec.alloc(cap);
     S.bx.release();  // sort buffers are re-made at the next sort
     S.bz.release();
     S.bvx.release();
@@ -557,6 +572,7 @@ PushArgs Sim::push_args(int s, bool init)
     a.periodic = p.boundary == BND_PERIODIC ? 1 : 0;
     a.check_mask = check_mask ? 1 : 0;
     a.mask = d_mask.p;
+    a.cellfree = d_cellfree.p;
     a.emode = emode;
     a.Exf = Exf.p;
     a.Ezf = Ezf.p;
@@ -584,6 +600,7 @@ PushArgs Sim::push_args(int s, bool init)
     a.sy = (float)(ty * f);
     a.sz = (float)(tz * f);
     a.btab = p.magnetic_field_const ? 0 : 1;
+    a.has_b = (a.btab || p.Br != 0.0 || p.Bt != 0.0 || p.Bz != 0.0) ? 1 : 0;
     a.Br = d_Br.p;
     a.Bz = d_Bz.p;
     a.bnx = bnx;
@@ -600,19 +617,27 @@ PushArgs Sim::push_args(int s, bool init)
     a.cz = (float)(dt / dz);
     a.rho = p.selfconsistent ? S.rho.p : nullptr;
     a.coll_threshold = init ? 0u : S.threshold;
-    a.coll_mode = init ? 0 : coll_mode(s);
     a.cand = S.cand.p;
+    a.cand_rec = S.cand_rec.p;
     a.mcc = S.mcc.p;
     a.seed = seed;
     a.species = (uint32_t)s;
     a.cnt = S.cnt.p;
-    a.close_step = a.coll_mode == 2 ? 0 : 1;
+    a.slot = 0;
+    a.fold_slot = -1;
     return a;
 }
 
-// 0: no collisions (the particle kernel closes the step), 2: candidate list
-// processed by k_collide, which closes the step
+// 0: no collisions; 2: the particle kernel lists candidates, k_collide runs them
 int Sim::coll_mode(int s) const { return sp[s].threshold == 0 ? 0 : 2; }
+
+bool Sim::any_target_slots(int s) const
+{
+    const SpeciesState& S = sp[s];
+    for (size_t t = 0; t < sp.size() && t < S.rates.size(); ++t)
+        if (S.rates[t] > 0.0 && sp[t].n_slots > 0) return true;
+    return false;
+}
 
 CollideArgs Sim::collide_args(int s)
 {
@@ -621,10 +646,14 @@ CollideArgs Sim::collide_args(int s)
     a.vx = S.vx.p;
     a.vy = S.vy.p;
     a.vz = S.vz.p;
-    a.id = S.id.p;
     a.cand = S.cand.p;
+    a.cand_rec = S.cand_rec.p;
     a.cnt = S.cnt.p;
     a.mcc = S.mcc.p;
+    a.inter = d_inter.p;
+    a.n_inter = (int)d_inter.n;
+    a.tables = d_tables.p;
+    a.n_tables = (int)d_tables.n;
     for (size_t t = 0; t < sp.size(); ++t) {
         a.t_has_slots[t] = sp[t].n_slots > 0 ? 1 : 0;
         a.t_x[t] = sp[t].x.p;
@@ -633,6 +662,7 @@ CollideArgs Sim::collide_args(int s)
         a.t_vz[t] = sp[t].vz.p;
         a.t_n[t] = sp[t].n_slots;
     }
+    a.any_target_slots = any_target_slots(s) ? 1 : 0;
     a.seed = seed;
     a.species = (uint32_t)s;
     a.step = S.niter;
@@ -682,57 +712,72 @@ void Sim::sort_species(int s)
     std::swap(S.id, S.bid);
 }
 
-// One Pic::advance (src/pic.cpp:330-358).  With ev != nullptr, events
-// ev[0..3] are recorded before the solve, after the solve, after the particle
-// kernels and after the collision kernels.
-void Sim::step(cudaEvent_t* ev)
+// One Pic::advance (src/pic.cpp:330-358).  Species advance in order, each
+// with its collisions (as Species::advance runs scatter inside the push loop).
+// With ms != nullptr, events split the step into sort, solve, particle
+// kernels and collision kernels and the four device times are added to ms
+// (an event between a particle kernel and its collision kernel removes their
+// overlap, so the split costs a little time).
+void Sim::step(double* ms)
 {
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> kind;  // window of the interval that ends at each event
+    auto mark = [&](int k) {
+        if (!ms) return;
+        cudaEvent_t e;
+        MAG_CK(cudaEventCreate(&e));
+        MAG_CK(cudaEventRecord(e, stream));
+        ev.push_back(e);
+        kind.push_back(k);
+    };
+    mark(-1);
     if (sort_interval > 0 && (sort_due || steps_done % (uint64_t)sort_interval == 0)) {
         for (size_t s = 0; s < sp.size(); ++s) sort_species((int)s);
         sort_due = false;
     }
     ++steps_done;
-    if (ev) MAG_CK(cudaEventRecord(ev[0], stream));
+    mark(0);
     if (p.selfconsistent) solve(false, rho_override ? 2 : 1, true, false);
     rho_override = false;
-    if (ev) MAG_CK(cudaEventRecord(ev[1], stream));
+    mark(1);
     for (size_t s = 0; s < sp.size(); ++s) {
         SpeciesState& S = sp[s];
-        if (S.n_slots == 0) continue;
-        PushArgs pa = push_args((int)s, false);
-        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, false, stream);
-    }
-    if (ev) MAG_CK(cudaEventRecord(ev[2], stream));
-    for (size_t s = 0; s < sp.size(); ++s) {
-        SpeciesState& S = sp[s];
-        if (S.n_slots > 0 && coll_mode((int)s) == 2) {
-            const double expect = (double)S.n_slots * S.prob;
-            const int grid = (int)std::min<double>(304.0, std::ceil(4.0 * expect / 128.0) + 1.0);
-            launches += launch_collide(collide_args((int)s), grid, stream);
+        if (S.n_slots == 0) {
+            S.niter++;
+            continue;
         }
+        PushArgs pa = push_args((int)s, false);
+        pa.slot = (int)(S.launches & 1);
+        pa.fold_slot = S.launches > 0 ? (int)((S.launches - 1) & 1) : -1;
+        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, false, push_vec, sm_count, stream);
+        mark(2);
+        if (coll_mode((int)s) == 2) {
+            CollideArgs ca = collide_args((int)s);
+            ca.slot = pa.slot;
+            const double expect = (double)S.n_slots * S.prob;
+            const int grid = (int)std::min<double>(4.0 * sm_count, std::ceil(4.0 * expect / 128.0) + 1.0);
+            launches += launch_collide(ca, grid, stream);
+            mark(3);
+        }
+        S.launches++;
         S.niter++;
     }
-    if (ev) MAG_CK(cudaEventRecord(ev[3], stream));
+    if (ms) {
+        MAG_CK(cudaEventSynchronize(ev.back()));
+        for (size_t k = 1; k < ev.size(); ++k) {
+            float t = 0.f;
+            MAG_CK(cudaEventElapsedTime(&t, ev[k - 1], ev[k]));
+            ms[kind[k]] += t;
+        }
+        for (auto e : ev) cudaEventDestroy(e);
+    }
 }
 
-void Sim::advance_timed(uint64_t nsteps, double* ms3)
+void Sim::advance_timed(uint64_t nsteps, double* ms4)
 {
     MAG_CK(cudaSetDevice(device));
-    cudaEvent_t ev[4];
-    for (auto& e : ev) MAG_CK(cudaEventCreate(&e));
-    ms3[0] = ms3[1] = ms3[2] = 0.0;
-    for (uint64_t k = 0; k < nsteps; ++k) {
-        step(ev);
-        MAG_CK(cudaEventSynchronize(ev[3]));
-        float a, b, c;
-        MAG_CK(cudaEventElapsedTime(&a, ev[0], ev[1]));
-        MAG_CK(cudaEventElapsedTime(&b, ev[1], ev[2]));
-        MAG_CK(cudaEventElapsedTime(&c, ev[2], ev[3]));
-        ms3[0] += a;
-        ms3[1] += b;
-        ms3[2] += c;
-    }
-    for (auto& e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 4; ++k) ms4[k] = 0.0;
+    for (uint64_t k = 0; k < nsteps; ++k) step(ms4);
 }
 
 void Sim::advance(uint64_t nsteps)
@@ -753,7 +798,7 @@ void Sim::advance_init()
     for (size_t s = 0; s < sp.size(); ++s) {
         if (sp[s].n_slots == 0) continue;
         PushArgs pa = push_args((int)s, true);
-        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, true, stream);
+        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, true, push_vec, sm_count, stream);
     }
     MAG_CK(cudaGetLastError());
 }
@@ -896,6 +941,8 @@ Counters Sim::counters(int s)
     Counters c{};
     MAG_CK(cudaStreamSynchronize(stream));
     MAG_CK(cudaMemcpy(&c, sp[s].cnt.p, sizeof c, cudaMemcpyDeviceToHost));
+    // the last launch's per-step counts are folded by the next launch only
+    if (sp[s].launches > 0) c.live_sum += c.live_par[(sp[s].launches - 1) & 1];
     return c;
 }
 

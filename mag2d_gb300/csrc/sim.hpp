@@ -72,6 +72,7 @@ struct SimOptions {
     double poisson_tol = 1e-12;
     int poisson_max_iter = 200;
     int64_t capacity_hint = 0;
+    int push_vec = 0;       // slots per thread of the particle kernel: 1, 2 or 4 (0: 2)
 };
 
 struct SpeciesState {
@@ -82,6 +83,7 @@ struct SpeciesState {
     std::vector<std::vector<int>> by_target;  // interaction indices per target species
     // device particles (x, z fixed point, see device.hpp) and their sort double buffers
     DevArray<uint32_t> x, z, id, cand;
+    DevArray<float4> cand_rec;
     DevArray<float> vx, vy, vz;
     DevArray<uint32_t> bx, bz, bid;
     DevArray<float> bvx, bvy, bvz;
@@ -91,6 +93,7 @@ struct SpeciesState {
     DevArray<unsigned long long> rho;  // fixed-point charge grid
     DevArray<Counters> cnt;
     uint64_t niter = 0;                // steps advanced (Species::advance niter++, particles.hpp:347)
+    uint64_t launches = 0;             // particle kernel launches (parity of the per-step counters)
     int inter_off = 0;                 // first entry of this species in the device interaction list
 };
 
@@ -108,7 +111,7 @@ public:
     void run_initscript(const std::string& path);
     void advance_init();
     void advance(uint64_t nsteps);
-    void advance_timed(uint64_t nsteps, double* ms3);
+    void advance_timed(uint64_t nsteps, double* ms4);
     int sync();  // returns first device error code (0 = none)
 
     // accessors used by the C ABI
@@ -129,6 +132,8 @@ public:
     bool rho_override = false;
     SolveStatus last_solve{};
     int sort_interval = 20;
+    int push_vec = 2;
+    int sm_count = 1;
     uint64_t steps_done = 0;
     bool sort_due = true;
 
@@ -150,6 +155,7 @@ private:
     int emode = 1;
     bool check_mask = true;
     DevArray<int8_t> d_mask;
+    DevArray<uint8_t> d_cellfree;
     DevArray<double> d_volt, u64, urf64, b64, rho64, red;
     DevArray<float> Exf, Ezf, Exf_rf, Ezf_rf, d_Br, d_Bz;
     DevArray<float2> Exf2, Ezf2;
@@ -174,11 +180,12 @@ private:
     void add_single(int s, double x, double z, double vx, double vy, double vz);
     PushArgs push_args(int s, bool init);
     CollideArgs collide_args(int s);
-    void step(cudaEvent_t* ev = nullptr);
+    void step(double* ms = nullptr);
     void sort_species(int s);
     void refresh_rf_pairs();
     void upload_slots(int s);
     int coll_mode(int s) const;
+    bool any_target_slots(int s) const;
 };
 
 }  // namespace mag

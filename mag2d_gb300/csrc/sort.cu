@@ -115,33 +115,58 @@ __global__ void __launch_bounds__(1024) k_scan_add(const SortArgs a)
 
 // Every slot k >= total of the destination is marked removed, so all slots
 // below the host's slot count are either live or removed in both buffers.
-__global__ void k_cell_scatter(const SortArgs a, long long n_src)
+// Each thread moves SP particles per pass: all their loads and all their
+// counter atomics are issued before any result is used, so the atomic round
+// trips overlap.
+constexpr int SP = 2;
+__global__ void __launch_bounds__(256) k_cell_scatter(const SortArgs a, long long n_src)
 {
-    const long long total = a.offset[a.ncells];
+    const long long total = __ldg(&a.offset[a.ncells]);
     const int lane = threadIdx.x & 31;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < n_src; base += (long long)gridDim.x * blockDim.x) {
-        const long long k = base + threadIdx.x;
-        if (k < n_src && k >= total) a.ox[k] = kDead;
-        const uint32_t x = k < n_src ? a.x[k] : kDead;
-        const bool valid = x != kDead;
-        const unsigned vm = __ballot_sync(0xffffffffu, valid);
-        if (!valid) continue;
-        const uint32_t z = a.z[k];
-        const int c = cell_of(x, z, a.nx, a.nz);
-        // one atomic per run of equal cells in the warp; lanes take the slots below the old count
-        const unsigned peers = __match_any_sync(vm, c);
-        const int leader = __ffs(peers) - 1;
-        uint32_t old = 0;
-        if (lane == leader) old = atomicSub(&a.count[c], (unsigned)__popc(peers));
-        old = __shfl_sync(peers, old, leader);
-        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-        const uint32_t pos = a.offset[c] + old - 1u - rank;
-        a.ox[pos] = x;
-        a.oz[pos] = z;
-        a.ovx[pos] = a.vx[k];
-        a.ovy[pos] = a.vy[k];
-        a.ovz[pos] = a.vz[k];
-        a.oid[pos] = a.id[k];
+    const long long span = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n_src; base += SP * span) {
+        uint32_t x[SP], z[SP], id[SP];
+        float vx[SP], vy[SP], vz[SP];
+        long long k[SP];
+        int c[SP];
+        unsigned peers[SP];
+        uint32_t old[SP];
+#pragma unroll
+        for (int q = 0; q < SP; ++q) {
+            k[q] = base + q * span + threadIdx.x;
+            const bool in = k[q] < n_src;
+            if (in && k[q] >= total) a.ox[k[q]] = kDead;
+            x[q] = in ? a.x[k[q]] : kDead;
+            z[q] = in ? a.z[k[q]] : 0u;
+            vx[q] = in ? a.vx[k[q]] : 0.f;
+            vy[q] = in ? a.vy[k[q]] : 0.f;
+            vz[q] = in ? a.vz[k[q]] : 0.f;
+            id[q] = in ? a.id[k[q]] : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < SP; ++q) {
+            // one atomic per run of equal cells in the warp; lanes take the slots below the old count
+            const bool valid = x[q] != kDead;
+            const unsigned vm = __ballot_sync(0xffffffffu, valid);
+            c[q] = valid ? cell_of(x[q], z[q], a.nx, a.nz) : -1;
+            peers[q] = __match_any_sync(0xffffffffu, c[q]);
+            old[q] = 0;
+            if (valid && lane == __ffs(peers[q]) - 1) old[q] = atomicSub(&a.count[c[q]], (unsigned)__popc(peers[q]));
+            (void)vm;
+        }
+#pragma unroll
+        for (int q = 0; q < SP; ++q) {
+            const uint32_t o = __shfl_sync(0xffffffffu, old[q], __ffs(peers[q]) - 1);
+            if (x[q] == kDead) continue;
+            const uint32_t rank = __popc(peers[q] & ((1u << lane) - 1u));
+            const uint32_t pos = __ldg(&a.offset[c[q]]) + o - 1u - rank;
+            a.ox[pos] = x[q];
+            a.oz[pos] = z[q];
+            a.ovx[pos] = vx[q];
+            a.ovy[pos] = vy[q];
+            a.ovz[pos] = vz[q];
+            a.oid[pos] = id[q];
+        }
     }
 }
 
@@ -156,7 +181,7 @@ int launch_sort(const SortArgs& a, long long n_src, cudaStream_t s)
     k_scan_local<<<nb, 1024, 0, s>>>(a);
     k_scan_top<<<1, 1024, 0, s>>>(a, nb);
     k_scan_add<<<nb, 1024, 0, s>>>(a);
-    k_cell_scatter<<<grid, 256, 0, s>>>(a, n_src);
+    k_cell_scatter<<<(int)std::min<long long>((n_src + 2 * 256 - 1) / (2 * 256), 152 * 8), 256, 0, s>>>(a, n_src);
     return 5;
 }
 

@@ -156,9 +156,9 @@ class Pic:
 
     def __init__(self, config, species_conf, initscript=None, *, seed: int = 1, device: int = 0,
                  poisson_tol: float = 0.0, poisson_max_iter: int = 0, capacity_hint: int = 0,
-                 sort_interval: int = 0):
+                 sort_interval: int = 0, push_vec: int = 0):
         opts = MagOpts(device=device, seed=seed, sort_interval=sort_interval, poisson_tol=poisson_tol,
-                       poisson_max_iter=poisson_max_iter, capacity_hint=capacity_hint)
+                       poisson_max_iter=poisson_max_iter, capacity_hint=capacity_hint, push_vec=push_vec)
         h = ctypes.c_void_p()
         ini = str(initscript).encode() if initscript else None
         check(lib().mag_create(str(config).encode(), str(species_conf).encode(), ini, ctypes.byref(opts),
@@ -195,8 +195,8 @@ class Pic:
         check(lib().mag_advance(self.h, n))
 
     def advance_timed(self, n: int = 1):
-        """advance(n) with per-kernel CUDA event timing: (solve_ms, particle_ms, collide_ms)."""
-        ms = np.zeros(3)
+        """advance(n) with CUDA event timing: (sort_ms, solve_ms, particle_ms, collide_ms)."""
+        ms = np.zeros(4)
         check(lib().mag_advance_timed(self.h, n, _dp(ms)))
         return tuple(ms)
 

@@ -208,10 +208,12 @@ def test_sort_does_not_change_results(m, tmp_path):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
-def test_mcc_candidate_list_path(m, tmp_path):
+@pytest.mark.parametrize("n", [20_000, 200_000], ids=["500_per_step", "5000_per_step"])
+def test_mcc_candidate_list_path(m, tmp_path, n):
     """Charge exchange with a neutral background and Coulomb collisions with a
     second ion species that holds particles (partner = random live particle):
-    collision counts against the oracle within 3 sigma."""
+    collision counts against the oracle within 3 sigma, with about 500 and
+    about 5000 candidates per step."""
     from mag2d_cases import AMU, QE, write_config, write_species_conf
 
     cfg = dict(coord="CARTESIAN", boundary="PERIODIC", geometry="EMPTY", x_max=1e-2, z_max=1e-2, x_sampl=9,
@@ -227,7 +229,7 @@ def test_mcc_candidate_list_path(m, tmp_path):
     cpath = write_config(cfg, tmp_path / "c.txt")
     spath = write_species_conf(sp, inter, tmp_path / "s.txt")
     rng = np.random.default_rng(4)
-    n, steps = 20000, 50
+    steps = 50
     vth = np.sqrt(1.380662e-23 * 3000.0 / (40 * AMU))
     def parts(mass):
         v = np.sqrt(1.380662e-23 * 3000.0 / mass)
@@ -251,3 +253,42 @@ def test_mcc_candidate_list_path(m, tmp_path):
         assert ref > 100
         assert abs(cand - ref) < 3 * math.sqrt(2 * ref), (s, cand, ref)
     pic.close()
+
+
+@pytest.mark.parametrize("case", ["multipole_mcc", "penning_b"])
+def test_push_variants_bit_identical(m, tmp_path, case):
+    """The particle kernel's slots-per-thread variants (1, 2, 4) run the same
+    per-particle arithmetic and the same keyed random streams: identical
+    particles, counters and charge after 100 steps, with collisions (22-pole
+    trap) and with a magnetic field and self-consistent deposit (Penning)."""
+    from cases import multipole_xy, penning_rz
+
+    combos = [1, 2, 4]
+    out = []
+    for vec in combos:
+        if case == "multipole_mcc":
+            cfg, species, inter, cpath, spath, parts, loaded = multipole_xy(tmp_path, n=10_001, n_nodes=129,
+                                                                            pressure=5.0)
+            pic = m.Pic(cpath, spath, seed=3, push_vec=vec)
+            sp = pic.speclist[1]
+        else:
+            cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=10_001)
+            pic = m.Pic(cpath, spath, seed=3, push_vec=vec)
+            sp = pic.speclist[0]
+        sp.set_particles(*parts)
+        pic.advance_init()
+        pic.advance(100)
+        g = sp.particles()
+        d = sp.diag()
+        order = np.argsort(g["id"])
+        out.append(({k: v[order] for k, v in g.items()}, d, sp.rho_fixed() if case == "penning_b" else None))
+        pic.close()
+    if case == "multipole_mcc":
+        assert out[0][1]["collisions"] > 50
+    for vec, (g, d, r) in zip(combos[1:], out[1:]):
+        for k in ("id", "x", "z", "vx", "vy", "vz"):
+            assert np.array_equal(g[k], out[0][0][k]), (vec, k)
+        for k in ("n_live", "collisions", "null_collisions", "removed", "particle_steps"):
+            assert d[k] == out[0][1][k], (vec, k)
+        if r is not None:
+            assert np.array_equal(r, out[0][2])
