@@ -133,6 +133,12 @@ int mag_set_field(mag_sim* sim, int which, const double* host_in);
  * rho (MAG_RHO) exactly as a self-consistent step does. */
 int mag_field_solve(mag_sim* sim, mag_solve_info* info);
 
+/* Status of the most recent Poisson solve (the one of the last self-consistent
+ * step, or of mag_field_solve): outer FP64 refinement iterations, final
+ * residual, convergence.  Synchronises.  No reference counterpart (UMFPACK's
+ * direct solve has no iteration count). */
+int mag_solve_status(mag_sim* sim, mag_solve_info* info);
+
 /* Live particles of a species as SoA doubles in SI units (the t_particle
  * fields x, z, vx, vy, vz of src/particles.hpp:26-33) plus a persistent id.
  * Any pointer may be NULL.  *n_out receives the number written (<= cap). */

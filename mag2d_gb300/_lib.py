@@ -70,6 +70,7 @@ def lib() -> ctypes.CDLL:
     L.mag_advance.argtypes = [P, ctypes.c_uint64]
     L.mag_sync.argtypes = [P]
     L.mag_advance_timed.argtypes = [P, ctypes.c_uint64, D]
+    L.mag_solve_status.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
     L.mag_grid.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), D, D, D, D]
     L.mag_n_species.argtypes = [P]
     L.mag_species.argtypes = [P, ctypes.c_int, ctypes.POINTER(MagSpeciesInfo)]

@@ -222,6 +222,21 @@ int mag_field_solve(mag_sim* sim, mag_solve_info* info)
     });
 }
 
+int mag_solve_status(mag_sim* sim, mag_solve_info* info)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!info) throw mag::Error(MAG_EINVAL, "null argument");
+        int rc = device_status(sim);  // synchronises and refreshes the last solve's status
+        const mag::SolveStatus st = sim->s->last_solve;
+        info->iterations = st.iterations;
+        info->residual = st.residual;
+        info->status = st.converged ? MAG_OK : MAG_ENOTCONV;
+        info->levels = sim->s->solver_levels();
+        return rc;
+    });
+}
+
 int mag_get_particles(mag_sim* sim, int species, int64_t cap, double* x, double* z, double* vx, double* vy,
                       double* vz, uint32_t* id, int64_t* n_out)
 {

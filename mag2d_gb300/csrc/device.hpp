@@ -25,6 +25,7 @@ namespace mag {
 constexpr int kMaxSpecies = 16;
 constexpr int kMaxInteractions = 64;
 constexpr int kMaxLevels = 12;
+constexpr long long kSingleBlockNodes = 70000;  // grids (and levels) up to this size run on one block
 constexpr int kFracBits = 20;      // fixed-point fraction of a cell in the positions
 constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis (= kFracBits)
 constexpr uint32_t kFracMask = (1u << kFracBits) - 1u;
@@ -201,7 +202,12 @@ struct SolveArgs {
     const double* rho64;
     int clear_rho;
     double mpf, dV;         // macroparticle_factor, cell volume (Cartesian scaling)
+    const double* st64;     // fine stencil per row i: (w, e, c, 1/c), FP64 (4 * nx)
+    const float* st32;      // the same in FP32 for the smoother
+    double k2;              // s/n coefficient of the fine stencil
     int nlev;
+    int l_single;           // multi-block solves: first level run by block 0 alone (0: none)
+    const float* coarse_inv;  // dense inverse of the coarsest level, column-major (null: smooth it)
     MGLevelDev lev[kMaxLevels];
     int nu1, nu2, ncoarse;
     float omega;            // SOR factor for the one-level smoother

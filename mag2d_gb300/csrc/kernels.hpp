@@ -17,6 +17,9 @@ int launch_sort(const SortArgs& a, long long n_src, cudaStream_t s);
 // whole FP64-refined multigrid solve in one kernel; nblocks > 1 uses a
 // cooperative launch with a bounded grid barrier
 int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s);
+// blocks of 1024 threads a cooperative launch of the solve can have (1 when
+// the device cannot launch cooperatively)
+int solve_max_blocks(int sm_count);
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s);
 int launch_load_disk(uint32_t* x, uint32_t* z, float* vx, float* vy, float* vz, uint32_t* id, int64_t n,
                      uint32_t id0, int kind, double cx, double cz, double radius, double zlo, double zhi,

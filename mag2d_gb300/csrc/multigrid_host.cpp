@@ -1,6 +1,9 @@
 // Host set-up of the multigrid hierarchy (see multigrid_host.hpp).
 #include "multigrid_host.hpp"
 
+#include <cmath>
+#include <utility>
+
 namespace mag {
 
 namespace {
@@ -105,10 +108,80 @@ void multigrid_levels(int nx, int nz, int max_levels, std::vector<int>& lnx, std
     lnx.assign(1, nx);
     lnz.assign(1, nz);
     while ((int)lnx.size() < max_levels && (lnx.back() - 1) % 2 == 0 && (lnz.back() - 1) % 2 == 0 && lnx.back() >= 5 &&
-           lnz.back() >= 5) {
+           lnz.back() >= 5 && (long long)lnx.back() * lnz.back() > kDenseCoarseMax) {
         lnx.push_back((lnx.back() - 1) / 2 + 1);
         lnz.push_back((lnz.back() - 1) / 2 + 1);
     }
+}
+
+void fine_stencil_table(int coord, int nx, double dx, double dz, std::vector<double>& st, double& k2)
+{
+    st.assign(4 * (size_t)nx, 0.0);
+    k2 = coord == 1 ? 1.0 / (dz * dz) : 1.0;
+    for (int i = 0; i < nx; ++i) {
+        double w, e, c;
+        if (coord != 1) {
+            w = 1.0;
+            e = 1.0;
+            c = -4.0;
+        } else if (i == 0) {
+            const double k3 = 1.0 / (dx * dx * 0.25);
+            w = 0.0;
+            e = k3;
+            c = -2.0 * k2 - k3;
+        } else {
+            const double k1 = (i - 0.5) / (dx * dx * i), k3 = (i + 0.5) / (dx * dx * i);
+            w = k1;
+            e = k3;
+            c = -2.0 * k2 - k1 - k3;
+        }
+        st[4 * i] = w;
+        st[4 * i + 1] = e;
+        st[4 * i + 2] = c;
+        st[4 * i + 3] = 1.0 / c;
+    }
+}
+
+bool dense_inverse(int nx, int nz, const std::vector<double>& A9, std::vector<float>& inv)
+{
+    const int n = nx * nz;
+    std::vector<double> M((size_t)n * 2 * n, 0.0);  // [A | I], row-major, row length 2n
+    const size_t w = 2 * (size_t)n;
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) {
+            const int r = i * nz + j;
+            for (int di = -1; di <= 1; ++di)
+                for (int dj = -1; dj <= 1; ++dj) {
+                    const int ii = i + di, jj = j + dj;
+                    if (ii < 0 || ii >= nx || jj < 0 || jj >= nz) continue;
+                    M[r * w + (size_t)(ii * nz + jj)] = A9[(size_t)plane(di, dj) * n + r];
+                }
+            M[r * w + n + r] = 1.0;
+        }
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        double best = std::abs(M[c * w + c]);
+        for (int r = c + 1; r < n; ++r)
+            if (std::abs(M[r * w + c]) > best) {
+                best = std::abs(M[r * w + c]);
+                piv = r;
+            }
+        if (!(best > 0.0)) return false;
+        if (piv != c)
+            for (size_t q = 0; q < w; ++q) std::swap(M[c * w + q], M[piv * w + q]);
+        const double d = 1.0 / M[c * w + c];
+        for (size_t q = 0; q < w; ++q) M[c * w + q] *= d;
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            const double f = M[r * w + c];
+            if (f == 0.0) continue;
+            for (size_t q = (size_t)c; q < w; ++q) M[r * w + q] -= f * M[c * w + q];
+        }
+    }
+    inv.assign((size_t)n * n, 0.f);
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) inv[(size_t)c * n + r] = (float)M[r * w + n + c];
+    return true;
 }
 
 }  // namespace mag

@@ -21,7 +21,22 @@ void fine_operator(int coord, int nx, int nz, double dx, double dz, const std::v
 void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int& nxc,
               int& nzc, std::vector<double>& Ac);
 
-// Level sizes: halve while both sizes are odd and >= 5 (at most max_levels levels).
+// Coarsest levels up to this many nodes are solved exactly with a dense inverse.
+constexpr long long kDenseCoarseMax = 600;
+
+// Level sizes: halve while both sizes are odd and >= 5 (at most max_levels
+// levels), and stop at the first level of at most kDenseCoarseMax nodes.
 void multigrid_levels(int nx, int nz, int max_levels, std::vector<int>& lnx, std::vector<int>& lnz);
+
+// Per-row coefficients (w, e, c, 1/c) of the fine 5-point stencil, FP64,
+// 4 * nx values, and the common s/n coefficient k2 (src/fields.cpp:149-238);
+// rows of the axis (i = 0, cylindrical) have w = 0.  Cartesian: (1, 1, -4),
+// k2 = 1.
+void fine_stencil_table(int coord, int nx, double dx, double dz, std::vector<double>& st, double& k2);
+
+// Dense inverse of a level's 9-point operator (n = nx*nz nodes), FP64
+// Gauss-Jordan with partial pivoting, stored in FP32 column-major
+// (inv[col * n + row]).  Returns false when the operator is singular.
+bool dense_inverse(int nx, int nz, const std::vector<double>& A9, std::vector<float>& inv);
 
 }  // namespace mag

@@ -122,6 +122,7 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
     multigrid_levels(nx, nz, kMaxLevels, lnx, lnz);
     const int nlev = (int)lnx.size();
     std::vector<std::vector<float>> coef(nlev), idiag(nlev);
+    std::vector<float> cinv;
     {
         std::vector<double> A, Ac;
         fine_operator(coord, nx, nz, dx, dz, mask, A);
@@ -137,7 +138,13 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
             A.swap(Ac);
             fixed_f.assign(n, 0);
         }
+        if (nlev > 1 && (long long)lnx.back() * lnz.back() <= kDenseCoarseMax)
+            if (!dense_inverse(lnx.back(), lnz.back(), A, cinv)) cinv.clear();
     }
+    std::vector<double> st64;
+    double k2 = 1.0;
+    fine_stencil_table(coord, nx, dx, dz, st64, k2);
+    std::vector<float> st32(st64.begin(), st64.end());
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
@@ -156,6 +163,12 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
             o_c[l] = take(9 * n * 4);
             o_d[l] = take(n * 4);
         }
+    }
+    const size_t o_st64 = take(st64.size() * 8), o_st32 = take(st32.size() * 4);
+    size_t o_cinv = 0;
+    if (!cinv.empty()) {  // the dense coarsest solve, when it still fits
+        if (align256(off + cinv.size() * 4) <= kNoAllocScratchBytes) o_cinv = take(cinv.size() * 4);
+        else cinv.clear();
     }
     if (off > kNoAllocScratchBytes) {
         g_noalloc_err = "mag_poisson_solve_noalloc: scratch layout of " + std::to_string(off) +
@@ -179,6 +192,10 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
         ck(cudaMemcpyAsync(base + o_d[l], idiag[l].data(), idiag[l].size() * 4, cudaMemcpyHostToDevice, s),
            "diag copy");
     }
+    ck(cudaMemcpyAsync(base + o_st64, st64.data(), st64.size() * 8, cudaMemcpyHostToDevice, s), "stencil copy");
+    ck(cudaMemcpyAsync(base + o_st32, st32.data(), st32.size() * 4, cudaMemcpyHostToDevice, s), "stencil copy");
+    if (!cinv.empty())
+        ck(cudaMemcpyAsync(base + o_cinv, cinv.data(), cinv.size() * 4, cudaMemcpyHostToDevice, s), "inverse copy");
     // state left by the previous call that must start at zero
     ck(cudaMemsetAsync(base + o_red, 0, 4 * 8, s), "clear");
     ck(cudaMemsetAsync(base + o_status, 0, sizeof(SolveStatus), s), "clear");
@@ -202,6 +219,10 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
     a.clear_rho = 0;
     a.mpf = macroparticle_factor;
     a.dV = dV;
+    a.st64 = (const double*)(base + o_st64);
+    a.st32 = (const float*)(base + o_st32);
+    a.k2 = k2;
+    a.coarse_inv = cinv.empty() ? nullptr : (const float*)(base + o_cinv);
     a.nlev = nlev;
     for (int l = 0; l < nlev; ++l) {
         a.lev[l].nx = lnx[l];

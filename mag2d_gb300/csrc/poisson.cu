@@ -28,6 +28,8 @@ constexpr double kPi = 3.14159265358979323846;
 constexpr double kEps0d = 8.854187817e-12;
 constexpr long long kBarrierSpinLimit = 20000000;  // ~seconds of __nanosleep(64) polling
 
+// The threads that share a piece of the solve: the whole grid (synchronised
+// by a bounded grid barrier) or one block (synchronised by __syncthreads).
 struct Team {
     GridBarrier* bar;
     unsigned nblocks;
@@ -35,6 +37,15 @@ struct Team {
     __device__ Team(GridBarrier* b)
         : bar(b), nblocks(gridDim.x), tid(blockIdx.x * blockDim.x + threadIdx.x), nthreads(gridDim.x * blockDim.x)
     {
+    }
+    // this block alone
+    __device__ static Team block(GridBarrier* b)
+    {
+        Team t(b);
+        t.nblocks = 1;
+        t.tid = threadIdx.x;
+        t.nthreads = blockDim.x;
+        return t;
     }
     // returns false when the grid barrier gave up (the kernel then returns)
     __device__ bool sync()
@@ -73,29 +84,35 @@ struct Team {
 
 __device__ __forceinline__ bool is_fixed(int8_t m) { return m == 0 || m == 1; }
 
-// 5-point row of the fine operator (fields.cpp:149-238) at node (i, j)
-struct Stencil5 {
-    double w, e, s, n, c;
-};
-__device__ __forceinline__ Stencil5 fine_stencil(int coord, int i, double dx, double dz)
-{
-    Stencil5 st;
-    if (coord == 1) {
-        const double k2 = 1.0 / (dz * dz);
-        if (i == 0) {
-            const double k3 = 1.0 / (dx * dx * 0.25);
-            st = {0.0, k3, k2, k2, -2.0 * k2 - k3};
-        } else {
-            const double k1 = (i - 0.5) / (dx * dx * i);
-            const double k3 = (i + 0.5) / (dx * dx * i);
-            st = {k1, k3, k2, k2, -2.0 * k2 - k1 - k3};
-        }
-    } else {
-        st = {1.0, 1.0, 1.0, 1.0, -4.0};
+// Unsigned division by a divisor fixed for a whole pass, as a multiply-high
+// and shifts (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, figure 4.1): exact for every 32-bit n.
+struct FastDiv {
+    unsigned d, mp;
+    int l;
+    __device__ explicit FastDiv(unsigned dd) : d(dd)
+    {
+        l = dd > 1 ? 32 - __clz(dd - 1) : 0;  // ceil(log2 d)
+        mp = (unsigned)(((1ull << 32) * ((1ull << l) - dd)) / dd + 1);
     }
-    return st;
-}
+    __device__ __forceinline__ unsigned div(unsigned n) const
+    {
+        if (d == 1) return n;
+        const unsigned t1 = __umulhi(mp, n);
+        return (t1 + ((n - t1) >> 1)) >> (l - 1);
+    }
+};
 
+// 5-point row of the fine operator (fields.cpp:149-238) of row i, from the
+// per-row table built on the host
+struct Stencil5 {
+    double w, e, s, n, c, inv_c;
+};
+__device__ __forceinline__ Stencil5 fine_stencil(const SolveArgs& a, int i)
+{
+    const double* t = a.st64 + 4 * i;
+    return {t[0], t[1], a.k2, a.k2, t[2], t[3]};
+}
 __device__ __forceinline__ double atomic_max_nonneg(double* p, double v)
 {
     return __longlong_as_double(
@@ -123,37 +140,56 @@ __device__ T block_max(T v)
 }
 
 // ---- FP32 multigrid pieces -------------------------------------------------
+//
+// Every pass is a strided loop over the nodes of a level, unrolled so that a
+// thread issues the loads of several nodes before it computes and stores any.
+// Within one pass a node is either only read or only written (the other
+// colour, or another array), so the arrays are accessed through separate
+// __restrict__ read and write pointers and the compiler may batch the loads.
 
 // red-black Gauss-Seidel (or SOR) sweeps on the fine level
 __device__ void smooth_fine(const SolveArgs& a, Team& t, int sweeps, bool reverse, float omega, bool& ok)
 {
     const MGLevelDev& L = a.lev[0];
     const int nx = L.nx, nz = L.nz, hz = (nz + 1) / 2;
+    const float* __restrict__ ein = L.e;
+    float* __restrict__ eout = L.e;
+    const float* __restrict__ r = L.r;
+    const int8_t* __restrict__ mask = a.mask;
+    const float* __restrict__ st = a.st32;
+    const float k2 = (float)a.k2;
+    const unsigned n = (unsigned)(nx * hz);
+    const FastDiv dh((unsigned)hz);
     for (int s = 0; s < sweeps && ok; ++s)
         for (int cc = 0; cc < 2 && ok; ++cc) {
             const int color = reverse ? 1 - cc : cc;
-            for (unsigned q = t.tid; q < (unsigned)(nx * hz); q += t.nthreads) {
-                const int i = q / hz;
-                const int j = 2 * (q % hz) + ((i + color) & 1);
+#pragma unroll 4
+            for (unsigned q = t.tid; q < n; q += t.nthreads) {
+                const int i = (int)dh.div(q);
+                const int j = 2 * (int)(q - (unsigned)i * hz) + ((i + color) & 1);
                 if (j >= nz) continue;
                 const size_t k = (size_t)i * nz + j;
-                if (is_fixed(a.mask[k])) continue;
-                const Stencil5 st = fine_stencil(a.coord, i, a.dx, a.dz);
-                float acc = L.r[k];
-                if (i > 0) acc -= (float)st.w * L.e[k - nz];
-                acc -= (float)st.e * L.e[k + nz];
-                acc -= (float)st.s * L.e[k - 1];
-                acc -= (float)st.n * L.e[k + 1];
-                const float enew = acc / (float)st.c;
-                L.e[k] = omega == 1.f ? enew : L.e[k] + omega * (enew - L.e[k]);
+                if (is_fixed(mask[k])) continue;
+                float acc = r[k];
+                if (i > 0) acc -= st[4 * i] * ein[k - nz];
+                acc -= st[4 * i + 1] * ein[k + nz];
+                acc -= k2 * ein[k - 1];
+                acc -= k2 * ein[k + 1];
+                const float enew = acc / st[4 * i + 2];
+                if (omega == 1.f) {
+                    eout[k] = enew;
+                } else {
+                    const float e0 = ein[k];  // this node is read and written by this thread only
+                    eout[k] = e0 + omega * (enew - e0);
+                }
             }
             ok = t.sync();
         }
 }
 
-__device__ __forceinline__ float coarse_apply(const MGLevelDev& L, int i, int j, size_t k, const float* e, bool skip_center)
+__device__ __forceinline__ float coarse_apply(const float* __restrict__ coef, int nx, int nz, int i, int j, size_t k,
+                                              const float* __restrict__ e, bool skip_center)
 {
-    const int nx = L.nx, nz = L.nz;
     const size_t n = (size_t)nx * nz;
     float acc = 0.f;
 #pragma unroll
@@ -164,7 +200,7 @@ __device__ __forceinline__ float coarse_apply(const MGLevelDev& L, int i, int j,
             if (j + dj < 0 || j + dj >= nz) continue;
             if (skip_center && di == 0 && dj == 0) continue;
             const int p = (di + 1) * 3 + (dj + 1);
-            acc += L.coef[p * n + k] * e[k + (ptrdiff_t)di * nz + dj];
+            acc += __ldg(&coef[p * n + k]) * e[k + (ptrdiff_t)di * nz + dj];
         }
     }
     return acc;
@@ -176,54 +212,79 @@ __device__ void smooth_coarse(const SolveArgs& a, Team& t, int l, int sweeps, bo
     const MGLevelDev& L = a.lev[l];
     const int nx = L.nx, nz = L.nz;
     const int hx = (nx + 1) / 2, hz = (nz + 1) / 2;
+    const float* __restrict__ ein = L.e;
+    float* __restrict__ eout = L.e;
+    const float* __restrict__ r = L.r;
+    const float* __restrict__ coef = L.coef;
+    const float* __restrict__ idg = L.inv_diag;
+    const unsigned n = (unsigned)(hx * hz);
+    const FastDiv dh((unsigned)hz);
     for (int s = 0; s < sweeps && ok; ++s)
         for (int cc = 0; cc < 4 && ok; ++cc) {
             const int color = reverse ? 3 - cc : cc;
             const int ci = color >> 1, cj = color & 1;
-            for (unsigned q = t.tid; q < (unsigned)(hx * hz); q += t.nthreads) {
-                const int i = 2 * (q / hz) + ci, j = 2 * (q % hz) + cj;
+#pragma unroll 2
+            for (unsigned q = t.tid; q < n; q += t.nthreads) {
+                const unsigned qi = dh.div(q);
+                const int i = 2 * (int)qi + ci, j = 2 * (int)(q - qi * hz) + cj;
                 if (i >= nx || j >= nz) continue;
                 const size_t k = (size_t)i * nz + j;
-                const float off = coarse_apply(L, i, j, k, L.e, true);
-                L.e[k] = (L.r[k] - off) * L.inv_diag[k];
+                const float off = coarse_apply(coef, nx, nz, i, j, k, ein, true);
+                eout[k] = (r[k] - off) * __ldg(&idg[k]);
             }
             ok = t.sync();
         }
 }
 
 // t = r - A e on level l (fine level: free nodes only)
-__device__ void residual_level(const SolveArgs& a, Team& t, int l, float* out)
+__device__ void residual_level(const SolveArgs& a, Team& t, int l, float* __restrict__ out)
 {
     const MGLevelDev& L = a.lev[l];
     const int nx = L.nx, nz = L.nz;
-    for (unsigned q = t.tid; q < (unsigned)(nx * nz); q += t.nthreads) {
-        const int i = q / nz, j = q % nz;
-        const size_t k = q;
-        if (l == 0) {
-            if (is_fixed(a.mask[k])) {
-                out[k] = 0.f;
+    const float* __restrict__ e = L.e;
+    const float* __restrict__ r = L.r;
+    const unsigned n = (unsigned)(nx * nz);
+    const FastDiv dz((unsigned)nz);
+    if (l == 0) {
+        const int8_t* __restrict__ mask = a.mask;
+        const float* __restrict__ st = a.st32;
+        const float k2 = (float)a.k2;
+#pragma unroll 4
+        for (unsigned q = t.tid; q < n; q += t.nthreads) {
+            const int i = (int)dz.div(q);
+            if (is_fixed(mask[q])) {
+                out[q] = 0.f;
                 continue;
             }
-            const Stencil5 st = fine_stencil(a.coord, i, a.dx, a.dz);
-            float acc = L.r[k] - (float)st.c * L.e[k];
-            if (i > 0) acc -= (float)st.w * L.e[k - nz];
-            acc -= (float)st.e * L.e[k + nz];
-            acc -= (float)st.s * L.e[k - 1];
-            acc -= (float)st.n * L.e[k + 1];
-            out[k] = acc;
-        } else {
-            out[k] = L.r[k] - coarse_apply(L, i, j, k, L.e, false);
+            float acc = r[q] - st[4 * i + 2] * e[q];
+            if (i > 0) acc -= st[4 * i] * e[q - nz];
+            acc -= st[4 * i + 1] * e[q + nz];
+            acc -= k2 * e[q - 1];
+            acc -= k2 * e[q + 1];
+            out[q] = acc;
+        }
+    } else {
+        const float* __restrict__ coef = L.coef;
+#pragma unroll 2
+        for (unsigned q = t.tid; q < n; q += t.nthreads) {
+            const unsigned i = dz.div(q);
+            out[q] = r[q] - coarse_apply(coef, nx, nz, (int)i, (int)(q - i * nz), q, e, false);
         }
     }
 }
 
 // r_{l+1} = P^T t_l (weights 1, 1/2, 1/4; fixed fine nodes carry no residual); e_{l+1} = 0
-__device__ void restrict_level(const SolveArgs& a, Team& t, int l, const float* tl)
+__device__ void restrict_level(const SolveArgs& a, Team& t, int l, const float* __restrict__ tl)
 {
     const MGLevelDev& F = a.lev[l];
     const MGLevelDev& C = a.lev[l + 1];
-    for (unsigned q = t.tid; q < (unsigned)(C.nx * C.nz); q += t.nthreads) {
-        const int I = q / C.nz, J = q % C.nz;
+    float* __restrict__ cr = C.r;
+    float* __restrict__ ce = C.e;
+    const unsigned n = (unsigned)(C.nx * C.nz);
+    const FastDiv dz((unsigned)C.nz);
+#pragma unroll 2
+    for (unsigned q = t.tid; q < n; q += t.nthreads) {
+        const int I = (int)dz.div(q), J = (int)(q - (unsigned)I * C.nz);
         float acc = 0.f;
 #pragma unroll
         for (int di = -1; di <= 1; ++di) {
@@ -238,8 +299,8 @@ __device__ void restrict_level(const SolveArgs& a, Team& t, int l, const float* 
                 acc += wi * wj * tl[(size_t)i * F.nz + j];
             }
         }
-        C.r[q] = acc;
-        C.e[q] = 0.f;
+        cr[q] = acc;
+        ce[q] = 0.f;
     }
 }
 
@@ -248,30 +309,51 @@ __device__ void prolong_level(const SolveArgs& a, Team& t, int l)
 {
     const MGLevelDev& F = a.lev[l];
     const MGLevelDev& C = a.lev[l + 1];
-    for (unsigned q = t.tid; q < (unsigned)(F.nx * F.nz); q += t.nthreads) {
+    const float* __restrict__ ec = C.e;
+    float* __restrict__ fe = F.e;
+    const unsigned n = (unsigned)(F.nx * F.nz);
+    const FastDiv dz((unsigned)F.nz);
+#pragma unroll 4
+    for (unsigned q = t.tid; q < n; q += t.nthreads) {
         if (l == 0 && is_fixed(a.mask[q])) continue;
-        const int i = q / F.nz, j = q % F.nz;
+        const int i = (int)dz.div(q), j = (int)(q - (unsigned)i * F.nz);
         const int I0 = i >> 1, J0 = j >> 1;
         const bool oi = i & 1, oj = j & 1;
-        const float* ec = C.e;
         const size_t b = (size_t)I0 * C.nz + J0;
         float v;
         if (!oi && !oj) v = ec[b];
         else if (oi && !oj) v = 0.5f * (ec[b] + ec[b + C.nz]);
         else if (!oi && oj) v = 0.5f * (ec[b] + ec[b + 1]);
         else v = 0.25f * (ec[b] + ec[b + C.nz] + ec[b + 1] + ec[b + C.nz + 1]);
-        F.e[q] += v;
+        fe[q] += v;
     }
 }
 
-__device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
+// Coarsest level: e = A^-1 r with the dense inverse (one pass), else
+// Gauss-Seidel sweeps.
+__device__ void coarse_solve(const SolveArgs& a, Team& t, bool& ok)
 {
-    const int L = a.nlev;
-    if (L == 1) {
-        smooth_fine(a, t, a.ncoarse, false, a.omega, ok);
+    const int l = a.nlev - 1;
+    const MGLevelDev& L = a.lev[l];
+    if (a.coarse_inv == nullptr) {
+        smooth_coarse(a, t, l, a.ncoarse, false, ok);
         return;
     }
-    for (int l = 0; l < L - 1 && ok; ++l) {
+    const unsigned n = (unsigned)(L.nx * L.nz);
+    for (unsigned row = t.tid; row < n; row += t.nthreads) {
+        float acc = 0.f;
+        for (unsigned c = 0; c < n; ++c) acc += a.coarse_inv[(size_t)c * n + row] * L.r[c];
+        L.e[row] = acc;
+    }
+    ok = t.sync();
+}
+
+// The part of a V-cycle from level l0 down to the coarsest level and back up
+// to l0, pre- and post-smoothing on l0 included.
+__device__ void vcycle_from(const SolveArgs& a, Team& t, int l0, bool& ok)
+{
+    const int L = a.nlev;
+    for (int l = l0; l < L - 1 && ok; ++l) {
         if (l == 0) smooth_fine(a, t, a.nu1, false, 1.f, ok);
         else smooth_coarse(a, t, l, a.nu1, false, ok);
         if (!ok) return;
@@ -282,8 +364,51 @@ __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
         ok = t.sync();
     }
     if (!ok) return;
-    smooth_coarse(a, t, L - 1, a.ncoarse, false, ok);
-    for (int l = L - 2; l >= 0 && ok; --l) {
+    coarse_solve(a, t, ok);
+    for (int l = L - 2; l >= l0 && ok; --l) {
+        prolong_level(a, t, l);
+        ok = t.sync();
+        if (!ok) return;
+        if (l == 0) smooth_fine(a, t, a.nu2, true, 1.f, ok);
+        else smooth_coarse(a, t, l, a.nu2, true, ok);
+    }
+}
+
+// One V-cycle.  On a multi-block grid the levels from a.l_single down (at most
+// kSingleBlockNodes nodes each) run on block 0 alone, synchronised by
+// __syncthreads, while the other blocks wait at one grid barrier: a coarse
+// level has too little work to pay for the grid barriers of its sweeps.
+__device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
+{
+    const int L = a.nlev;
+    if (L == 1) {
+        smooth_fine(a, t, a.ncoarse, false, a.omega, ok);
+        return;
+    }
+    if (t.nblocks == 1 || a.l_single <= 0 || a.l_single >= L) {
+        vcycle_from(a, t, 0, ok);
+        return;
+    }
+    const int ls = a.l_single;
+    for (int l = 0; l < ls && ok; ++l) {
+        if (l == 0) smooth_fine(a, t, a.nu1, false, 1.f, ok);
+        else smooth_coarse(a, t, l, a.nu1, false, ok);
+        if (!ok) return;
+        residual_level(a, t, l, a.lev[l].t);
+        ok = t.sync();
+        if (!ok) return;
+        restrict_level(a, t, l, a.lev[l].t);
+        ok = t.sync();
+    }
+    if (!ok) return;
+    if (blockIdx.x == 0) {
+        Team tb = Team::block(a.bar);
+        bool okb = true;
+        vcycle_from(a, tb, ls, okb);
+        __threadfence();
+    }
+    ok = t.sync();
+    for (int l = ls - 1; l >= 0 && ok; --l) {
         prolong_level(a, t, l);
         ok = t.sync();
         if (!ok) return;
@@ -299,8 +424,9 @@ __global__ void __launch_bounds__(1024) k_solve(const SolveArgs a)
     const unsigned nn = (unsigned)(nx * nz);
     bool ok = true;
     // 1. right-hand side and Dirichlet values (boundary_solve / boundary_solve_rf)
+    const FastDiv dnz((unsigned)nz);
     for (unsigned k = t.tid; k < nn; k += t.nthreads) {
-        const int i = k / nz;
+        const int i = (int)dnz.div(k);
         const int8_t m = a.mask[k];
         if (is_fixed(m)) {
             const double v = a.rf_solve ? (m == 1 ? a.voltage[k] : 0.0) : (m == 0 ? a.voltage[k] : 0.0);
@@ -330,26 +456,35 @@ __global__ void __launch_bounds__(1024) k_solve(const SolveArgs a)
     double res = 0.0;
     bool conv = false;
     const MGLevelDev& F = a.lev[0];
+    const double* __restrict__ uin = a.u;
+    const double* __restrict__ bb = a.b;
+    const int8_t* __restrict__ mask = a.mask;
+    const float* __restrict__ st32 = a.st32;
     for (; ok; ++it) {
-        double lres = 0.0, lumax = 0.0;
+        // residual in FP64; its Jacobi-scaled max norm and max|u| only steer
+        // the stopping test and are taken in FP32
+        float lres32 = 0.f, lumax32 = 0.f;
+#pragma unroll 1
         for (unsigned k = t.tid; k < nn; k += t.nthreads) {
-            const int i = k / nz;
-            lumax = fmax(lumax, fabs(a.u[k]));
+            const int i = (int)dnz.div(k);
+            const double uk = uin[k];
+            lumax32 = fmaxf(lumax32, fabsf((float)uk));
             F.e[k] = 0.f;
-            if (is_fixed(a.mask[k])) {
+            if (is_fixed(mask[k])) {
                 F.r[k] = 0.f;
                 continue;
             }
-            const Stencil5 st = fine_stencil(a.coord, i, a.dx, a.dz);
-            double acc = st.c * a.u[k];
-            if (i > 0) acc += st.w * a.u[k - nz];
-            acc += st.e * a.u[k + nz];
-            acc += st.s * a.u[k - 1];
-            acc += st.n * a.u[k + 1];
-            const double r = a.b[k] - acc;
-            F.r[k] = (float)r;
-            lres = fmax(lres, fabs(r / st.c));
+            const Stencil5 st = fine_stencil(a, i);
+            double acc = st.c * uk;
+            if (i > 0) acc += st.w * uin[k - nz];
+            acc += st.e * uin[k + nz];
+            acc += st.s * uin[k - 1];
+            acc += st.n * uin[k + 1];
+            const float rf = (float)(bb[k] - acc);
+            F.r[k] = rf;
+            lres32 = fmaxf(lres32, fabsf(rf * st32[4 * i + 3]));
         }
+        double lres = lres32, lumax = lumax32;
         lres = block_max(lres);
         lumax = block_max(lumax);
         if (t.nblocks > 1) {
@@ -428,6 +563,16 @@ __global__ void k_faces(const double* __restrict__ u, int nx, int nz, double dx,
 }
 
 }  // namespace
+
+int solve_max_blocks(int sm_count)
+{
+    int per_sm = 0, coop = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve, 1024, 0) != cudaSuccess || per_sm < 1)
+        return 1;
+    return per_sm * sm_count;
+}
 
 int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s)
 {

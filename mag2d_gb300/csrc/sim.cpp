@@ -278,6 +278,18 @@ void Sim::setup_solver()
         A.swap(Ac);
         fixed_f.assign(n, 0);
     }
+    // coarsest level solved exactly when small (A holds its operator now)
+    lv.coarse_inv.release();
+    if (lv.nlev > 1 && (long long)lnx.back() * lnz.back() <= kDenseCoarseMax) {
+        std::vector<float> inv;
+        if (dense_inverse(lnx.back(), lnz.back(), A, inv)) lv.coarse_inv.upload(inv.data(), inv.size(), stream);
+    }
+    std::vector<double> st;
+    fine_stencil_table(coord, nx, dx, dz, st, lv.k2);
+    std::vector<float> st32(st.begin(), st.end());
+    lv.st64.upload(st.data(), st.size(), stream);
+    lv.st32.upload(st32.data(), st32.size(), stream);
+    MAG_CK(cudaStreamSynchronize(stream));
     solver_ready = true;
 }
 
@@ -305,6 +317,10 @@ SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
     a.clear_rho = clear_rho ? 1 : 0;
     a.mpf = p.macroparticle_factor;
     a.dV = p.dV;
+    a.st64 = lv.st64.p;
+    a.st32 = lv.st32.p;
+    a.k2 = lv.k2;
+    a.coarse_inv = lv.coarse_inv.p;
     a.nlev = lv.nlev;
     for (int l = 0; l < lv.nlev; ++l) {
         a.lev[l].nx = lv.nx[l];
@@ -327,7 +343,24 @@ SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
     a.bar = d_bar.p;
     a.status = d_status.p;
     a.err = d_err.p;
-    const int nblocks = (size_t)nx * nz <= 70000 ? 1 : 1;  // multi-block path enabled once validated on the GPU
+    // grids above kSingleBlockNodes: one block of 1024 threads per SM under a
+    // cooperative launch; their coarse levels below that size run on block 0
+    int nblocks = 1;
+    a.l_single = 0;
+    if ((long long)nx * nz > kSingleBlockNodes) {
+        if (solve_blocks == 0) solve_blocks = std::min(solve_max_blocks(sm_count), sm_count);
+        nblocks = std::max(1, solve_blocks);
+        if (nblocks > 1) {
+            a.l_single = lv.nlev;
+            for (int l = 0; l < lv.nlev; ++l)
+                if ((long long)lv.nx[l] * lv.nz[l] <= kSingleBlockNodes) {
+                    a.l_single = l;
+                    break;
+                }
+            MAG_CK(cudaMemsetAsync(d_bar.p, 0, sizeof(GridBarrier), stream));
+            MAG_CK(cudaMemsetAsync(red.p, 0, 4 * sizeof(double), stream));
+        }
+    }
     launches += launch_solve(a, nblocks, stream);
     MAG_CK(cudaGetLastError());
     SolveStatus st{};

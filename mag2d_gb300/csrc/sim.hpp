@@ -101,6 +101,10 @@ struct SolverLevels {
     int nlev = 0;
     std::vector<int> nx, nz;
     std::vector<DevArray<float>> e, r, t, coef, inv_diag;
+    DevArray<float> coarse_inv;  // dense inverse of the coarsest level (column-major) or empty
+    DevArray<double> st64;       // fine stencil rows (w, e, c)
+    DevArray<float> st32;
+    double k2 = 1.0;
 };
 
 class Sim {
@@ -134,6 +138,7 @@ public:
     int sort_interval = 20;
     int push_vec = 2;
     int sm_count = 1;
+    int solve_blocks = 0;  // blocks of a cooperative solve (0: not yet chosen)
     uint64_t steps_done = 0;
     bool sort_due = true;
 

@@ -200,6 +200,13 @@ class Pic:
         check(lib().mag_advance_timed(self.h, n, _dp(ms)))
         return tuple(ms)
 
+    def solve_status(self) -> dict:
+        """Status of the most recent Poisson solve (iterations, residual, status, levels)."""
+        info = MagSolveInfo()
+        check(lib().mag_solve_status(self.h, ctypes.byref(info)))
+        return {"iterations": info.iterations, "residual": info.residual, "status": info.status,
+                "levels": info.levels}
+
     def sync(self) -> None:
         check(lib().mag_sync(self.h))
 

@@ -14,6 +14,11 @@ Inputs are synthetic and seeded (the reference ships no dataset):
                  r < 4 mm; He at 300 K and 1e-2 Pa; elastic collisions with
                  sigma(E) = 5e-19 m^2 (E / 0.01 eV)^-1/2 given as a RATE
                  (sigma v is constant for that sigma); dt = 2e-9 s.
+  penning_large — the large single instance: the Penning geometry on an r-z
+                 grid of 1025x2049 nodes, electrons at 1 eV, Bz = 0.5 T,
+                 He at 1e-3 Pa with a constant collision frequency
+                 nu = 1e6 s^-1 (elastic RATE = nu / n_He), dt = 1e-12 s
+                 (omega_c dt = 0.088), self-consistent.
 """
 from __future__ import annotations
 
@@ -86,3 +91,27 @@ def multipole_xy(tmp: Path, n: int = 1_000_000, n_nodes: int = 257, seed: int = 
     parts = (5e-3 + rr * np.cos(ph), 5e-3 + rr * np.sin(ph), vth * rng.standard_normal(n),
              vth * rng.standard_normal(n), vth * rng.standard_normal(n))
     return cfg, species, inter, cpath, spath, parts, loaded
+
+
+def penning_large(tmp: Path, n: int = 100_000_000, nr: int = 1025, nz: int = 2049, mpf: float = 1.0,
+                  seed: int = 1, nu: float = 1e6, pressure: float = 1e-3, make_particles: bool = True):
+    """Large single instance: r-z 1025x2049, B = 0.5 T, constant-nu electron-He collisions."""
+    cfg = dict(coord="CYLINDRICAL", boundary="FREE", geometry="PENNING_ENDCAP", r_max=5e-3, z_max=20e-3,
+               r_sampl=nr, z_sampl=nz, u_endcap=-10.0, u_ring=0.0, selfconsistent=1, rf=0,
+               magnetic_field_const=1, Bz=0.5, Br=0.0, Bt=0.0, do_plot=0, macroparticle_factor=mpf,
+               n_particles_total=float(n), density_total=1e13, mover="ADVANCE_BORIS")
+    n_he = pressure / (KB * 300.0)
+    species = [dict(name="ELECTRON", type="ELECTRON", mass=ME, charge=-QE, dt=1e-12, density=1e13,
+                    temperature=11604.5),
+               dict(name="HE", type="NEUTRAL", mass=4 * AMU, density=n_he, temperature=300.0)]
+    inter = [dict(name="e_he", type="ELASTIC", primary="ELECTRON", secondary="HE", rate=nu / n_he)]
+    cpath = write_config(cfg, tmp / "penning_large.txt")
+    spath = write_species_conf(species, inter, tmp / "penning_large_species.txt")
+    parts = None
+    if make_particles:
+        rng = np.random.default_rng(seed)
+        r = 2e-3 * np.sqrt(rng.random(n))
+        z = 5e-3 + 10e-3 * rng.random(n)
+        vth = np.sqrt(KB * 11604.5 / ME)
+        parts = (r, z, vth * rng.standard_normal(n), vth * rng.standard_normal(n), vth * rng.standard_normal(n))
+    return cfg, species, inter, cpath, spath, parts

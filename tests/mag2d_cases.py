@@ -50,6 +50,51 @@ def full_config(cfg: dict) -> dict:
     return out
 
 
+def poisson_system(cfg: dict, mask: np.ndarray, volt: np.ndarray, rho: np.ndarray):
+    """The reference's linear system of Fields::boundary_solve (src/fields.cpp:136-312):
+    the 5-point row stencil of every free node (cylindrical axis row at i = 0),
+    identity rows at fixed nodes, the right-hand side scaled as the reference
+    scales rho.  Vectorised; returns (A as scipy CSR, b)."""
+    import scipy.sparse as sp
+
+    c = full_config(cfg)
+    nx, nz = mask.shape
+    dx, dz = float(c["x_max"]) / (nx - 1), float(c["z_max"]) / (nz - 1)
+    cyl = c["coord"] == "CYLINDRICAL"
+    N = nx * nz
+    k = np.arange(N).reshape(nx, nz)
+    i = np.broadcast_to(np.arange(nx)[:, None], (nx, nz))
+    fixed = (mask == 0) | (mask == 1)
+    free = ~fixed
+    b = np.zeros(N)
+    rows, cols, vals = [k[fixed]], [k[fixed]], [np.ones(int(fixed.sum()))]
+    b[k[fixed]] = np.where(mask[fixed] == 0, volt[fixed], 0.0)
+    mpf = float(c["macroparticle_factor"])
+    if cyl:
+        ax = free & (i == 0)
+        ka = k[ax]
+        k2, k3 = 1 / dz ** 2, 1 / (dx * dx * 0.25)
+        for off, v in ((-1, k2), (0, -2 * k2 - k3), (1, k2), (nz, k3)):
+            rows.append(ka), cols.append(ka + off), vals.append(np.full(len(ka), v))
+        b[ka] = rho[ax] * (-1.0 / EPS0 / (np.pi * dx * dx * 0.25 * dz) * mpf)
+        inn = free & (i > 0)
+        ki, ii = k[inn], i[inn].astype(float)
+        k1, k3 = (ii - 0.5) / (dx * dx * ii), (ii + 0.5) / (dx * dx * ii)
+        for off, v in ((-nz, k1), (-1, np.full(len(ki), k2)), (0, -2 * k2 - k1 - k3), (1, np.full(len(ki), k2)),
+                       (nz, k3)):
+            rows.append(ki), cols.append(ki + off), vals.append(v)
+        b[ki] = rho[inn] * (-1.0 / EPS0 / (np.pi * dx * dx * 2.0 * ii * dz) * mpf)
+    else:
+        kf = k[free]
+        V = float(c["n_particles_total"]) / float(c["density_total"])
+        dV = V / ((nx - 1) * (nz - 1))
+        for off, v in ((-nz, 1.0), (-1, 1.0), (0, -4.0), (1, 1.0), (nz, 1.0)):
+            rows.append(kf), cols.append(kf + off), vals.append(np.full(len(kf), v))
+        b[kf] = rho[free] * (-dx * dx / EPS0 / dV)
+    A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
+    return A, b
+
+
 def write_config(cfg: dict, path) -> Path:
     """Write a GetPot-style config.txt (key = value lines)."""
     path = Path(path)

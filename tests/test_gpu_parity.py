@@ -75,6 +75,68 @@ def test_poisson_matches_direct_solve(m, tmp_path, geom):
     pic.close()
 
 
+def _direct_solve(A, b):
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    lu = spl.splu(A.tocsc())
+    u = lu.solve(b)
+    for _ in range(3):  # iterative refinement: SuperLU alone leaves ~1e-8 residuals on these systems
+        u = u + lu.solve(b - A @ u)
+    return u
+
+
+def test_poisson_multiblock_matches_direct_solve(m, tmp_path):
+    """A grid above the one-block size (257 x 513 = 131841 nodes): the solve
+    runs on one block per SM under a cooperative launch with its coarse levels
+    on block 0; the potential agrees with a sparse direct solve of the
+    reference's system within 1e-9 relative."""
+    pytest.importorskip("scipy")
+    from mag2d_cases import QE, poisson_system, write_config, write_species_conf
+
+    cfg = dict(coord="CYLINDRICAL", geometry="PENNING_ENDCAP", r_max=5e-3, z_max=20e-3, r_sampl=257, z_sampl=513,
+               selfconsistent=1, rf=0, do_plot=0, macroparticle_factor=100.0)
+    species = [dict(name="E", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11, temperature=1e4, density=1e13)]
+    cpath = write_config(cfg, tmp_path / "c.txt")
+    spath = write_species_conf(species, [], tmp_path / "s.txt")
+    pic = m.Pic(cpath, spath, seed=1)
+    mask, volt = m.config_geometry(cpath)
+    nx, nz = pic.shape
+    rng = np.random.default_rng(5)
+    for trial in range(2):
+        rho = -QE * 10 * rng.random((nx, nz))
+        info = pic.field.boundary_solve(rho)
+        u_gpu = pic.field.u
+        A, b = poisson_system(cfg, mask, volt, rho)
+        u_ref = _direct_solve(A, b).reshape(nx, nz)
+        err = np.abs(u_gpu - u_ref).max() / np.abs(u_ref).max()
+        assert info["status"] == 0 and info["levels"] > 3, info
+        assert err <= 1e-9, (trial, err, info)
+    pic.close()
+
+
+def test_poisson_large_grid_residual(m, tmp_path):
+    """The 1025 x 2049 grid of the large single instance: the FP64 residual of
+    the returned potential in the reference's own system, Jacobi-scaled, is
+    below 1e-10 of max|u| (the solve's stopping rule, checked independently)."""
+    pytest.importorskip("scipy")
+    from cases import penning_large
+    from mag2d_cases import QE, poisson_system
+
+    cfg, species, inter, cpath, spath, _ = penning_large(tmp_path, make_particles=False)
+    pic = m.Pic(cpath, spath, seed=1, poisson_tol=1e-10)
+    mask, volt = m.config_geometry(cpath)
+    nx, nz = pic.shape
+    rng = np.random.default_rng(6)
+    rho = -QE * 50 * rng.random((nx, nz))
+    info = pic.field.boundary_solve(rho)
+    u = pic.field.u.reshape(-1)
+    A, b = poisson_system(cfg, mask, volt, rho)
+    r = b - A @ u
+    res = np.abs(r / A.diagonal()).max() / np.abs(u).max()
+    assert info["status"] == 0, info
+    assert res <= 1e-10, (res, info)
+    pic.close()
+
+
 # ---------------------------------------------------------------------------
 def test_deposit_bit_exact(m, tmp_path):
     from cases import penning_rz
