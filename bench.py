@@ -351,6 +351,91 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def run_batched(args) -> None:
+    """256 Penning instances (uneven grids, particle counts, pressures, end caps)
+    advanced by the batched path, against the same instances one at a time."""
+    rank, world, local = _env_rank()
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    import __graft_entry__
+
+    if rank == 0 or not (ROOT / "mag2d_gb300" / "lib" / "libmag2d_gpu.so").exists():
+        __graft_entry__.build()
+    import mag2d_gb300 as m
+    from cases import batched_penning
+
+    n_inst = args.instances
+    tmp = Path(tempfile.mkdtemp(prefix=f"mag2d_batch_{rank}_"))
+    inst = batched_penning(tmp, n=n_inst, seed0=rank * n_inst)
+    t0 = time.perf_counter()
+    b = m.Batch([(c[3], c[4], c[5], c[6]) for c in inst], device=local, poisson_tol=1e-9)
+    b.advance_init()
+    setup_s = time.perf_counter() - t0
+    tuning = b.tune(3)
+    stream = torch.cuda.ExternalStream(b.stream, device=local)
+    b.advance(args.warmup)
+    b.sync()
+
+    def live_total():
+        return sum(b[i].speclist[0].diag()["particle_steps"] for i in range(len(b)))
+
+    ps0 = live_total()
+    launches0 = b.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        b.advance(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1)
+    b.sync()
+    psteps = live_total() - ps0
+    launches = b.kernel_launches - launches0
+    solves = [b[i].solve_status() for i in range(len(b))]
+    max_res = max(s["residual"] for s in solves)
+    # plain path: a stratified sample of the same instances, one at a time
+    stride = max(1, n_inst // args.plain_sample)
+    sample = list(range(0, n_inst, stride))
+    plain_ms = []
+    for i in sample:
+        c = inst[i]
+        pic = m.Pic(c[3], c[4], c[5], seed=c[6], device=local, poisson_tol=1e-9)
+        pic.advance_init()
+        pic.advance(3)
+        s_ = torch.cuda.ExternalStream(pic.stream, device=local)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a0.record(s_)
+        pic.advance(args.plain_steps)
+        a1.record(s_)
+        torch.cuda.synchronize()
+        plain_ms.append(a0.elapsed_time(a1) / args.plain_steps)
+        pic.close()
+    plain_step_ms = float(np.mean(plain_ms)) * n_inst  # the sweep one instance after another
+    batch_step_ms = batch_ms / args.steps
+    value = psteps / (batch_ms * 1e-3)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": batch_step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"batched_penning: {n_inst} Penning r-z instances, grid 65x129 or 129x257, "
+                                   "1e3-1e5 electrons (log-uniform), He 1e-4-1e-1 Pa (log-uniform), end caps "
+                                   "-20..-5 V, self-consistent, Poisson refined to 1e-9",
+                       "instances": n_inst, "l2": "not flushed: one step streams every instance's state",
+                       "parallelism": "single GPU"},
+            "clocks": clk.summary(), "gpu_launches": int(launches),
+            "batched_vs_plain": {"batched_ms_per_step": batch_step_ms, "plain_ms_per_step": plain_step_ms,
+                                 "speedup": plain_step_ms / batch_step_ms,
+                                 "plain_sample": f"{len(sample)} of {n_inst} instances (every {stride}th), "
+                                                 f"{args.plain_steps} steps each, summed over the sweep",
+                                 "max_final_poisson_residual": max_res},
+            "tuning": tuning, "setup_s": setup_s}
+    print(json.dumps(line), flush=True)
+    b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -360,9 +445,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--particles", type=int, default=None, help="particles per GPU (default: the workload's own)")
-    ap.add_argument("--workload", default="multipole", choices=["multipole", "penning_large"],
+    ap.add_argument("--instances", type=int, default=256, help="batched workload: instances")
+    ap.add_argument("--plain-sample", type=int, default=16, help="batched workload: instances timed one at a time")
+    ap.add_argument("--plain-steps", type=int, default=10, help="batched workload: steps per plain instance")
+    ap.add_argument("--workload", default="multipole", choices=["multipole", "penning_large", "batched"],
                     help="multipole: 22-pole ion trap 257x257, 1e6 ions (default); penning_large: r-z 1025x2049, "
-                         "1e8 electrons, B 0.5 T, nu 1e6/s")
+                         "1e8 electrons, B 0.5 T, nu 1e6/s; batched: 256 Penning instances")
     ap.add_argument("--push-vec", type=int, default=0, help="slots per thread of the particle kernel (0: library default)")
     ap.add_argument("--sort-interval", type=int, default=100, help="steps between particle sorts (0: library default, 20)")
     args = ap.parse_args()
@@ -379,6 +467,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 

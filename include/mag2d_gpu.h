@@ -213,6 +213,58 @@ void* mag_stream(mag_sim* sim);
 /* Number of kernel launches the handle has issued since creation. */
 int64_t mag_kernel_launches(mag_sim* sim);
 
+/* ---- Batched instances ----------------------------------------------------
+ * Many independent simulations (each one the Pic of its own config.txt,
+ * species_conf and initscript, as src/test.cpp builds it, with its own seed)
+ * advanced together: each step issues one Poisson launch with a block per
+ * self-consistent instance, one particle launch over every instance's
+ * particles and one collision launch, replayed from a captured CUDA graph
+ * between particle sorts.  No reference counterpart: the reference runs one
+ * Pic per process (the drive_*.py sweeps).  Instances keep the reference's
+ * step semantics; with several moving species per instance the collision
+ * scatter of all species follows the push of all species. */
+typedef struct mag_batch mag_batch;
+
+typedef struct {
+    const char* config_path;
+    const char* species_conf_path;
+    const char* initscript_path;   /* may be NULL */
+    uint64_t seed;
+} mag_instance_desc;
+
+typedef struct {
+    int push_vec;        /* slots per thread of the particle kernel */
+    int solve_threads;   /* threads of each instance's solve block */
+    int sort_interval;   /* steps between particle sorts */
+    double ms_per_step;  /* device time per step measured with these parameters */
+} mag_batch_tuning;
+
+/* opts: device, sort_interval, poisson_tol, poisson_max_iter, push_vec apply to
+ * every instance (seed comes from each descriptor); opts may be NULL. */
+int mag_batch_create(int n, const mag_instance_desc* desc, const mag_opts* opts, mag_batch** out);
+void mag_batch_destroy(mag_batch* b);
+int mag_batch_size(mag_batch* b);
+/* Pic::advance_init of every instance */
+int mag_batch_advance_init(mag_batch* b);
+/* nsteps steps of every instance; asynchronous like mag_advance */
+int mag_batch_advance(mag_batch* b, uint64_t nsteps);
+/* The batch's own autotuner: times candidate launch parameters on
+ * steps_per_trial real steps each (the instances advance; no parameter changes
+ * any result) and keeps the fastest.  out may be NULL. */
+int mag_batch_tune(mag_batch* b, int steps_per_trial, mag_batch_tuning* out);
+/* 0: every step is issued as separate launches; 1 (default): steps between
+ * sorts are replayed from a captured CUDA graph */
+int mag_batch_set_graph(mag_batch* b, int enabled);
+/* wait for queued work; first device error of any instance */
+int mag_batch_sync(mag_batch* b);
+/* Borrowed handle of instance i for the single-instance getters (mag_diag,
+ * mag_get_field, mag_get_particles, ...).  It must not be advanced on its own
+ * and stays valid until mag_batch_destroy; mag_destroy on it is a no-op. */
+int mag_batch_instance(mag_batch* b, int i, mag_sim** out);
+/* Device stream of the batch (a cudaStream_t) */
+void* mag_batch_stream(mag_batch* b);
+int64_t mag_batch_kernel_launches(mag_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,16 @@ class MagSolveInfo(ctypes.Structure):
                 ("levels", ctypes.c_int)]
 
 
+class MagInstanceDesc(ctypes.Structure):
+    _fields_ = [("config_path", ctypes.c_char_p), ("species_conf_path", ctypes.c_char_p),
+                ("initscript_path", ctypes.c_char_p), ("seed", ctypes.c_uint64)]
+
+
+class MagBatchTuning(ctypes.Structure):
+    _fields_ = [("push_vec", ctypes.c_int), ("solve_threads", ctypes.c_int), ("sort_interval", ctypes.c_int),
+                ("ms_per_step", ctypes.c_double)]
+
+
 class MagError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"mag2d_gpu error {code}: {msg}")
@@ -71,6 +81,21 @@ def lib() -> ctypes.CDLL:
     L.mag_sync.argtypes = [P]
     L.mag_advance_timed.argtypes = [P, ctypes.c_uint64, D]
     L.mag_solve_status.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
+    L.mag_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(MagInstanceDesc), ctypes.POINTER(MagOpts),
+                                   ctypes.POINTER(P)]
+    L.mag_batch_destroy.argtypes = [P]
+    L.mag_batch_destroy.restype = None
+    L.mag_batch_size.argtypes = [P]
+    L.mag_batch_advance_init.argtypes = [P]
+    L.mag_batch_advance.argtypes = [P, ctypes.c_uint64]
+    L.mag_batch_tune.argtypes = [P, ctypes.c_int, ctypes.POINTER(MagBatchTuning)]
+    L.mag_batch_set_graph.argtypes = [P, ctypes.c_int]
+    L.mag_batch_sync.argtypes = [P]
+    L.mag_batch_instance.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
+    L.mag_batch_stream.argtypes = [P]
+    L.mag_batch_stream.restype = ctypes.c_void_p
+    L.mag_batch_kernel_launches.argtypes = [P]
+    L.mag_batch_kernel_launches.restype = ctypes.c_int64
     L.mag_grid.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), D, D, D, D]
     L.mag_n_species.argtypes = [P]
     L.mag_species.argtypes = [P, ctypes.c_int, ctypes.POINTER(MagSpeciesInfo)]

@@ -7,11 +7,27 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <vector>
 
+#include "batch.hpp"
 #include "sim.hpp"
 
+// A handle owns its Sim, or borrows one that a batch owns.
+struct SimRelease {
+    bool owned = true;
+    void operator()(mag::Sim* p) const
+    {
+        if (owned) delete p;
+    }
+};
+
 struct mag_sim {
-    std::unique_ptr<mag::Sim> s;
+    std::unique_ptr<mag::Sim, SimRelease> s;
+};
+
+struct mag_batch {
+    std::unique_ptr<mag::Batch> b;
+    std::vector<std::unique_ptr<mag_sim>> views;
 };
 
 namespace {
@@ -83,14 +99,18 @@ int mag_create(const char* config_path, const char* species_conf_path, const cha
             o.push_vec = opts->push_vec;
         }
         auto h = std::make_unique<mag_sim>();
-        h->s = std::make_unique<mag::Sim>(config_path, species_conf_path, o);
+        h->s = std::unique_ptr<mag::Sim, SimRelease>(new mag::Sim(config_path, species_conf_path, o), SimRelease{true});
         if (initscript_path && *initscript_path) h->s->run_initscript(initscript_path);
         *out = h.release();
         return MAG_OK;
     });
 }
 
-void mag_destroy(mag_sim* sim) { delete sim; }
+void mag_destroy(mag_sim* sim)
+{
+    if (sim && sim->s && !sim->s.get_deleter().owned) return;  // a batch's borrowed instance
+    delete sim;
+}
 
 int mag_run_initscript(mag_sim* sim, const char* path)
 {
@@ -378,5 +398,119 @@ int mag_config_species(const char* config_path, const char* species_conf_path, i
 void* mag_stream(mag_sim* sim) { return sim && sim->s ? (void*)sim->s->stream : nullptr; }
 
 int64_t mag_kernel_launches(mag_sim* sim) { return sim && sim->s ? sim->s->launches : 0; }
+
+int mag_batch_create(int n, const mag_instance_desc* desc, const mag_opts* opts, mag_batch** out)
+{
+    return guarded([&]() {
+        if (n <= 0 || !desc || !out) throw mag::Error(MAG_EINVAL, "invalid arguments");
+        mag::SimOptions o;
+        if (opts) {
+            o.device = opts->device;
+            o.sort_interval = opts->sort_interval;
+            o.poisson_tol = opts->poisson_tol;
+            o.poisson_max_iter = opts->poisson_max_iter;
+            o.capacity_hint = opts->capacity_hint;
+            o.push_vec = opts->push_vec;
+        }
+        std::vector<mag::BatchInstanceDesc> d((size_t)n);
+        for (int i = 0; i < n; ++i) {
+            if (!desc[i].config_path || !desc[i].species_conf_path)
+                throw mag::Error(MAG_EINVAL, "instance " + std::to_string(i) + ": null path");
+            d[i].config = desc[i].config_path;
+            d[i].species_conf = desc[i].species_conf_path;
+            d[i].initscript = desc[i].initscript_path ? desc[i].initscript_path : "";
+            d[i].seed = desc[i].seed;
+        }
+        auto h = std::make_unique<mag_batch>();
+        h->b = std::make_unique<mag::Batch>(d, o);
+        h->views.resize((size_t)n);
+        *out = h.release();
+        return MAG_OK;
+    });
+}
+
+void mag_batch_destroy(mag_batch* b) { delete b; }
+
+static mag::Batch& batch_of(mag_batch* b)
+{
+    if (!b || !b->b) throw mag::Error(MAG_EINVAL, "null batch handle");
+    return *b->b;
+}
+
+int mag_batch_size(mag_batch* b)
+{
+    return guarded([&]() { return batch_of(b).size(); });
+}
+
+int mag_batch_advance_init(mag_batch* b)
+{
+    return guarded([&]() {
+        batch_of(b).advance_init();
+        return MAG_OK;
+    });
+}
+
+int mag_batch_advance(mag_batch* b, uint64_t nsteps)
+{
+    return guarded([&]() {
+        batch_of(b).advance(nsteps);
+        return MAG_OK;
+    });
+}
+
+int mag_batch_tune(mag_batch* b, int steps_per_trial, mag_batch_tuning* out)
+{
+    return guarded([&]() {
+        const mag::BatchTuning t = batch_of(b).tune(steps_per_trial);
+        if (out) {
+            out->push_vec = t.push_vec;
+            out->solve_threads = t.solve_threads;
+            out->sort_interval = t.sort_interval;
+            out->ms_per_step = t.ms_per_step;
+        }
+        return MAG_OK;
+    });
+}
+
+int mag_batch_set_graph(mag_batch* b, int enabled)
+{
+    return guarded([&]() {
+        batch_of(b).use_graph = enabled != 0;
+        return MAG_OK;
+    });
+}
+
+int mag_batch_sync(mag_batch* b)
+{
+    return guarded([&]() {
+        const int e = batch_of(b).sync();
+        if (e) g_last_error = "device error " + std::to_string(e) + " in a batched instance";
+        return e;
+    });
+}
+
+int mag_batch_instance(mag_batch* b, int i, mag_sim** out)
+{
+    return guarded([&]() {
+        mag::Batch& B = batch_of(b);
+        if (i < 0 || i >= B.size() || !out) throw mag::Error(MAG_EINVAL, "instance index out of range");
+        if (!b->views[i]) {
+            b->views[i] = std::make_unique<mag_sim>();
+            b->views[i]->s = std::unique_ptr<mag::Sim, SimRelease>(&B.instance(i), SimRelease{false});
+        }
+        *out = b->views[i].get();
+        return MAG_OK;
+    });
+}
+
+void* mag_batch_stream(mag_batch* b) { return (b && b->b) ? (void*)b->b->stream : nullptr; }
+
+int64_t mag_batch_kernel_launches(mag_batch* b)
+{
+    if (!b || !b->b) return 0;
+    int64_t n = b->b->launches;
+    for (int i = 0; i < b->b->size(); ++i) n += b->b->instance(i).launches;
+    return n;
+}
 
 }  // extern "C"

@@ -10,8 +10,17 @@ namespace mag {
 // particle step (init: leapfrog start).  vec = slots per thread (1, 2 or 4);
 // sm_count = multiprocessors of the device (sizes the persistent grid)
 int launch_push(const PushArgs& a, int coord, bool init, int vec, int sm_count, cudaStream_t s);
+// batched particle step: nitems work items (one species of one instance each)
+// with the same coord / field mode / B flag; d_chunk_off = first chunk of each
+// item (nitems + 1 entries), chunks of push_batch_chunk(vec) slots
+int push_batch_chunk(int vec);
+int launch_push_batch(const PushArgs* d_args, const unsigned* d_chunk_off, int nitems, int coord, int emode,
+                      bool has_b, int vec, int sm_count, cudaStream_t s);
 int launch_deposit(const PushArgs& a, cudaStream_t s);
 int launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
+// candidate lists of nitems work items (one block each); max_tables = the
+// largest cross-section table size among them (shared-memory staging)
+int launch_collide_batch(const CollideArgs* d_args, int nitems, int max_tables, cudaStream_t s);
 // counting sort by cell with compaction; n_src = slots of the source arrays
 int launch_sort(const SortArgs& a, long long n_src, cudaStream_t s);
 // whole FP64-refined multigrid solve in one kernel; nblocks > 1 uses a
@@ -20,6 +29,9 @@ int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s);
 // blocks of 1024 threads a cooperative launch of the solve can have (1 when
 // the device cannot launch cooperatively)
 int solve_max_blocks(int sm_count);
+// n independent single-block solves, arguments in device memory (one block of
+// 'threads' threads each; grids up to kSingleBlockNodes nodes)
+int launch_solve_batch(const SolveArgs* d_args, int n, int threads, cudaStream_t s);
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s);
 int launch_load_disk(uint32_t* x, uint32_t* z, float* vx, float* vy, float* vz, uint32_t* id, int64_t n,
                      uint32_t id0, int kind, double cx, double cz, double radius, double zlo, double zhi,

@@ -51,7 +51,56 @@ __global__ void __launch_bounds__(128) k_collide(const __grid_constant__ Collide
     }
 }
 
+// Collisions of many instances in one launch (batched runs): block b runs
+// the candidate list of work item b (one colliding species of one instance).
+__global__ void __launch_bounds__(128) k_collide_batch(const CollideArgs* __restrict__ args)
+{
+    __shared__ __align__(16) unsigned char raw[sizeof(CollideArgs)];
+    __shared__ unsigned long long s_cnt[3];
+    __shared__ MccStage st;
+    extern __shared__ double s_tab[];
+    static_assert(sizeof(CollideArgs) % 8 == 0, "word copy");
+    {
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(args + blockIdx.x);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(raw);
+        for (int w = threadIdx.x; w < (int)(sizeof(CollideArgs) / 8); w += blockDim.x) dst[w] = src[w];
+    }
+    if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const CollideArgs& a = *reinterpret_cast<const CollideArgs*>(raw);
+    double* tab = a.n_tables <= kStageTables ? s_tab : nullptr;
+    mcc_stage(a, st, tab);
+    __syncthreads();
+    if (threadIdx.x == 0) mcc_stage_pointers(a, st, tab);
+    __syncthreads();
+    const unsigned long long ncand = __ldcg(&a.cnt->ncand_par[a.slot]);
+    unsigned long long nc = 0, nn = 0, nm = 0;
+    for (unsigned long long c = threadIdx.x; c < ncand; c += blockDim.x) {
+        const int r = collide_one(a, st.m, c);
+        nc += r == MCC_HIT;
+        nn += r == MCC_NULL;
+        nm += r == MCC_NOPARTNER;
+    }
+    if (nc) atomicAdd(&s_cnt[0], nc);
+    if (nn) atomicAdd(&s_cnt[1], nn);
+    if (nm) atomicAdd(&s_cnt[2], nm);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_cnt[0]) atomicAdd(&a.cnt->ncoll, s_cnt[0]);
+        if (s_cnt[1]) atomicAdd(&a.cnt->nnull, s_cnt[1]);
+        if (s_cnt[2]) atomicAdd(&a.cnt->partner_miss, s_cnt[2]);
+    }
+}
+
 }  // namespace
+
+int launch_collide_batch(const CollideArgs* d_args, int nitems, int max_tables, cudaStream_t s)
+{
+    if (nitems <= 0) return 0;
+    const size_t smem = max_tables <= kStageTables ? (size_t)max_tables * sizeof(double) : 0;
+    k_collide_batch<<<nitems, 128, smem, s>>>(d_args);
+    return 1;
+}
 
 int launch_collide(const CollideArgs& a, int grid, cudaStream_t s)
 {

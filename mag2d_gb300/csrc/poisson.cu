@@ -417,9 +417,8 @@ __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
     }
 }
 
-__global__ void __launch_bounds__(1024) k_solve(const SolveArgs a)
+__device__ void solve_body(const SolveArgs& a, Team& t)
 {
-    Team t(a.bar);
     const int nx = a.nx, nz = a.nz;
     const unsigned nn = (unsigned)(nx * nz);
     bool ok = true;
@@ -542,6 +541,26 @@ __global__ void __launch_bounds__(1024) k_solve(const SolveArgs a)
     }
 }
 
+__global__ void __launch_bounds__(1024) k_solve(const __grid_constant__ SolveArgs a)
+{
+    Team t(a.bar);
+    solve_body(a, t);
+}
+
+// Independent solves, one per block (batched instances): the block copies its
+// arguments to shared memory and runs the single-block solve.
+__global__ void __launch_bounds__(1024) k_solve_batch(const SolveArgs* __restrict__ args)
+{
+    __shared__ __align__(16) unsigned char raw[sizeof(SolveArgs)];
+    static_assert(sizeof(SolveArgs) % 8 == 0, "word copy");
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(args + blockIdx.x);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(raw);
+    for (int w = threadIdx.x; w < (int)(sizeof(SolveArgs) / 8); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+    Team t = Team::block(nullptr);
+    solve_body(*reinterpret_cast<const SolveArgs*>(raw), t);
+}
+
 __global__ void k_faces(const double* __restrict__ u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf)
 {
     const double idx = 1.0 / dx, idz = 1.0 / dz;
@@ -582,6 +601,13 @@ int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s)
         void* args[] = {(void*)&a};
         cudaLaunchCooperativeKernel((const void*)k_solve, dim3(nblocks), dim3(1024), args, 0, s);
     }
+    return 1;
+}
+
+int launch_solve_batch(const SolveArgs* d_args, int n, int threads, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    k_solve_batch<<<n, threads, 0, s>>>(d_args);
     return 1;
 }
 

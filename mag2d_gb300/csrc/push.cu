@@ -385,6 +385,108 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
     }
 }
 
+// Particle step of many independent instances in one launch (batched runs).
+// Work item i is one species of one instance (arguments args[i]); its slots
+// are cut into chunks of kBatchIters x 256 x VEC slots and chunk_off[i] is the
+// first chunk of item i (chunk_off[nitems] = all chunks).  A persistent grid
+// takes chunks in turn; the block stages the item's arguments in shared memory
+// and runs the loop body of k_push over the chunk.
+constexpr int kBatchIters = 4;
+
+template <int COORD, int EMODE, bool BFIELD, int VEC>
+__global__ void __launch_bounds__(256, push_min_blocks<VEC>())
+    k_push_batch(const PushArgs* __restrict__ args, const unsigned* __restrict__ chunk_off, int nitems)
+{
+    using V = Vec<VEC>;
+    __shared__ __align__(16) unsigned char raw[sizeof(PushArgs)];
+    __shared__ int s_item;
+    static_assert(sizeof(PushArgs) % 8 == 0, "word copy");
+    const PushArgs& a = *reinterpret_cast<const PushArgs*>(raw);
+    const unsigned nchunks = chunk_off[nitems];
+    const unsigned full = 0xffffffffu;
+    for (unsigned c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        __syncthreads();  // the previous chunk is done with the staged arguments
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = nitems - 1;  // last item whose first chunk is <= c
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (chunk_off[mid] <= c) lo = mid;
+                else hi = mid - 1;
+            }
+            s_item = lo;
+        }
+        __syncthreads();
+        const int item = s_item;
+        {
+            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(args + item);
+            unsigned long long* dst = reinterpret_cast<unsigned long long*>(raw);
+            for (int w = threadIdx.x; w < (int)(sizeof(PushArgs) / 8); w += blockDim.x) dst[w] = src[w];
+        }
+        __syncthreads();
+        const unsigned first = chunk_off[item];
+        if (c == first && a.fold_slot >= 0 && threadIdx.x == 0) {
+            Counters* cn = a.cnt;
+            cn->live_sum += cn->live_par[a.fold_slot];
+            cn->live_par[a.fold_slot] = 0;
+            cn->ncand_par[a.fold_slot] = 0;
+        }
+        const int64_t n = a.n;
+        const int64_t ngroups = (n + VEC - 1) / VEC;
+        const bool coll = a.coll_threshold != 0u;
+        unsigned live = 0, removed = 0;
+        const int64_t g0 = (int64_t)(c - first) * kBatchIters * blockDim.x;
+#pragma unroll 1
+        for (int it = 0; it < kBatchIters; ++it) {
+            const int64_t g = g0 + (int64_t)it * blockDim.x + threadIdx.x;
+            if (g - threadIdx.x >= ngroups) break;
+            const bool act = g < ngroups;
+            typename V::U X{}, Z{}, ID{};
+            typename V::F VX{}, VY{}, VZ{};
+            if (act) {
+                X = V::ldu(a.x, g);
+                Z = V::ldu(a.z, g);
+                VX = V::ldf(a.vx, g);
+                VY = V::ldf(a.vy, g);
+                VZ = V::ldf(a.vz, g);
+                if (coll) ID = V::ldu(a.id, g);
+            }
+            bool cand[VEC];
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                cand[j] = false;
+                const int64_t k = g * VEC + j;
+                uint32_t& x = V::at(X, j);
+                if (!act || k >= n || x == kDead) continue;
+                bool al;
+                step_particle<COORD, EMODE, BFIELD>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j), V::at(VZ, j),
+                                                    V::at(ID, j), al, cand[j]);
+                if (!al) x = kDead;
+                live += al;
+                removed += !al;
+            }
+            if (act) {
+                V::stu(a.x, g, X);
+                V::stu(a.z, g, Z);
+                V::stf(a.vx, g, VX);
+                V::stf(a.vy, g, VY);
+                V::stf(a.vz, g, VZ);
+            }
+            if (coll) {
+#pragma unroll
+                for (int j = 0; j < VEC; ++j)
+                    append_candidate(a, cand[j], g * VEC + j, V::at(VX, j), V::at(VY, j), V::at(VZ, j),
+                                     V::at(ID, j));
+            }
+        }
+        live = __reduce_add_sync(full, live);
+        removed = __reduce_add_sync(full, removed);
+        if ((threadIdx.x & 31) == 0) {
+            if (live) atomicAdd(&a.cnt->live_par[a.slot], (unsigned long long)live);
+            if (removed) atomicAdd(&a.cnt->removed, (unsigned long long)removed);
+        }
+    }
+}
+
 // Leapfrog start (advance_boris_init, src/particles.cpp:623-679, :997-1050):
 // a backward half rotation and a backward half acceleration, no move.  The
 // caller passes the half-angle backward rotation vectors and hq = -q/m dt/2.
@@ -483,7 +585,62 @@ void launch_push_t(const PushArgs& a, bool init, int vec, int sm_count, cudaStre
     }
 }
 
+template <int COORD, int EMODE, bool BFIELD, int VEC>
+void launch_batch_t(const PushArgs* d_args, const unsigned* d_chunk_off, int nitems, int sm_count, cudaStream_t s)
+{
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_push_batch<COORD, EMODE, BFIELD, VEC>, 256, 0) !=
+                cudaSuccess ||
+            b < 1)
+            b = 1;
+        per_sm = b;
+    }
+    k_push_batch<COORD, EMODE, BFIELD, VEC><<<per_sm * std::max(sm_count, 1), 256, 0, s>>>(d_args, d_chunk_off, nitems);
+}
+
+template <int COORD, int EMODE, bool BFIELD>
+void launch_batch_v(const PushArgs* d_args, const unsigned* d_off, int nitems, int vec, int sm, cudaStream_t s)
+{
+    switch (vec) {
+    case 1: launch_batch_t<COORD, EMODE, BFIELD, 1>(d_args, d_off, nitems, sm, s); break;
+    case 2: launch_batch_t<COORD, EMODE, BFIELD, 2>(d_args, d_off, nitems, sm, s); break;
+    default: launch_batch_t<COORD, EMODE, BFIELD, 4>(d_args, d_off, nitems, sm, s); break;
+    }
+}
+
+template <int COORD, int EMODE>
+void launch_batch_b(const PushArgs* d_args, const unsigned* d_off, int nitems, bool has_b, int vec, int sm,
+                    cudaStream_t s)
+{
+    if (has_b) launch_batch_v<COORD, EMODE, true>(d_args, d_off, nitems, vec, sm, s);
+    else launch_batch_v<COORD, EMODE, false>(d_args, d_off, nitems, vec, sm, s);
+}
+
+template <int COORD>
+void launch_batch_e(const PushArgs* d_args, const unsigned* d_off, int nitems, int emode, bool has_b, int vec,
+                    int sm, cudaStream_t s)
+{
+    switch (emode) {
+    case 0: launch_batch_b<COORD, 0>(d_args, d_off, nitems, has_b, vec, sm, s); break;
+    case 1: launch_batch_b<COORD, 1>(d_args, d_off, nitems, has_b, vec, sm, s); break;
+    default: launch_batch_b<COORD, 2>(d_args, d_off, nitems, has_b, vec, sm, s); break;
+    }
+}
+
 }  // namespace
+
+int push_batch_chunk(int vec) { return kBatchIters * 256 * vec; }
+
+int launch_push_batch(const PushArgs* d_args, const unsigned* d_chunk_off, int nitems, int coord, int emode,
+                      bool has_b, int vec, int sm_count, cudaStream_t s)
+{
+    if (nitems <= 0) return 0;
+    if (coord == 1) launch_batch_e<1>(d_args, d_chunk_off, nitems, emode, has_b, vec, sm_count, s);
+    else launch_batch_e<0>(d_args, d_chunk_off, nitems, emode, has_b, vec, sm_count, s);
+    return 1;
+}
 
 int launch_push(const PushArgs& a, int coord, bool init, int vec, int sm_count, cudaStream_t s)
 {

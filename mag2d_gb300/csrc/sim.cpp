@@ -6,7 +6,9 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <mutex>
 #include <sstream>
+#include <string>
 
 #include "kernels.hpp"
 #include "multigrid_host.hpp"
@@ -72,7 +74,12 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     if ((int)inters.size() > kMaxInteractions) throw Error(-1, "too many interactions");
     build_geometry(p, mask, voltage);
     MAG_CK(cudaSetDevice(device));
-    MAG_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    if (opts.stream) {
+        stream = opts.stream;
+        own_stream = false;
+    } else {
+        MAG_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    }
     d_err.alloc(1);
     d_err.zero(stream);
     d_status.alloc(1);
@@ -97,7 +104,7 @@ Sim::~Sim()
         cudaStreamSynchronize(stream);
         sp.clear();
         lv = SolverLevels{};
-        cudaStreamDestroy(stream);
+        if (own_stream) cudaStreamDestroy(stream);
     }
 }
 
@@ -278,11 +285,31 @@ void Sim::setup_solver()
         A.swap(Ac);
         fixed_f.assign(n, 0);
     }
-    // coarsest level solved exactly when small (A holds its operator now)
+    // coarsest level solved exactly when small (A holds its operator now); the
+    // inverse depends only on the operator, so instances that share grid and
+    // geometry (batched sweeps) compute it once per process
     lv.coarse_inv.release();
     if (lv.nlev > 1 && (long long)lnx.back() * lnz.back() <= kDenseCoarseMax) {
+        static std::mutex mu;
+        static std::map<std::string, std::vector<float>> cache;
+        std::string key((const char*)A.data(), A.size() * sizeof(double));
+        key += std::to_string(lnx.back()) + "x" + std::to_string(lnz.back());
         std::vector<float> inv;
-        if (dense_inverse(lnx.back(), lnz.back(), A, inv)) lv.coarse_inv.upload(inv.data(), inv.size(), stream);
+        bool found = false;
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            auto it = cache.find(key);
+            if (it != cache.end()) {
+                inv = it->second;
+                found = true;
+            }
+        }
+        if (!found && dense_inverse(lnx.back(), lnz.back(), A, inv)) {
+            std::lock_guard<std::mutex> lock(mu);
+            if (cache.size() > 64) cache.clear();
+            cache[key] = inv;
+        }
+        if (!inv.empty()) lv.coarse_inv.upload(inv.data(), inv.size(), stream);
     }
     std::vector<double> st;
     fine_stencil_table(coord, nx, dx, dz, st, lv.k2);
@@ -294,6 +321,39 @@ void Sim::setup_solver()
 }
 
 SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
+{
+    SolveArgs a = solve_args(rf_solve, rho_src, clear_rho);
+    // grids above kSingleBlockNodes: one block of 1024 threads per SM under a
+    // cooperative launch; their coarse levels below that size run on block 0
+    int nblocks = 1;
+    a.l_single = 0;
+    if ((long long)nx * nz > kSingleBlockNodes) {
+        if (solve_blocks == 0) solve_blocks = std::min(solve_max_blocks(sm_count), sm_count);
+        nblocks = std::max(1, solve_blocks);
+        if (nblocks > 1) {
+            a.l_single = lv.nlev;
+            for (int l = 0; l < lv.nlev; ++l)
+                if ((long long)lv.nx[l] * lv.nz[l] <= kSingleBlockNodes) {
+                    a.l_single = l;
+                    break;
+                }
+            MAG_CK(cudaMemsetAsync(d_bar.p, 0, sizeof(GridBarrier), stream));
+            MAG_CK(cudaMemsetAsync(red.p, 0, 4 * sizeof(double), stream));
+        }
+    }
+    launches += launch_solve(a, nblocks, stream);
+    MAG_CK(cudaGetLastError());
+    SolveStatus st{};
+    if (wait) {
+        MAG_CK(cudaStreamSynchronize(stream));
+        MAG_CK(cudaMemcpy(&st, d_status.p, sizeof st, cudaMemcpyDeviceToHost));
+        last_solve = st;
+    }
+    return st;
+}
+
+// Arguments of one Poisson solve (Fields::boundary_solve / boundary_solve_rf)
+SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
 {
     setup_solver();
     SolveArgs a{};
@@ -343,33 +403,7 @@ SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
     a.bar = d_bar.p;
     a.status = d_status.p;
     a.err = d_err.p;
-    // grids above kSingleBlockNodes: one block of 1024 threads per SM under a
-    // cooperative launch; their coarse levels below that size run on block 0
-    int nblocks = 1;
-    a.l_single = 0;
-    if ((long long)nx * nz > kSingleBlockNodes) {
-        if (solve_blocks == 0) solve_blocks = std::min(solve_max_blocks(sm_count), sm_count);
-        nblocks = std::max(1, solve_blocks);
-        if (nblocks > 1) {
-            a.l_single = lv.nlev;
-            for (int l = 0; l < lv.nlev; ++l)
-                if ((long long)lv.nx[l] * lv.nz[l] <= kSingleBlockNodes) {
-                    a.l_single = l;
-                    break;
-                }
-            MAG_CK(cudaMemsetAsync(d_bar.p, 0, sizeof(GridBarrier), stream));
-            MAG_CK(cudaMemsetAsync(red.p, 0, 4 * sizeof(double), stream));
-        }
-    }
-    launches += launch_solve(a, nblocks, stream);
-    MAG_CK(cudaGetLastError());
-    SolveStatus st{};
-    if (wait) {
-        MAG_CK(cudaStreamSynchronize(stream));
-        MAG_CK(cudaMemcpy(&st, d_status.p, sizeof st, cudaMemcpyDeviceToHost));
-        last_solve = st;
-    }
-    return st;
+    return a;
 }
 
 // Speclist (pic.cpp:27-80) and lifetime_init (particles.cpp:142-206)

@@ -73,7 +73,10 @@ struct SimOptions {
     int poisson_max_iter = 200;
     int64_t capacity_hint = 0;
     int push_vec = 0;       // slots per thread of the particle kernel: 1, 2 or 4 (0: 2)
+    cudaStream_t stream = nullptr;  // work on this stream instead of one of its own (not destroyed)
 };
+
+class Batch;
 
 struct SpeciesState {
     SpeciesParams prm;
@@ -157,6 +160,8 @@ public:
     int solver_levels() const { return lv.nlev; }
 
 private:
+    friend class Batch;
+    bool own_stream = true;
     int emode = 1;
     bool check_mask = true;
     DevArray<int8_t> d_mask;
@@ -180,6 +185,7 @@ private:
     void setup_solver();
     void validate_operator() const;
     SolveStatus solve(bool rf_solve, int rho_src, bool clear_rho, bool wait);
+    SolveArgs solve_args(bool rf_solve, int rho_src, bool clear_rho);
     void ensure_capacity(int s, int64_t need);
     void add_loaded(int s, int64_t n, int kind, double cx, double cz, double radius, double zlo, double zhi);
     void add_single(int s, double x, double z, double vx, double vy, double vz);

@@ -163,7 +163,19 @@ class Pic:
         ini = str(initscript).encode() if initscript else None
         check(lib().mag_create(str(config).encode(), str(species_conf).encode(), ini, ctypes.byref(opts),
                                ctypes.byref(h)))
+        self._attach(h, config)
+
+    @classmethod
+    def _borrowed(cls, h, config) -> "Pic":
+        """View of an instance that a Batch owns (not closed by this object)."""
+        obj = cls.__new__(cls)
+        obj._attach(h, config)
+        obj._owned = False
+        return obj
+
+    def _attach(self, h, config) -> None:
         self.h = h
+        self._owned = True
         nx, nz = ctypes.c_int(), ctypes.c_int()
         dx, dz, x0, z0 = (ctypes.c_double() for _ in range(4))
         check(lib().mag_grid(self.h, ctypes.byref(nx), ctypes.byref(nz), ctypes.byref(dx), ctypes.byref(dz),
@@ -176,7 +188,8 @@ class Pic:
 
     def close(self) -> None:
         if getattr(self, "h", None):
-            lib().mag_destroy(self.h)
+            if getattr(self, "_owned", True):
+                lib().mag_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -250,3 +263,79 @@ def config_species(config, species_conf, index: int):
                                        ctypes.byref(info), _dp(rates)))
     d = {k: (getattr(info, k).decode() if k == "name" else getattr(info, k)) for k, _ in info._fields_}
     return d, rates[:n]
+
+
+class Batch:
+    """Many independent Pic instances advanced together (mag_batch_* of the C ABI).
+
+    instances: sequence of (config, species_conf, initscript or None, seed).
+    """
+
+    def __init__(self, instances, *, device: int = 0, poisson_tol: float = 0.0, poisson_max_iter: int = 0,
+                 capacity_hint: int = 0, sort_interval: int = 0, push_vec: int = 0):
+        from ._lib import MagInstanceDesc
+
+        opts = MagOpts(device=device, seed=0, sort_interval=sort_interval, poisson_tol=poisson_tol,
+                       poisson_max_iter=poisson_max_iter, capacity_hint=capacity_hint, push_vec=push_vec)
+        inst = list(instances)
+        self._keep = []
+        arr = (MagInstanceDesc * len(inst))()
+        for i, (cfg, spc, ini, seed) in enumerate(inst):
+            c, sc, ic = str(cfg).encode(), str(spc).encode(), (str(ini).encode() if ini else None)
+            self._keep += [c, sc, ic]
+            arr[i].config_path, arr[i].species_conf_path, arr[i].initscript_path, arr[i].seed = c, sc, ic, int(seed)
+        h = ctypes.c_void_p()
+        check(lib().mag_batch_create(len(inst), arr, ctypes.byref(opts), ctypes.byref(h)))
+        self.h = h
+        self.instances = []
+        for i, (cfg, _, _, _) in enumerate(inst):
+            v = ctypes.c_void_p()
+            check(lib().mag_batch_instance(self.h, i, ctypes.byref(v)))
+            self.instances.append(Pic._borrowed(v, cfg))
+
+    def __len__(self) -> int:
+        return len(self.instances)
+
+    def __getitem__(self, i) -> Pic:
+        return self.instances[i]
+
+    def advance_init(self) -> None:
+        check(lib().mag_batch_advance_init(self.h))
+
+    def advance(self, n: int = 1) -> None:
+        check(lib().mag_batch_advance(self.h, n))
+
+    def tune(self, steps_per_trial: int = 3) -> dict:
+        from ._lib import MagBatchTuning
+
+        t = MagBatchTuning()
+        check(lib().mag_batch_tune(self.h, steps_per_trial, ctypes.byref(t)))
+        return {"push_vec": t.push_vec, "solve_threads": t.solve_threads, "sort_interval": t.sort_interval,
+                "ms_per_step": t.ms_per_step}
+
+    def set_graph(self, enabled: bool) -> None:
+        check(lib().mag_batch_set_graph(self.h, 1 if enabled else 0))
+
+    def sync(self) -> None:
+        check(lib().mag_batch_sync(self.h))
+
+    @property
+    def stream(self) -> int:
+        return lib().mag_batch_stream(self.h) or 0
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().mag_batch_kernel_launches(self.h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            for p in self.instances:
+                p.h = None
+            lib().mag_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -14,6 +14,11 @@ Inputs are synthetic and seeded (the reference ships no dataset):
                  r < 4 mm; He at 300 K and 1e-2 Pa; elastic collisions with
                  sigma(E) = 5e-19 m^2 (E / 0.01 eV)^-1/2 given as a RATE
                  (sigma v is constant for that sigma); dt = 2e-9 s.
+  batched_penning — the batched sweep: instance i (seed i) is the Penning
+                 trap on a 65x129 or 129x257 grid (50/50), N_p log-uniform in
+                 [1e3, 1e5] electrons loaded by the initscript loader, He at a
+                 pressure log-uniform in [1e-4, 1e-1] Pa (elastic, constant
+                 sigma v = 3.6e-14 m^3/s), end caps uniform in [-20, -5] V.
   penning_large — the large single instance: the Penning geometry on an r-z
                  grid of 1025x2049 nodes, electrons at 1 eV, Bz = 0.5 T,
                  He at 1e-3 Pa with a constant collision frequency
@@ -115,3 +120,33 @@ def penning_large(tmp: Path, n: int = 100_000_000, nr: int = 1025, nz: int = 204
         vth = np.sqrt(KB * 11604.5 / ME)
         parts = (r, z, vth * rng.standard_normal(n), vth * rng.standard_normal(n), vth * rng.standard_normal(n))
     return cfg, species, inter, cpath, spath, parts
+
+
+def batched_penning(tmp: Path, n: int = 256, seed0: int = 0, np_range=(1e3, 1e5), grids=((65, 129), (129, 257)),
+                    pressure_range=(1e-4, 1e-1), endcap_range=(-20.0, -5.0)):
+    """The batched sweep: list of (cfg, species, inter, config path, species path, initscript path, seed)."""
+    out = []
+    for i in range(n):
+        seed = seed0 + i
+        rng = np.random.default_rng(10_000 + seed)
+        nr, nz = grids[int(rng.integers(0, len(grids)))]
+        npart = int(round(np.exp(rng.uniform(np.log(np_range[0]), np.log(np_range[1])))))
+        pressure = float(np.exp(rng.uniform(np.log(pressure_range[0]), np.log(pressure_range[1]))))
+        u_end = float(rng.uniform(*endcap_range))
+        d = tmp / f"inst{i:04d}"
+        d.mkdir(parents=True, exist_ok=True)
+        cfg = dict(coord="CYLINDRICAL", boundary="FREE", geometry="PENNING_ENDCAP", r_max=5e-3, z_max=20e-3,
+                   r_sampl=nr, z_sampl=nz, u_endcap=u_end, u_ring=0.0, selfconsistent=1, rf=0,
+                   magnetic_field_const=1, Bz=1.0, Br=0.0, Bt=0.0, do_plot=0, macroparticle_factor=10.0,
+                   n_particles_total=float(npart), density_total=1e13, mover="ADVANCE_BORIS")
+        n_he = pressure / (KB * 300.0)
+        species = [dict(name="ELECTRON", type="ELECTRON", mass=ME, charge=-QE, dt=1e-11, density=1e13,
+                        temperature=11604.5),
+                   dict(name="HE", type="NEUTRAL", mass=4 * AMU, density=n_he, temperature=300.0)]
+        inter = [dict(name="e_he", type="ELASTIC", primary="ELECTRON", secondary="HE", rate=3.6e-14)]
+        cpath = write_config(cfg, d / "config.txt")
+        spath = write_species_conf(species, inter, d / "species_conf.txt")
+        ipath = d / "initscript.txt"
+        ipath.write_text(f"add_particles_in_cylinder ELECTRON {npart} 2e-3 5e-3 15e-3\n")
+        out.append((cfg, species, inter, cpath, spath, ipath, seed))
+    return out
