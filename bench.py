@@ -436,6 +436,62 @@ def run_batched(args) -> None:
     b.close()
 
 
+def run_adjoint(args) -> None:
+    """Gradients per second of the segmented Penning trap (8 ring segments + B):
+    one adjoint run (forward with checkpoints, recomputation, reverse sweep)
+    against the forward runs that central differences would need."""
+    import torch
+
+    torch.cuda.set_device(0)
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import mag2d_gb300 as m
+    from cases import penning_segments
+
+    tmp = Path(tempfile.mkdtemp(prefix="mag2d_adj_"))
+    keys = [f"u_segment_{k}" for k in range(8)]
+    n, steps = args.particles, args.adj_steps
+    volts = __import__("numpy").random.default_rng(7).uniform(-15.0, -5.0, 8)
+    c = penning_segments(tmp, n=n, volts=volts, Bz=1.0, tag="bench")
+    # warm-up: one short adjoint run (kernels loaded, solver set up)
+    pic = m.Pic(c[3], c[4], c[5], seed=c[6], poisson_tol=1e-10)
+    pic.adjoint(20, keys, checkpoint=10)
+    pic.close()
+    times = []
+    for _ in range(max(1, args.steps)):
+        pic = m.Pic(c[3], c[4], c[5], seed=c[6], poisson_tol=1e-10)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        info, grad = pic.adjoint(steps, keys, checkpoint=100)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        pic.close()
+    pic = m.Pic(c[3], c[4], c[5], seed=c[6], poisson_tol=1e-10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pic.advance_init()
+    pic.advance(steps)
+    pic.sync()
+    fwd = time.perf_counter() - t0
+    pic.close()
+    t_adj = min(times)
+    nparam = len(grad)
+    line = {"metric": "grads/s", "value": 1.0 / t_adj, "unit": "gradients/s", "n_gpus": 1, "steps": len(times),
+            "warmup": 1, "ms_per_step": t_adj * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"adjoint: Penning r-z 65x129, 8 ring segments (-15..-5 V) + Bz 1 T, {n} electrons, "
+                                   f"{steps} steps, checkpoint every 100, collisions off, Poisson refined to 1e-10",
+                       "parameters": nparam},
+            "gradient": {"loss": info["loss"], "d_loss_d_params": [float(x) for x in grad]},
+            "forward_run_s": fwd, "central_difference_s": 2 * nparam * fwd,
+            "adjoint_vs_central_difference": 2 * nparam * fwd / t_adj, "e2e": {"value": 1.0 / t_adj,
+                                                                              "unit": "gradients/s",
+                                                                              "h2d_bytes_per_step": 0,
+                                                                              "d2h_bytes_per_step": 8 * nparam}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -448,14 +504,15 @@ def main():
     ap.add_argument("--instances", type=int, default=256, help="batched workload: instances")
     ap.add_argument("--plain-sample", type=int, default=16, help="batched workload: instances timed one at a time")
     ap.add_argument("--plain-steps", type=int, default=10, help="batched workload: steps per plain instance")
-    ap.add_argument("--workload", default="multipole", choices=["multipole", "penning_large", "batched"],
+    ap.add_argument("--adj-steps", type=int, default=2000, help="adjoint workload: steps of the run")
+    ap.add_argument("--workload", default="multipole", choices=["multipole", "penning_large", "batched", "adjoint"],
                     help="multipole: 22-pole ion trap 257x257, 1e6 ions (default); penning_large: r-z 1025x2049, "
                          "1e8 electrons, B 0.5 T, nu 1e6/s; batched: 256 Penning instances")
     ap.add_argument("--push-vec", type=int, default=0, help="slots per thread of the particle kernel (0: library default)")
     ap.add_argument("--sort-interval", type=int, default=100, help="steps between particle sorts (0: library default, 20)")
     args = ap.parse_args()
     if args.particles is None:
-        args.particles = 100_000_000 if args.workload == "penning_large" else N_IONS
+        args.particles = {"penning_large": 100_000_000, "adjoint": 100_000}.get(args.workload, N_IONS)
     if args.workload == "penning_large":
         if args.sort_interval == 100:
             args.sort_interval = 20
@@ -469,6 +526,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 

@@ -213,6 +213,35 @@ void* mag_stream(mag_sim* sim);
 /* Number of kernel launches the handle has issued since creation. */
 int64_t mag_kernel_launches(mag_sim* sim);
 
+/* ---- Adjoint gradients ------------------------------------------------------
+ * Gradient of a trap diagnostic after nsteps steps,
+ *   L = w_energy * mean over live particles of m vz^2 / 2 [eV]
+ *     + w_lost * (particles lost) / (particles at the start),
+ * with respect to electrode voltages (config keys such as u_segment_3 or
+ * u_endcap; the geometry is linear in them) and the constant magnetic field,
+ * by a hand-written adjoint of the collisionless step (push, gather, deposit,
+ * Poisson), checkpointed every `checkpoint` steps and recomputed in between.
+ * The handle must be fresh: particles loaded, mag_advance_init not yet called;
+ * the call runs advance_init and the nsteps forward steps itself and leaves
+ * the handle at the end of them.  Requires collisions off, constant B and no
+ * RF.  No reference counterpart (the reference computes no derivatives). */
+typedef struct {
+    uint64_t nsteps;
+    int checkpoint;                 /* steps between checkpoints (0 = 100) */
+    int n_voltage_keys;
+    const char* const* voltage_keys;
+    int grad_b;                     /* 1: append d L / d(Br, Bt, Bz) */
+    double w_energy, w_lost;
+} mag_adj_cfg;
+
+typedef struct {
+    double loss, mean_energy_eV, lost_fraction;
+    int64_t n0, n_live;
+} mag_adj_out;
+
+/* grad_out: n_voltage_keys (+ 3 with grad_b) doubles */
+int mag_adjoint_run(mag_sim* sim, const mag_adj_cfg* cfg, double* grad_out, mag_adj_out* out);
+
 /* ---- Batched instances ----------------------------------------------------
  * Many independent simulations (each one the Pic of its own config.txt,
  * species_conf and initscript, as src/test.cpp builds it, with its own seed)

@@ -50,6 +50,17 @@ class MagBatchTuning(ctypes.Structure):
                 ("ms_per_step", ctypes.c_double)]
 
 
+class MagAdjCfg(ctypes.Structure):
+    _fields_ = [("nsteps", ctypes.c_uint64), ("checkpoint", ctypes.c_int), ("n_voltage_keys", ctypes.c_int),
+                ("voltage_keys", ctypes.POINTER(ctypes.c_char_p)), ("grad_b", ctypes.c_int),
+                ("w_energy", ctypes.c_double), ("w_lost", ctypes.c_double)]
+
+
+class MagAdjOut(ctypes.Structure):
+    _fields_ = [("loss", ctypes.c_double), ("mean_energy_eV", ctypes.c_double), ("lost_fraction", ctypes.c_double),
+                ("n0", ctypes.c_int64), ("n_live", ctypes.c_int64)]
+
+
 class MagError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"mag2d_gpu error {code}: {msg}")
@@ -81,6 +92,7 @@ def lib() -> ctypes.CDLL:
     L.mag_sync.argtypes = [P]
     L.mag_advance_timed.argtypes = [P, ctypes.c_uint64, D]
     L.mag_solve_status.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
+    L.mag_adjoint_run.argtypes = [P, ctypes.POINTER(MagAdjCfg), D, ctypes.POINTER(MagAdjOut)]
     L.mag_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(MagInstanceDesc), ctypes.POINTER(MagOpts),
                                    ctypes.POINTER(P)]
     L.mag_batch_destroy.argtypes = [P]

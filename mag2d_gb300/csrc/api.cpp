@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint.hpp"
 #include "batch.hpp"
 #include "sim.hpp"
 
@@ -398,6 +399,35 @@ int mag_config_species(const char* config_path, const char* species_conf_path, i
 void* mag_stream(mag_sim* sim) { return sim && sim->s ? (void*)sim->s->stream : nullptr; }
 
 int64_t mag_kernel_launches(mag_sim* sim) { return sim && sim->s ? sim->s->launches : 0; }
+
+int mag_adjoint_run(mag_sim* sim, const mag_adj_cfg* cfg, double* grad_out, mag_adj_out* out)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!cfg || (cfg->n_voltage_keys > 0 && !cfg->voltage_keys) || cfg->n_voltage_keys < 0)
+            throw mag::Error(MAG_EINVAL, "invalid adjoint configuration");
+        mag::AdjointConfig c;
+        c.nsteps = cfg->nsteps;
+        c.checkpoint = cfg->checkpoint > 0 ? cfg->checkpoint : 100;
+        for (int q = 0; q < cfg->n_voltage_keys; ++q) {
+            if (!cfg->voltage_keys[q]) throw mag::Error(MAG_EINVAL, "null voltage key");
+            c.voltage_keys.push_back(cfg->voltage_keys[q]);
+        }
+        c.grad_b = cfg->grad_b != 0;
+        c.w_energy = cfg->w_energy;
+        c.w_lost = cfg->w_lost;
+        const mag::AdjointResult r = mag::Adjoint::run(*sim->s, c);
+        if (grad_out) std::copy(r.grad.begin(), r.grad.end(), grad_out);
+        if (out) {
+            out->loss = r.loss;
+            out->mean_energy_eV = r.mean_energy_eV;
+            out->lost_fraction = r.lost_fraction;
+            out->n0 = r.n0;
+            out->n_live = r.n_live;
+        }
+        return device_status(sim);
+    });
+}
 
 int mag_batch_create(int n, const mag_instance_desc* desc, const mag_opts* opts, mag_batch** out)
 {

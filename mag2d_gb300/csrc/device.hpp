@@ -221,4 +221,20 @@ struct SolveArgs {
     int* err;
 };
 
+// Adjoint of one particle step (or of the leapfrog start) for every particle
+// of a species: the state before the step, the removal marker after it, and
+// the adjoints of the state after the step, overwritten with those before it.
+// Positions in cells, velocities in m/s.
+struct AdjPushArgs {
+    const uint32_t *x0, *z0;
+    const float *vx0, *vy0, *vz0;
+    const uint32_t* x1;     // state after the step (kDead: removed during it); null for the start
+    int64_t n;
+    float *lr, *lz, *lvx, *lvy, *lvz;
+    float* lExf;            // adjoints of the face fields of this step, accumulated
+    float* lEzf;
+    double* lB;             // d loss / d(Br, Bt, Bz), accumulated
+    int init;               // 1: the leapfrog start (backward half rotation and half kick, no move)
+};
+
 }  // namespace mag

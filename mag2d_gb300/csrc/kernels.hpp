@@ -14,6 +14,24 @@ int launch_push(const PushArgs& a, int coord, bool init, int vec, int sm_count, 
 // with the same coord / field mode / B flag; d_chunk_off = first chunk of each
 // item (nitems + 1 entries), chunks of push_batch_chunk(vec) slots
 int push_batch_chunk(int vec);
+// adjoint of the particle step (or of the leapfrog start) of one species;
+// field mode 1 (potential faces) or 0 (uniform field)
+int launch_adj_push(const PushArgs& a, const AdjPushArgs& d, int coord, cudaStream_t s);
+// adjoint helpers of the self-consistent step (adjoint_kernels.cu)
+int launch_adj_faces(int nx, int nz, double dx, double dz, const float* lExf, const float* lEzf, double* g,
+                     cudaStream_t s);
+int launch_adj_rhs(int nx, int nz, const int8_t* mask, const double* g, const double* w_scale, double* rho,
+                   cudaStream_t s);
+int launch_adj_post(int nx, int nz, const int8_t* mask, const double* x, const double* w, const double* scale,
+                    double* y, double* lrho, cudaStream_t s);
+int launch_adj_dirichlet(int nx, int nz, const int8_t* mask, const double* g, const double* y, const double* st64,
+                         double k2, const double* basis, int nparam, double* grad, cudaStream_t s);
+int launch_adj_deposit(const uint32_t* x, const uint32_t* z, int64_t n, int nx, int nz, const double* lrho,
+                       double charge, float* lr, float* lz, cudaStream_t s);
+int launch_adj_loss(const uint32_t* x, const float* vz, int64_t n, double half_m_eV, double* out_e,
+                    unsigned long long* out_n, cudaStream_t s);
+int launch_adj_seed(const uint32_t* x, const float* vz, int64_t n, double coef, float* lr, float* lz, float* lvx,
+                    float* lvy, float* lvz, cudaStream_t s);
 int launch_push_batch(const PushArgs* d_args, const unsigned* d_chunk_off, int nitems, int coord, int emode,
                       bool has_b, int vec, int sm_count, cudaStream_t s);
 int launch_deposit(const PushArgs& a, cudaStream_t s);

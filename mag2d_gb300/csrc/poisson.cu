@@ -452,7 +452,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
     ok = t.sync();
     // 2. FP64 residual refinement around the FP32 multigrid
     int it = 0;
-    double res = 0.0;
+    double res = 0.0, ref0 = 0.0;
     bool conv = false;
     const MGLevelDev& F = a.lev[0];
     const double* __restrict__ uin = a.u;
@@ -501,7 +501,11 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
                 a.red[3 - slot] = 0.0;
             }
         }
-        res = lumax > 0.0 ? lres / lumax : lres;
+        // relative to max|u|; a cold start from u = 0 (a homogeneous solve)
+        // measures against its own initial residual instead
+        if (it == 0) ref0 = lres;
+        const double uref = lumax > 0.0 ? lumax : ref0;
+        res = uref > 0.0 ? lres / uref : lres;
         if (res <= a.tol || lres == 0.0) {
             conv = true;
             break;

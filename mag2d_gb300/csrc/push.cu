@@ -585,6 +585,182 @@ void launch_push_t(const PushArgs& a, bool init, int vec, int sm_count, cudaStre
     }
 }
 
+// ---- adjoint of the particle step ----------------------------------------
+//
+// Reverse-mode derivative of step_particle (collisionless, constant B, field
+// from the potential faces) and of the leapfrog start, for the adjoint runs.
+// The forward quantities are recomputed from the stored state before the
+// step; positions are continuous in the derivative (the fixed-point rounding
+// of a move passes the adjoint through unchanged).  Derivatives are FP32.
+
+struct Vec3 {
+    float x, y, z;
+};
+__device__ __forceinline__ Vec3 cross3(Vec3 a, Vec3 b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ Vec3 add3(Vec3 a, Vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ Vec3 scale3(float k, Vec3 a) { return {k * a.x, k * a.y, k * a.z}; }
+__device__ __forceinline__ float dot3(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// field at the particle with its derivatives in cells, and the stencil for the adjoint scatter
+struct GatherD {
+    GatherIdx g;
+    float ex, ez, dex_dr, dex_dz, dez_dr, dez_dz;
+};
+template <int EMODE>
+__device__ __forceinline__ GatherD gather_E_d(const PushArgs& a, uint32_t x, uint32_t z)
+{
+    GatherD G{};
+    if (EMODE == 0) {
+        G.ez = a.extern_ez;
+        return G;
+    }
+    G.g = gather_idx(x, z, a.nx, a.nz);
+    const GatherIdx& g = G.g;
+    {
+        const float* p = a.Exf + (size_t)g.ix * a.nz + g.jz;
+        const float A = p[0], B = p[1], C = p[a.nz], D = p[a.nz + 1];
+        G.ex = lerp4(A, B, C, D, g.fx, g.fz);
+        G.dex_dr = (1.f - g.fz) * (C - A) + g.fz * (D - B);
+        G.dex_dz = (1.f - g.fx) * (B - A) + g.fx * (D - C);
+    }
+    {
+        const int st = a.nz + 1;
+        const float* p = a.Ezf + (size_t)g.iz * st + g.jz2;
+        const float A = p[0], B = p[1], C = p[st], D = p[st + 1];
+        G.ez = lerp4(A, B, C, D, g.gx, g.gz);
+        G.dez_dr = (1.f - g.gz) * (C - A) + g.gz * (D - B);
+        G.dez_dz = (1.f - g.gx) * (B - A) + g.gx * (D - C);
+    }
+    return G;
+}
+
+template <int EMODE>
+__device__ __forceinline__ void scatter_lE(const PushArgs& a, const AdjPushArgs& d, const GatherIdx& g, float lex,
+                                           float lez)
+{
+    if (EMODE == 0) return;
+    float* p = d.lExf + (size_t)g.ix * a.nz + g.jz;
+    atomicAdd(p, (1.f - g.fx) * (1.f - g.fz) * lex);
+    atomicAdd(p + 1, (1.f - g.fx) * g.fz * lex);
+    atomicAdd(p + a.nz, g.fx * (1.f - g.fz) * lex);
+    atomicAdd(p + a.nz + 1, g.fx * g.fz * lex);
+    const int st = a.nz + 1;
+    float* q = d.lEzf + (size_t)g.iz * st + g.jz2;
+    atomicAdd(q, (1.f - g.gx) * (1.f - g.gz) * lez);
+    atomicAdd(q + 1, (1.f - g.gx) * g.gz * lez);
+    atomicAdd(q + st, g.gx * (1.f - g.gz) * lez);
+    atomicAdd(q + st + 1, g.gx * g.gz * lez);
+}
+
+template <int COORD, int EMODE>
+__global__ void __launch_bounds__(256) k_adj_push(const __grid_constant__ PushArgs a,
+                                                  const __grid_constant__ AdjPushArgs d)
+{
+    const float sg = COORD == 1 ? 1.f : -1.f;  // p = v + sg v x t, v' = v + sg p x s (rotate<COORD>)
+    const Vec3 t{a.tx, a.ty, a.tz}, s{a.sx, a.sy, a.sz};
+    float lb0 = 0.f, lb1 = 0.f, lb2 = 0.f;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < d.n; k += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t x = d.x0[k];
+        if (x == kDead) continue;
+        if (!d.init && d.x1[k] == kDead) {  // removed during the step: the loss no longer depends on it
+            d.lr[k] = d.lz[k] = d.lvx[k] = d.lvy[k] = d.lvz[k] = 0.f;
+            continue;
+        }
+        const uint32_t z = d.z0[k];
+        const Vec3 v{d.vx0[k], d.vy0[k], d.vz0[k]};
+        const GatherD G = gather_E_d<EMODE>(a, x, z);
+        float lr = d.lr[k], lz = d.lz[k];
+        Vec3 lv{d.lvx[k], d.lvy[k], d.lvz[k]};
+        float lex = 0.f, lez = 0.f;
+        Vec3 v1 = v;
+        if (!d.init) {
+            v1.x += a.hq * G.ex;
+            v1.z += a.hq * G.ez;
+        }
+        const Vec3 p = add3(v1, scale3(sg, cross3(v1, t)));
+        Vec3 l2;  // adjoint of the rotated velocity
+        if (d.init) {
+            // v0 = rot(v_in) + hq E: no move
+            l2 = lv;
+            lex += a.hq * lv.x;
+            lez += a.hq * lv.z;
+        } else {
+            const Vec3 v2 = add3(v1, scale3(sg, cross3(p, s)));
+            Vec3 v3 = v2;
+            v3.x += a.hq * G.ex;
+            v3.z += a.hq * G.ez;
+            Vec3 l3;
+            if (COORD == 1) {
+                const float r = cells(x);
+                const float ax = v3.x * a.cx, by = v3.y * a.cx;
+                const float x2 = r + ax;
+                const float rn = sqrtf(x2 * x2 + by * by);
+                float ca = 1.f, sa = 0.f, ir3 = 0.f;
+                if (rn > 0.f) {
+                    ca = x2 / rn;
+                    sa = by / rn;
+                    ir3 = 1.f / (rn * rn * rn);
+                }
+                // outputs: r' = rn, z' = z + v3z cz, v4 = (ca v3x + sa v3y, -sa v3x + ca v3y, v3z)
+                const float lca = v3.x * lv.x + v3.y * lv.y, lsa = v3.y * lv.x - v3.x * lv.y;
+                l3.x = ca * lv.x - sa * lv.y;
+                l3.y = sa * lv.x + ca * lv.y;
+                l3.z = lv.z + lz * a.cz;
+                const float lx2 = lr * ca + (lca * by * by - lsa * by * x2) * ir3;
+                const float lby = lr * sa + (-lca * x2 * by + lsa * x2 * x2) * ir3;
+                lr = lx2;
+                l3.x += lx2 * a.cx;
+                l3.y += lby * a.cx;
+            } else {
+                // outputs: x' = x + v3x cx, z' = z + v3z cz, v3
+                l3.x = lv.x + lr * a.cx;
+                l3.y = lv.y;
+                l3.z = lv.z + lz * a.cz;
+            }
+            l2 = l3;
+            lex += a.hq * l3.x;
+            lez += a.hq * l3.z;
+        }
+        // rotation: v2 = v1 + sg p x s, p = v1 + sg v1 x t
+        const Vec3 lp = scale3(sg, cross3(s, l2));
+        Vec3 lv1 = add3(add3(l2, lp), scale3(sg, cross3(t, lp)));
+        const Vec3 ls = scale3(sg, cross3(l2, p));
+        Vec3 lt = scale3(sg, cross3(lp, v1));
+        const float f = 2.f / (1.f + dot3(t, t));
+        lt = add3(lt, add3(scale3(f, ls), scale3(-f * f * dot3(ls, t), t)));
+        lb0 += a.q_dt_2m * lt.x;
+        lb1 += a.q_dt_2m * lt.y;
+        lb2 += a.q_dt_2m * lt.z;
+        if (!d.init) {
+            lex += a.hq * lv1.x;
+            lez += a.hq * lv1.z;
+        }
+        // gather: E depends on the position before the step
+        lr += lex * G.dex_dr + lez * G.dez_dr;
+        lz += lex * G.dex_dz + lez * G.dez_dz;
+        scatter_lE<EMODE>(a, d, G.g, lex, lez);
+        d.lr[k] = lr;
+        d.lz[k] = lz;
+        d.lvx[k] = lv1.x;
+        d.lvy[k] = lv1.y;
+        d.lvz[k] = lv1.z;
+    }
+    const unsigned full = 0xffffffffu;
+    for (int o = 16; o > 0; o >>= 1) {
+        lb0 += __shfl_xor_sync(full, lb0, o);
+        lb1 += __shfl_xor_sync(full, lb1, o);
+        lb2 += __shfl_xor_sync(full, lb2, o);
+    }
+    if ((threadIdx.x & 31) == 0 && d.lB) {
+        atomicAdd(&d.lB[0], (double)lb0);
+        atomicAdd(&d.lB[1], (double)lb1);
+        atomicAdd(&d.lB[2], (double)lb2);
+    }
+}
+
 template <int COORD, int EMODE, bool BFIELD, int VEC>
 void launch_batch_t(const PushArgs* d_args, const unsigned* d_chunk_off, int nitems, int sm_count, cudaStream_t s)
 {
@@ -639,6 +815,21 @@ int launch_push_batch(const PushArgs* d_args, const unsigned* d_chunk_off, int n
     if (nitems <= 0) return 0;
     if (coord == 1) launch_batch_e<1>(d_args, d_chunk_off, nitems, emode, has_b, vec, sm_count, s);
     else launch_batch_e<0>(d_args, d_chunk_off, nitems, emode, has_b, vec, sm_count, s);
+    return 1;
+}
+
+int launch_adj_push(const PushArgs& a, const AdjPushArgs& d, int coord, cudaStream_t s)
+{
+    if (d.n == 0) return 0;
+    const unsigned grid = (unsigned)std::min<int64_t>((d.n + 255) / 256, 152 * 8);
+    const int em = a.emode == 0 ? 0 : 1;
+    if (coord == 1) {
+        if (em == 0) k_adj_push<1, 0><<<grid, 256, 0, s>>>(a, d);
+        else k_adj_push<1, 1><<<grid, 256, 0, s>>>(a, d);
+    } else {
+        if (em == 0) k_adj_push<0, 0><<<grid, 256, 0, s>>>(a, d);
+        else k_adj_push<0, 1><<<grid, 256, 0, s>>>(a, d);
+    }
     return 1;
 }
 

@@ -63,6 +63,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     push_vec = opts.push_vec == 1 || opts.push_vec == 2 || opts.push_vec == 4 ? opts.push_vec : 2;
     if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sm_count < 1)
         sm_count = 1;
+    config_path = config;
     p = make_param(KeyValueConfig::from_file(config));
     if (p.mover != ADVANCE_BORIS)
         throw Error(-1, "mover ADVANCE_MULTICOLL is not provided by this library (Boris mover only)");
@@ -322,7 +323,18 @@ void Sim::setup_solver()
 
 SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
 {
-    SolveArgs a = solve_args(rf_solve, rho_src, clear_rho);
+    run_solve(solve_args(rf_solve, rho_src, clear_rho));
+    SolveStatus st{};
+    if (wait) {
+        MAG_CK(cudaStreamSynchronize(stream));
+        MAG_CK(cudaMemcpy(&st, d_status.p, sizeof st, cudaMemcpyDeviceToHost));
+        last_solve = st;
+    }
+    return st;
+}
+
+void Sim::run_solve(SolveArgs a)
+{
     // grids above kSingleBlockNodes: one block of 1024 threads per SM under a
     // cooperative launch; their coarse levels below that size run on block 0
     int nblocks = 1;
@@ -343,13 +355,6 @@ SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
     }
     launches += launch_solve(a, nblocks, stream);
     MAG_CK(cudaGetLastError());
-    SolveStatus st{};
-    if (wait) {
-        MAG_CK(cudaStreamSynchronize(stream));
-        MAG_CK(cudaMemcpy(&st, d_status.p, sizeof st, cudaMemcpyDeviceToHost));
-        last_solve = st;
-    }
-    return st;
 }
 
 // Arguments of one Poisson solve (Fields::boundary_solve / boundary_solve_rf)

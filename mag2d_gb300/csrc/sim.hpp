@@ -77,6 +77,7 @@ struct SimOptions {
 };
 
 class Batch;
+class Adjoint;
 
 struct SpeciesState {
     SpeciesParams prm;
@@ -122,6 +123,7 @@ public:
     int sync();  // returns first device error code (0 = none)
 
     // accessors used by the C ABI
+    std::string config_path;  // the config.txt the simulation was made from
     Param p;
     std::vector<SpeciesParams> species_prm;
     std::vector<InteractionParams> inters;
@@ -161,6 +163,7 @@ public:
 
 private:
     friend class Batch;
+    friend class Adjoint;
     bool own_stream = true;
     int emode = 1;
     bool check_mask = true;
@@ -186,6 +189,7 @@ private:
     void validate_operator() const;
     SolveStatus solve(bool rf_solve, int rho_src, bool clear_rho, bool wait);
     SolveArgs solve_args(bool rf_solve, int rho_src, bool clear_rho);
+    void run_solve(SolveArgs a);  // launch (one block, or cooperative for large grids)
     void ensure_capacity(int s, int64_t need);
     void add_loaded(int s, int64_t n, int kind, double cx, double cz, double radius, double zlo, double zhi);
     void add_single(int s, double x, double z, double vx, double vy, double vz);

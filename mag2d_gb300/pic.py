@@ -220,6 +220,25 @@ class Pic:
         return {"iterations": info.iterations, "residual": info.residual, "status": info.status,
                 "levels": info.levels}
 
+    def adjoint(self, nsteps: int, voltage_keys=(), *, checkpoint: int = 100, grad_b: bool = True,
+                w_energy: float = 1.0, w_lost: float = 1.0):
+        """mag_adjoint_run: runs advance_init and nsteps steps, returns (info, gradient).
+
+        gradient = d loss / d(voltage_keys...) followed by d loss / d(Br, Bt, Bz) when grad_b;
+        loss = w_energy * mean axial kinetic energy [eV] + w_lost * lost fraction."""
+        from ._lib import MagAdjCfg, MagAdjOut
+
+        keys = [str(k).encode() for k in voltage_keys]
+        arr = (ctypes.c_char_p * max(1, len(keys)))(*keys)
+        cfg = MagAdjCfg(nsteps=nsteps, checkpoint=checkpoint, n_voltage_keys=len(keys), voltage_keys=arr,
+                        grad_b=1 if grad_b else 0, w_energy=w_energy, w_lost=w_lost)
+        grad = np.zeros(len(keys) + (3 if grad_b else 0))
+        out = MagAdjOut()
+        check(lib().mag_adjoint_run(self.h, ctypes.byref(cfg), _dp(grad), ctypes.byref(out)))
+        info = {"loss": out.loss, "mean_energy_eV": out.mean_energy_eV, "lost_fraction": out.lost_fraction,
+                "n0": out.n0, "n_live": out.n_live}
+        return info, grad
+
     def sync(self) -> None:
         check(lib().mag_sync(self.h))
 

@@ -19,6 +19,10 @@ Inputs are synthetic and seeded (the reference ships no dataset):
                  [1e3, 1e5] electrons loaded by the initscript loader, He at a
                  pressure log-uniform in [1e-4, 1e-1] Pa (elastic, constant
                  sigma v = 3.6e-14 m^3/s), end caps uniform in [-20, -5] V.
+  penning_segments — the adjoint case: the Penning trap with its ring wall
+                 split into 8 z-segments biased by u_segment_0..7 (uniform in
+                 [-15, -5] V), end caps at -25 V, Bz = 1 T, electrons at 1 eV,
+                 self-consistent, collisions off.
   penning_large — the large single instance: the Penning geometry on an r-z
                  grid of 1025x2049 nodes, electrons at 1 eV, Bz = 0.5 T,
                  He at 1e-3 Pa with a constant collision frequency
@@ -150,3 +154,25 @@ def batched_penning(tmp: Path, n: int = 256, seed0: int = 0, np_range=(1e3, 1e5)
         ipath.write_text(f"add_particles_in_cylinder ELECTRON {npart} 2e-3 5e-3 15e-3\n")
         out.append((cfg, species, inter, cpath, spath, ipath, seed))
     return out
+
+
+def penning_segments(tmp: Path, n: int = 100_000, volts=None, Bz: float = 1.0, seed: int = 1, endcap: float = -25.0,
+                     nr: int = 65, nz: int = 129, tag: str = ""):
+    """Adjoint case: 8 ring segments (u_segment_k), particles loaded by the initscript loader."""
+    if volts is None:
+        volts = np.random.default_rng(100 + seed).uniform(-15.0, -5.0, 8)
+    cfg = dict(coord="CYLINDRICAL", boundary="FREE", geometry="PENNING_ENDCAP", r_max=5e-3, z_max=20e-3,
+               r_sampl=nr, z_sampl=nz, u_endcap=endcap, u_ring=0.0, ring_segments=8, selfconsistent=1, rf=0,
+               magnetic_field_const=1, Bz=float(Bz), Br=0.0, Bt=0.0, do_plot=0, macroparticle_factor=10.0,
+               n_particles_total=float(n), density_total=1e13, mover="ADVANCE_BORIS")
+    for k, v in enumerate(volts):
+        cfg[f"u_segment_{k}"] = float(v)
+    species = [dict(name="ELECTRON", type="ELECTRON", mass=ME, charge=-QE, dt=1e-11, density=1e13,
+                    temperature=11604.5)]
+    d = tmp / f"seg{tag}"
+    d.mkdir(parents=True, exist_ok=True)
+    cpath = write_config(cfg, d / "config.txt")
+    spath = write_species_conf(species, [], d / "species_conf.txt")
+    ipath = d / "initscript.txt"
+    ipath.write_text(f"add_particles_in_cylinder ELECTRON {n} 2e-3 5e-3 15e-3\n")
+    return cfg, species, [], cpath, spath, ipath, seed

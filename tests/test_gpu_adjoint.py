@@ -1,0 +1,136 @@
+"""Adjoint gradients (mag_adjoint_run) against central finite differences.
+
+Loss after N steps of the segmented Penning trap: mean axial kinetic energy
+[eV] plus lost fraction.  The adjoint of the collisionless step (push, gather,
+deposit, Poisson) with checkpoints gives d loss / d u_segment_k and
+d loss / d Bz in one run; central differences need two forward runs per
+parameter.  Against the oracle's FP64 runs (h = 1e-3 V, 1e-4 T) the bar is
+1e-3 relative.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+KEYS = [f"u_segment_{k}" for k in range(8)]
+
+
+@pytest.fixture(scope="module")
+def m(built):
+    import mag2d_gb300
+
+    return mag2d_gb300
+
+
+def _loss(m, tmp_path, volts, Bz, n, steps, tag):
+    from cases import penning_segments
+    from mag2d_gb300.autograd import loss_from_state
+
+    c = penning_segments(tmp_path, n=n, volts=volts, Bz=Bz, tag=tag)
+    pic = m.Pic(c[3], c[4], c[5], seed=c[6])
+    n0 = pic.speclist[0].diag()["n_live"]
+    pic.advance_init()
+    pic.advance(steps)
+    val = loss_from_state(pic, n0=n0)
+    pic.close()
+    return val
+
+
+def _oracle_loss(m, tmp_path, volts, Bz, parts, steps, tag):
+    """The loss of the oracle (the reference's algorithm in FP64) from the same initial particles."""
+    from cases import penning_segments
+    from mag2d_cases import Port
+
+    cfg, species, inter, cpath, spath, ipath, seed = penning_segments(tmp_path, n=len(parts[0]), volts=volts, Bz=Bz,
+                                                                      tag=tag)
+    mask, volt = m.config_geometry(cpath)
+    port = Port(cfg, species, inter, mask, volt, seed=1)
+    port.set_particles(0, *parts)
+    port.advance_init()
+    port.advance(steps)
+    o = port.particles(0)
+    live = o[o[:, 7] == 0]
+    e = 0.5 * species[0]["mass"] * live[:, 5] ** 2 / 1.602189e-19
+    return float(e.mean()) + (len(parts[0]) - len(live)) / len(parts[0])
+
+
+def _adjoint(m, tmp_path, n, steps, volts, Bz):
+    from cases import penning_segments
+
+    c = penning_segments(tmp_path, n=n, volts=volts, Bz=Bz, tag="adj")
+    pic = m.Pic(c[3], c[4], c[5], seed=c[6])
+    g0 = pic.speclist[0].particles()
+    parts = tuple(np.asarray(g0[k], dtype=np.float64) for k in ("x", "z", "vx", "vy", "vz"))
+    info, grad = pic.adjoint(steps, KEYS, checkpoint=64, grad_b=True)
+    pic.close()
+    return info, grad, parts
+
+
+def test_adjoint_matches_oracle_finite_differences(m, tmp_path):
+    """Central differences of the oracle (FP64, h = 1e-3 V and 1e-4 T) from the
+    same initial particles: agreement within 1e-3 relative."""
+    n, steps = 20_000, 300
+    volts = np.random.default_rng(7).uniform(-15.0, -5.0, 8)
+    Bz = 1.0
+    info, grad, parts = _adjoint(m, tmp_path, n, steps, volts, Bz)
+    assert info["n_live"] > 0.9 * info["n0"], info
+    scale = np.abs(grad[:8]).max()
+    assert scale > 0
+    for k in (2, 5):
+        h = 1e-3
+        vp, vm = volts.copy(), volts.copy()
+        vp[k] += h
+        vm[k] -= h
+        fd = (_oracle_loss(m, tmp_path, vp, Bz, parts, steps, f"op{k}")
+              - _oracle_loss(m, tmp_path, vm, Bz, parts, steps, f"om{k}")) / (2 * h)
+        assert abs(grad[k] - fd) <= 1e-3 * max(abs(fd), 0.05 * scale), (k, grad[k], fd)
+    hb = 1e-4
+    fd = (_oracle_loss(m, tmp_path, volts, Bz + hb, parts, steps, "obp")
+          - _oracle_loss(m, tmp_path, volts, Bz - hb, parts, steps, "obm")) / (2 * hb)
+    assert abs(grad[8 + 2] - fd) <= 1e-3 * abs(fd) + 1e-6, (grad[8 + 2], fd)
+
+
+def test_adjoint_matches_gpu_finite_differences(m, tmp_path):
+    """Central differences of the GPU's own forward runs.  The FP32 state adds
+    rounding noise of about 1e-8 relative to the loss, so the steps are 1e-2 V
+    and 1e-3 T and the bar 5e-3 relative; the forward part of the adjoint run
+    reproduces the plain run's loss."""
+    n, steps = 20_000, 300
+    volts = np.random.default_rng(7).uniform(-15.0, -5.0, 8)
+    Bz = 1.0
+    info, grad, _ = _adjoint(m, tmp_path, n, steps, volts, Bz)
+    base = _loss(m, tmp_path, volts, Bz, n, steps, "base")
+    assert abs(base - info["loss"]) <= 1e-9 * abs(base) + 1e-12, (base, info)
+    scale = np.abs(grad[:8]).max()
+    for k in (2, 5):
+        h = 1e-2
+        vp, vm = volts.copy(), volts.copy()
+        vp[k] += h
+        vm[k] -= h
+        fd = (_loss(m, tmp_path, vp, Bz, n, steps, f"p{k}") - _loss(m, tmp_path, vm, Bz, n, steps, f"m{k}")) / (2 * h)
+        assert abs(grad[k] - fd) <= 5e-3 * max(abs(fd), 0.05 * scale), (k, grad[k], fd)
+    # the axial energy hardly depends on Bz (about 1e-6 eV/T here): the FP32
+    # noise floor of this difference, 1e-8 eV / 2e-3 T, sets the absolute bar
+    hb = 1e-3
+    fd = (_loss(m, tmp_path, volts, Bz + hb, n, steps, "bp") - _loss(m, tmp_path, volts, Bz - hb, n, steps, "bm")) / (2 * hb)
+    assert abs(grad[8 + 2] - fd) <= 5e-3 * abs(fd) + 5e-6, (grad[8 + 2], fd)
+
+
+def test_autograd_function(m, tmp_path):
+    torch = pytest.importorskip("torch")
+    from cases import penning_segments
+    from mag2d_gb300.autograd import TrapLoss
+
+    def make(v, b):
+        c = penning_segments(tmp_path, n=5000, volts=v, Bz=float(b[2]), tag="ag")
+        return m.Pic(c[3], c[4], c[5], seed=c[6])
+
+    v = torch.tensor(np.random.default_rng(3).uniform(-15, -5, 8), dtype=torch.float64, requires_grad=True)
+    b = torch.tensor([0.0, 0.0, 1.0], dtype=torch.float64, requires_grad=True)
+    loss = TrapLoss.apply(v, b, make, 100, KEYS, 50)
+    loss.backward()
+    assert v.grad is not None and b.grad is not None
+    assert torch.isfinite(v.grad).all() and torch.isfinite(b.grad).all()
+    assert float(v.grad.abs().max()) > 0

@@ -134,3 +134,25 @@ def test_getpot_conventions(m, tmp_path):
     assert m.config_param(p, "x_sampl") == 200
     assert m.config_param(p, "extern_field") == 300.0
     assert m.config_param(p, "dx") == 2e-2 / 199
+
+
+def test_cylindrical_operator_symmetrised_by_row_weights():
+    """The adjoint's transpose solve A^-T = W A^-1 W^-1 needs W A symmetric on
+    the free nodes, W = diag(i) with 1/8 on the axis row (src/fields.cpp:149-238)."""
+    pytest.importorskip("scipy")
+    from mag2d_cases import poisson_system
+
+    nx, nz = 17, 33
+    mask = np.full((nx, nz), 2, dtype=np.int8)
+    mask[-1, :] = 0
+    mask[:, 0] = 0
+    mask[:, -1] = 0
+    mask[5:8, 10:12] = 0
+    cfg = dict(coord="CYLINDRICAL", x_max=5e-3, z_max=20e-3, x_sampl=nx, z_sampl=nz, macroparticle_factor=1.0)
+    A, _ = poisson_system(cfg, mask, np.zeros((nx, nz)), np.zeros((nx, nz)))
+    free = np.flatnonzero(((mask != 0) & (mask != 1)).reshape(-1))
+    Aff = A[free][:, free].toarray()
+    i = free // nz
+    w = np.where(i > 0, i.astype(float), 0.125)
+    S = w[:, None] * Aff
+    assert np.abs(S - S.T).max() <= 1e-12 * np.abs(S).max()
