@@ -55,6 +55,12 @@ def _env_rank():
 
 def _config(n_gpus: int, n_ions: int = N_IONS, sort_interval: int = 100, workload: str = "multipole") -> dict:
     par = f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"
+    if workload == "penning":
+        return {"workload": "penning_rz: Penning trap r-z 65x129 grid (r 0-5 mm, z 0-20 mm), end caps -10 V, ring "
+                            "0 V, Bz 1 T, electrons 1 eV in r<2 mm, 5<z<15 mm, self-consistent (Poisson refined to "
+                            "1e-10), collisions off, dt 10 ps", "grid": [65, 129], "particles_per_gpu": n_ions,
+                "species": 1, "l2": "flushed between timed steps (512 MB write, then 256 MB read)",
+                "sort_interval": sort_interval, "parallelism": par}
     if workload == "penning_large":
         return {"workload": "penning_large: Penning trap r-z 1025x2049 grid, 1e8 electrons (1 eV), Bz 0.5 T, "
                             "He 1e-3 Pa constant nu 1e6/s elastic MCC, self-consistent, Poisson refined to 1e-10, "
@@ -71,44 +77,52 @@ def _config(n_gpus: int, n_ions: int = N_IONS, sort_interval: int = 100, workloa
 # CPU baseline: the oracle port on the host cores
 def _cpu_worker(args):
     """One core: the oracle port on a sample of the workload; returns (particle_steps, seconds)."""
-    n, steps, seed = args
+    n, steps, seed, workload = args
     sys.path.insert(0, str(ROOT / "tests"))
-    import numpy as np  # noqa: F401
+    import numpy as np
 
-    from cases import multipole_xy
-    from mag2d_cases import Port, load_port  # noqa: F401
+    from cases import multipole_xy, penning_rz
+    from mag2d_cases import Port
 
     with tempfile.TemporaryDirectory() as d:
         tmp = Path(d)
-        cfg, species, inter, cpath, spath, parts, loaded = multipole_xy(tmp, n=n, n_nodes=GRID, seed=seed)
-        import numpy as np
+        if workload == "penning":
+            cfg, species, inter, cpath, spath, parts = penning_rz(tmp, n=n, seed=seed)
+            sp = 0
+            from mag2d_gb300 import config_geometry
 
-        mask = np.zeros((3, 3), dtype=np.int8)
-        volt = np.zeros((3, 3))
-        port = Port(cfg, species, inter, mask, volt, seed=seed, loaded_fields=loaded)
-        port.set_particles(1, *parts)
+            mask, volt = config_geometry(cpath)
+            port = Port(cfg, species, inter, mask, volt, seed=seed)
+        else:
+            cfg, species, inter, cpath, spath, parts, loaded = multipole_xy(tmp, n=n, n_nodes=GRID, seed=seed)
+            sp = 1
+            mask = np.zeros((3, 3), dtype=np.int8)
+            volt = np.zeros((3, 3))
+            port = Port(cfg, species, inter, mask, volt, seed=seed, loaded_fields=loaded)
+        port.set_particles(sp, *parts)
         port.advance_init()
         port.advance(2)
-        live0 = port.n_live(1)
+        live0 = port.n_live(sp)
         t = port.time_advance(steps)
-        live1 = port.n_live(1)
+        live1 = port.n_live(sp)
     return 0.5 * (live0 + live1) * steps, t
 
 
-def cpu_baseline(sample_particles: int = 20_000, sample_steps: int = 100, cores: int | None = None) -> dict:
+def cpu_baseline(sample_particles: int = 20_000, sample_steps: int = 100, cores: int | None = None,
+                 workload: str = "multipole") -> dict:
     import multiprocessing as mp
 
     cores = cores or os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(sample_particles, sample_steps, 100 + i) for i in range(cores)])
+        res = pool.map(_cpu_worker, [(sample_particles, sample_steps, 100 + i, workload) for i in range(cores)])
     wall = time.perf_counter() - t0
     ps = sum(r[0] for r in res)
     per_core = sum(r[0] / r[1] for r in res) / len(res)
     busy = max(r[1] for r in res)
     return {"value": ps / busy, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{cores} independent processes x ({sample_particles} ions x {sample_steps} steps) of the "
+            "sample": f"{cores} independent processes x ({sample_particles} particles x {sample_steps} steps) of the "
                       f"same workload, FP64 oracle port with SHR3/ziggurat RNG; per-core {per_core:.3e} {UNIT}; "
                       f"wall {wall:.1f} s incl. set-up",
             "per_core": per_core}
@@ -211,7 +225,15 @@ def run_ours(args) -> None:
     import mag2d_gb300 as m
 
     tmp = Path(tempfile.mkdtemp(prefix=f"mag2d_bench_{rank}_"))
-    if args.workload == "penning_large":
+    if args.workload == "penning":
+        from cases import penning_rz
+
+        cfg, species, inter, cpath, spath, parts = penning_rz(tmp, n=args.particles, seed=2 + rank)
+        pic = m.Pic(cpath, spath, seed=1000 + rank, device=local, capacity_hint=args.particles,
+                    push_vec=args.push_vec, sort_interval=args.sort_interval, poisson_tol=1e-10)
+        ion = pic.speclist[0]
+        ion.set_particles(*parts)
+    elif args.workload == "penning_large":
         from cases import penning_large
 
         cfg, species, inter, cpath, spath, _ = penning_large(tmp, n=args.particles, make_particles=False)
@@ -281,7 +303,8 @@ def run_ours(args) -> None:
         kern += np.array(pic.advance_timed(1))
     push_ms = kern[2] / nk
     live_now = ion.diag()["n_live"]
-    alg_bytes = BYTES_PER_PARTICLE_STEP * live_now
+    bytes_ps = 40 if args.workload == "penning" else BYTES_PER_PARTICLE_STEP  # no id read without collisions
+    alg_bytes = bytes_ps * live_now
     achieved = alg_bytes / (push_ms * 1e-3) / 1e9
 
     # e2e through the C ABI with host buffers: upload the state from host arrays,
@@ -317,10 +340,11 @@ def run_ours(args) -> None:
     if rank == 0:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         peak = peaks.get("hbm_gbs", 6800.0)
-        traffic_ps = _load_profile_traffic()
+        traffic_ps = _load_profile_traffic() if args.workload == "multipole" else None
         base = None
         if not args.no_cpu_baseline:
-            base = cpu_baseline(sample_particles=20_000, sample_steps=50)
+            base = cpu_baseline(sample_particles=20_000, sample_steps=50 if args.workload == "multipole" else 20,
+                                workload=args.workload)
         line = {
             "metric": METRIC, "value": psteps_all / total_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
@@ -335,7 +359,9 @@ def run_ours(args) -> None:
                          "frac": achieved / peak,
                          "traffic": (traffic_ps * live_now) if traffic_ps else None,
                          "traffic_source": "profiles/k_push_multipole_xy_8e6.md, scaled to the live ions",
-                         "kernel": "k_push<0,2,0,2> (gather + Boris + collision test + boundary)",
+                         "kernel": ("k_push<0,2,0,2> (gather + Boris + collision test + boundary)"
+                                    if args.workload == "multipole" else
+                                    "k_push<1,1,1,2> (cylindrical gather + Boris + r map + boundary + deposit)"),
                          "alg_bytes_per_launch": alg_bytes, "kernel_ms": push_ms,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured" if peaks else "fallback"},
             "kernel_ms_per_step": {"sort": kern[0] / nk, "solve": kern[1] / nk, "particles": kern[2] / nk,
@@ -505,14 +531,16 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=16, help="batched workload: instances timed one at a time")
     ap.add_argument("--plain-steps", type=int, default=10, help="batched workload: steps per plain instance")
     ap.add_argument("--adj-steps", type=int, default=2000, help="adjoint workload: steps of the run")
-    ap.add_argument("--workload", default="multipole", choices=["multipole", "penning_large", "batched", "adjoint"],
+    ap.add_argument("--workload", default="multipole",
+                    choices=["multipole", "penning", "penning_large", "batched", "adjoint"],
                     help="multipole: 22-pole ion trap 257x257, 1e6 ions (default); penning_large: r-z 1025x2049, "
                          "1e8 electrons, B 0.5 T, nu 1e6/s; batched: 256 Penning instances")
     ap.add_argument("--push-vec", type=int, default=0, help="slots per thread of the particle kernel (0: library default)")
     ap.add_argument("--sort-interval", type=int, default=100, help="steps between particle sorts (0: library default, 20)")
     args = ap.parse_args()
     if args.particles is None:
-        args.particles = {"penning_large": 100_000_000, "adjoint": 100_000}.get(args.workload, N_IONS)
+        args.particles = {"penning_large": 100_000_000, "adjoint": 100_000, "penning": 100_000}.get(args.workload,
+                                                                                                   N_IONS)
     if args.workload == "penning_large":
         if args.sort_interval == 100:
             args.sort_interval = 20
