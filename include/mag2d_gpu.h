@@ -213,6 +213,24 @@ void* mag_stream(mag_sim* sim);
 /* Number of kernel launches the handle has issued since creation. */
 int64_t mag_kernel_launches(mag_sim* sim);
 
+/* ---- Particle files ---------------------------------------------------------
+ * BaseSpecies::save / load (src/particles.cpp:32-93): int32 slot count, int32
+ * live count, then one 64-byte t_particle record (doubles x, y, z, vx, vy, vz,
+ * time_to_death; bool empty; padding) per live particle.  Loading replaces the
+ * species' particles; positions outside the domain are redrawn uniformly in
+ * it.  A config with particle_reload = 1 loads every species from
+ * <particle_reload_dir>/particles_<name>.dat at mag_create (src/pic.cpp:138-146). */
+int mag_species_save(mag_sim* sim, int species, const char* path);
+int mag_species_load(mag_sim* sim, int species, const char* path);
+/* Host-only reading and writing of that file.  read: n_out = live records,
+ * total_out = the slot count of the header; arrays of at least cap entries
+ * (any may be NULL).  write: y and time_to_death may be NULL (zeros). */
+int mag_particle_file_read(const char* path, int64_t cap, double* x, double* y, double* z, double* vx, double* vy,
+                           double* vz, double* time_to_death, int64_t* n_out, int64_t* total_out);
+int mag_particle_file_write(const char* path, int64_t total, int64_t n, const double* x, const double* y,
+                            const double* z, const double* vx, const double* vy, const double* vz,
+                            const double* time_to_death);
+
 /* ---- Adjoint gradients ------------------------------------------------------
  * Gradient of a trap diagnostic after nsteps steps,
  *   L = w_energy * mean over live particles of m vz^2 / 2 [eV]

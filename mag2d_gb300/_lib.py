@@ -92,6 +92,11 @@ def lib() -> ctypes.CDLL:
     L.mag_sync.argtypes = [P]
     L.mag_advance_timed.argtypes = [P, ctypes.c_uint64, D]
     L.mag_solve_status.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
+    L.mag_species_save.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
+    L.mag_species_load.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
+    L.mag_particle_file_read.argtypes = [ctypes.c_char_p, ctypes.c_int64] + [D] * 7 + [
+        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.mag_particle_file_write.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int64] + [D] * 7
     L.mag_adjoint_run.argtypes = [P, ctypes.POINTER(MagAdjCfg), D, ctypes.POINTER(MagAdjOut)]
     L.mag_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(MagInstanceDesc), ctypes.POINTER(MagOpts),
                                    ctypes.POINTER(P)]

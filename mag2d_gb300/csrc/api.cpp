@@ -11,6 +11,7 @@
 
 #include "adjoint.hpp"
 #include "batch.hpp"
+#include "particle_io.hpp"
 #include "sim.hpp"
 
 // A handle owns its Sim, or borrows one that a batch owns.
@@ -399,6 +400,74 @@ int mag_config_species(const char* config_path, const char* species_conf_path, i
 void* mag_stream(mag_sim* sim) { return sim && sim->s ? (void*)sim->s->stream : nullptr; }
 
 int64_t mag_kernel_launches(mag_sim* sim) { return sim && sim->s ? sim->s->launches : 0; }
+
+int mag_species_save(mag_sim* sim, int species, const char* path)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (!path) throw mag::Error(MAG_EINVAL, "null path");
+        sim->s->save_species(species, path);
+        return device_status(sim);
+    });
+}
+
+int mag_species_load(mag_sim* sim, int species, const char* path)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (!path) throw mag::Error(MAG_EINVAL, "null path");
+        sim->s->load_species(species, path);
+        return device_status(sim);
+    });
+}
+
+int mag_particle_file_read(const char* path, int64_t cap, double* x, double* y, double* z, double* vx, double* vy,
+                           double* vz, double* time_to_death, int64_t* n_out, int64_t* total_out)
+{
+    return guarded([&]() {
+        if (!path) throw mag::Error(MAG_EINVAL, "null path");
+        const mag::ParticleFile f = mag::read_particle_file(path);
+        const int64_t n = (int64_t)f.x.size();
+        if (n_out) *n_out = n;
+        if (total_out) *total_out = f.total;
+        if (n > cap && (x || y || z || vx || vy || vz || time_to_death))
+            throw mag::Error(MAG_EINVAL, "output arrays too small");
+        auto put = [&](double* o, const std::vector<double>& v) {
+            if (o) std::copy(v.begin(), v.end(), o);
+        };
+        put(x, f.x);
+        put(y, f.y);
+        put(z, f.z);
+        put(vx, f.vx);
+        put(vy, f.vy);
+        put(vz, f.vz);
+        put(time_to_death, f.ttd);
+        return MAG_OK;
+    });
+}
+
+int mag_particle_file_write(const char* path, int64_t total, int64_t n, const double* x, const double* y,
+                            const double* z, const double* vx, const double* vy, const double* vz,
+                            const double* time_to_death)
+{
+    return guarded([&]() {
+        if (!path || n < 0 || (n > 0 && (!x || !z || !vx || !vy || !vz)))
+            throw mag::Error(MAG_EINVAL, "invalid arguments");
+        mag::ParticleFile f;
+        f.total = (int32_t)std::max(total, n);
+        f.x.assign(x, x + n);
+        f.z.assign(z, z + n);
+        f.vx.assign(vx, vx + n);
+        f.vy.assign(vy, vy + n);
+        f.vz.assign(vz, vz + n);
+        if (y) f.y.assign(y, y + n);
+        else f.y.assign(n, 0.0);
+        if (time_to_death) f.ttd.assign(time_to_death, time_to_death + n);
+        else f.ttd.assign(n, 0.0);
+        mag::write_particle_file(path, f);
+        return MAG_OK;
+    });
+}
 
 int mag_adjoint_run(mag_sim* sim, const mag_adj_cfg* cfg, double* grad_out, mag_adj_out* out)
 {

@@ -12,6 +12,7 @@
 
 #include "kernels.hpp"
 #include "multigrid_host.hpp"
+#include "particle_io.hpp"
 
 namespace mag {
 
@@ -93,6 +94,9 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     setup_species();
     if (opts.capacity_hint > 0)
         for (size_t s = 0; s < sp.size(); ++s) ensure_capacity((int)s, opts.capacity_hint);
+    if (p.particle_reload)  // Pic constructor (src/pic.cpp:138-146): every species from particle_reload_dir
+        for (size_t s = 0; s < sp.size(); ++s)
+            load_species((int)s, p.particle_reload_dir + "/particles_" + species_prm[s].name + ".dat");
     MAG_CK(cudaStreamSynchronize(stream));
     int e = sync();
     if (e != 0) throw Error(e, "initial field solve failed (device status " + std::to_string(e) + ")");
@@ -999,6 +1003,44 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     S.next_id = (uint32_t)n;
     upload_slots(s);
     sort_due = true;
+}
+
+// BaseSpecies::save (src/particles.cpp:32-57): the live particles as 64-byte
+// t_particle records after the slot and live counts
+void Sim::save_species(int s, const std::string& path)
+{
+    const int64_t n = sp[s].n_slots;
+    ParticleFile f;
+    for (auto* v : {&f.x, &f.z, &f.vx, &f.vy, &f.vz}) v->resize(n);
+    int64_t m = 0;
+    get_particles(s, n, f.x.data(), f.z.data(), f.vx.data(), f.vy.data(), f.vz.data(), nullptr, &m);
+    for (auto* v : {&f.x, &f.z, &f.vx, &f.vy, &f.vz}) v->resize(m);
+    f.y.assign(m, 0.0);
+    f.ttd.assign(m, 0.0);
+    f.total = (int32_t)std::max<int64_t>(n, m);
+    write_particle_file(path, f);
+}
+
+// BaseSpecies::load (src/particles.cpp:59-93): the file's particles replace
+// the species'; a position outside [x_min, x_max] or [z_min, z_max] is redrawn
+// uniformly in that range, as the reference does for particles that left the
+// domain in a non-self-consistent run
+void Sim::load_species(int s, const std::string& path)
+{
+    ParticleFile f = read_particle_file(path);
+    uint64_t st = seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(s + 1));
+    auto uni = [&]() {  // SplitMix64 (Steele, Lea, Flood 2014) -> [0, 1)
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (size_t i = 0; i < f.x.size(); ++i) {
+        if (f.x[i] < x0 || f.x[i] > xmax) f.x[i] = (xmax - x0) * uni() + x0;
+        if (f.z[i] < z0 || f.z[i] > zmax) f.z[i] = (zmax - z0) * uni() + z0;
+    }
+    set_particles(s, (int64_t)f.x.size(), f.x.data(), f.z.data(), f.vx.data(), f.vy.data(), f.vz.data());
 }
 
 void Sim::get_rho_fixed(int s, int64_t* out)

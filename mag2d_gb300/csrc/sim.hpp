@@ -156,6 +156,8 @@ public:
                        const double* vz);
     void deposit_all();
     void get_rho_fixed(int s, int64_t* out);
+    void save_species(int s, const std::string& path);  // BaseSpecies::save
+    void load_species(int s, const std::string& path);  // BaseSpecies::load
     Counters counters(int s);
     void energy(int s, double& sum_v2, unsigned long long& n);
     uint64_t niter(int s);

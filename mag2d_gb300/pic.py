@@ -120,6 +120,14 @@ class Species:
         check(lib().mag_diag(self._pic.h, self.index, ctypes.byref(d)))
         return {k: getattr(d, k) for k, _ in d._fields_}
 
+    def save(self, path) -> None:
+        """BaseSpecies::save (src/particles.cpp:32-57)."""
+        check(lib().mag_species_save(self._pic.h, self.index, str(path).encode()))
+
+    def load(self, path) -> None:
+        """BaseSpecies::load (src/particles.cpp:59-93)."""
+        check(lib().mag_species_load(self._pic.h, self.index, str(path).encode()))
+
     def rho_fixed(self) -> np.ndarray:
         nx, nz = self._pic.shape
         out = np.zeros((nx, nz), dtype=np.int64)
@@ -252,6 +260,28 @@ class Pic:
     @property
     def kernel_launches(self) -> int:
         return int(lib().mag_kernel_launches(self.h))
+
+
+def read_particle_file(path) -> dict:
+    """The particles of a BaseSpecies::save file (host only, no GPU)."""
+    n, total = ctypes.c_int64(), ctypes.c_int64()
+    check(lib().mag_particle_file_read(str(path).encode(), 0, *([None] * 7), ctypes.byref(n), ctypes.byref(total)))
+    out = {k: np.zeros(n.value) for k in ("x", "y", "z", "vx", "vy", "vz", "time_to_death")}
+    check(lib().mag_particle_file_read(str(path).encode(), n.value, *[_dp(out[k]) for k in out], ctypes.byref(n),
+                                       ctypes.byref(total)))
+    out["total"] = total.value
+    return out
+
+
+def write_particle_file(path, x, z, vx, vy, vz, *, y=None, time_to_death=None, total: int = 0) -> None:
+    """Write particles in the BaseSpecies::save format (host only, no GPU)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, z, vx, vy, vz)]
+    n = len(arrs[0])
+    yy = None if y is None else np.ascontiguousarray(y, dtype=np.float64)
+    tt = None if time_to_death is None else np.ascontiguousarray(time_to_death, dtype=np.float64)
+    check(lib().mag_particle_file_write(str(path).encode(), int(total), n, _dp(arrs[0]),
+                                        None if yy is None else _dp(yy), _dp(arrs[1]), _dp(arrs[2]), _dp(arrs[3]),
+                                        _dp(arrs[4]), None if tt is None else _dp(tt)))
 
 
 def config_param(config, key: str) -> float:

@@ -229,6 +229,17 @@ int ref_get_particles(void* h, int sp, double* out)
     });
 }
 
+// BaseSpecies::save / load (src/particles.cpp:32-93) of species sp
+int ref_save(void* h, int sp, const char* path)
+{
+    return with_pic(h, [&](auto& p) { p.speclist[sp]->save(path); return 0; });
+}
+
+int ref_load(void* h, int sp, const char* path)
+{
+    return with_pic(h, [&](auto& p) { p.speclist[sp]->load(path); return (int)p.speclist[sp]->particles.size(); });
+}
+
 int ref_advance_init(void* h)
 {
     return with_pic(h, [&](auto& p) { p.advance_init(); return 0; });

@@ -11,6 +11,9 @@ present), and stores inputs and outputs as small .npz files:
   geometry.npz         t_grid mask and voltage of every reference geometry
   params.npz           derived Param values of the reference's config files
   species.npz          parsed species, rates and lifetimes of its species_conf files
+  particles_ref.dat    a particle file written by BaseSpecies::save, with its
+  particles.npz        inputs, and the particles BaseSpecies::load makes of a
+                       file holding particles outside the domain
 
 The CPU tests replay the same inputs through the oracle port (bit-exact) and
 through the product's host-side parser and geometry builder.
@@ -291,9 +294,39 @@ def gen_params_species():
     save("params_species.npz", **out)
 
 
+def gen_particle_file():
+    """BaseSpecies::save of known particles, and BaseSpecies::load of a file
+    with particles outside the domain (they are redrawn inside it)."""
+    cfg = dict(coord="CARTESIAN", geometry="EMPTY", x_max=1e-2, z_max=2e-2, x_sampl=9, z_sampl=17,
+               selfconsistent=0, rf=0, do_plot=0)
+    cp = write_config(cfg, TMP / "pf_cfg.txt")
+    sp = write_species_conf([dict(name="ELECTRON", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11,
+                                  temperature=11604.5)], [], TMP / "pf_sp.txt")
+    rng = np.random.default_rng(44)
+    n = 50
+    x = rng.uniform(0, 1e-2, n)
+    z = rng.uniform(0, 2e-2, n)
+    v = rng.normal(0, 5e5, (3, n))
+    ref = Ref(cp, sp, TMP / "o", 1)
+    ref.set_particles(0, x, z, v[0], v[1], v[2])
+    ref.save(0, HERE / "particles_ref.dat")
+    # a file whose particles 0, 7, 19 lie outside the domain
+    xo, zo = x.copy(), z.copy()
+    xo[0], zo[7], xo[19], zo[19] = -1e-3, 3e-2, 2e-2, -5e-3
+    ref2 = Ref(cp, sp, TMP / "o", 1)
+    ref2.set_particles(0, xo, zo, v[0], v[1], v[2])
+    ref2.save(0, TMP / "oob.dat")
+    ref3 = Ref(cp, sp, TMP / "o", 1)
+    ref3.load(0, TMP / "oob.dat")
+    loaded = ref3.particles(0)
+    save("particles.npz", x=x, z=z, vx=v[0], vy=v[1], vz=v[2], x_oob=xo, z_oob=zo, loaded=loaded,
+         meta=meta(cfg=cfg))
+
+
 if __name__ == "__main__":
     gen_rng()
     gen_steps()
     gen_solves()
     gen_geometry()
     gen_params_species()
+    gen_particle_file()

@@ -420,6 +420,12 @@ class Ref:
         self.L.ref_get_particles(self.h, sp, _dp(out))
         return out[:n]
 
+    def save(self, sp: int, path) -> None:
+        self._check(self.L.ref_save(self.h, sp, str(path).encode()))
+
+    def load(self, sp: int, path) -> int:
+        return self._check(self.L.ref_load(self.h, sp, str(path).encode()))
+
     def seed(self, s: int):
         self.L.ref_seed(self.h, s)
 

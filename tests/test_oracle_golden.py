@@ -180,3 +180,27 @@ def test_fixed_point_deposit_properties(port_lib):
     # order independence: any permutation gives identical integers
     perm = rng.permutation(n)
     assert np.array_equal(deposit_fixed(nx, nz, xf[perm], zf[perm]), acc)
+
+
+def test_particle_file_matches_reference_save(built):
+    """The library reads the file BaseSpecies::save wrote (exact doubles) and
+    writes the same bytes for the same particles (record padding aside)."""
+    import mag2d_gb300 as m
+
+    d = np.load(GOLDEN / "particles.npz")
+    f = m.read_particle_file(GOLDEN / "particles_ref.dat")
+    assert f["total"] == len(d["x"])
+    for k in ("x", "z", "vx", "vy", "vz"):
+        assert np.array_equal(f[k], d[k]), k
+    assert not f["y"].any() and not f["time_to_death"].any()
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as t:
+        p = Path(t) / "ours.dat"
+        m.write_particle_file(p, d["x"], d["z"], d["vx"], d["vy"], d["vz"], total=len(d["x"]))
+        ours, ref = p.read_bytes(), (GOLDEN / "particles_ref.dat").read_bytes()
+    assert len(ours) == len(ref) == 8 + 64 * len(d["x"])
+    assert ours[:8] == ref[:8]
+    for i in range(len(d["x"])):
+        a = 8 + 64 * i
+        assert ours[a:a + 57] == ref[a:a + 57], i  # 7 doubles and the empty flag
