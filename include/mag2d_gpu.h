@@ -213,6 +213,26 @@ void* mag_stream(mag_sim* sim);
 /* Number of kernel launches the handle has issued since creation. */
 int64_t mag_kernel_launches(mag_sim* sim);
 
+/* ---- Sampled distributions ------------------------------------------------
+ * Pic::dist_reset / dist_sample (src/pic.cpp:412-428): each sample adds every
+ * species' kinetic-energy histogram (Histogram of 200 bins over [0, E_max],
+ * src/particles.hpp:169, filled as energy_dist_compute does) and its charge
+ * deposit (rhoAverage), and the potential (uAvg).  Computed on the GPU. */
+int mag_dist_reset(mag_sim* sim);
+int mag_dist_sample(mag_sim* sim);
+int mag_dist_samples(mag_sim* sim);  /* samples since the last reset, or < 0 on error */
+/* Histogram::print values of species s: bin centres and data / norm; stats =
+ * n_val, sum, n_val_tot, sum_tot (mean = sum / n_val, mean_tot = sum_tot /
+ * n_val_tot).  Arrays of cap >= 200 entries (any may be NULL).  Returns the
+ * number of bins or a negative status. */
+int mag_energy_dist(mag_sim* sim, int species, int cap, double* centers, double* values, double* stats);
+/* The average over the samples of MAG_U (uAvg) or MAG_SPECIES_RHO + s (rhoAverage) */
+int mag_get_average(mag_sim* sim, int which, double* host_out);
+/* BaseSpecies::print_distribution files <dir>/<name>_energy_dist.dat and
+ * <name>_rho.dat, and Fields::u_print (potential.dat) at path */
+int mag_print_distribution(mag_sim* sim, const char* dir);
+int mag_print_field(mag_sim* sim, const char* path);
+
 /* ---- Particle files ---------------------------------------------------------
  * BaseSpecies::save / load (src/particles.cpp:32-93): int32 slot count, int32
  * live count, then one 64-byte t_particle record (doubles x, y, z, vx, vy, vz,

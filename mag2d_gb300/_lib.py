@@ -92,6 +92,13 @@ def lib() -> ctypes.CDLL:
     L.mag_sync.argtypes = [P]
     L.mag_advance_timed.argtypes = [P, ctypes.c_uint64, D]
     L.mag_solve_status.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
+    L.mag_dist_reset.argtypes = [P]
+    L.mag_dist_sample.argtypes = [P]
+    L.mag_dist_samples.argtypes = [P]
+    L.mag_energy_dist.argtypes = [P, ctypes.c_int, ctypes.c_int, D, D, D]
+    L.mag_get_average.argtypes = [P, ctypes.c_int, D]
+    L.mag_print_distribution.argtypes = [P, ctypes.c_char_p]
+    L.mag_print_field.argtypes = [P, ctypes.c_char_p]
     L.mag_species_save.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
     L.mag_species_load.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
     L.mag_particle_file_read.argtypes = [ctypes.c_char_p, ctypes.c_int64] + [D] * 7 + [

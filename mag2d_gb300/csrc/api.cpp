@@ -401,6 +401,78 @@ void* mag_stream(mag_sim* sim) { return sim && sim->s ? (void*)sim->s->stream : 
 
 int64_t mag_kernel_launches(mag_sim* sim) { return sim && sim->s ? sim->s->launches : 0; }
 
+int mag_dist_reset(mag_sim* sim)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->dist_reset();
+        return device_status(sim);
+    });
+}
+
+int mag_dist_sample(mag_sim* sim)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->dist_sample();
+        return MAG_OK;
+    });
+}
+
+int mag_dist_samples(mag_sim* sim)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        return sim->s->dist_samples();
+    });
+}
+
+int mag_energy_dist(mag_sim* sim, int species, int cap, double* centers, double* values, double* stats)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        std::vector<double> pos, val;
+        double st[4];
+        sim->s->energy_dist(species, pos, val, st);
+        if ((int)pos.size() > cap && (centers || values)) throw mag::Error(MAG_EINVAL, "output arrays too small");
+        if (centers) std::copy(pos.begin(), pos.end(), centers);
+        if (values) std::copy(val.begin(), val.end(), values);
+        if (stats) std::copy(st, st + 4, stats);
+        return (int)pos.size();
+    });
+}
+
+int mag_get_average(mag_sim* sim, int which, double* host_out)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!host_out) throw mag::Error(MAG_EINVAL, "null output");
+        if (sim->s->dist_samples() <= 0) throw mag::Error(MAG_EINVAL, "no samples (call mag_dist_sample first)");
+        sim->s->average(which, host_out);
+        return device_status(sim);
+    });
+}
+
+int mag_print_distribution(mag_sim* sim, const char* dir)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!dir) throw mag::Error(MAG_EINVAL, "null directory");
+        sim->s->print_distribution(dir);
+        return device_status(sim);
+    });
+}
+
+int mag_print_field(mag_sim* sim, const char* path)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!path) throw mag::Error(MAG_EINVAL, "null path");
+        sim->s->print_field(path);
+        return device_status(sim);
+    });
+}
+
 int mag_species_save(mag_sim* sim, int species, const char* path)
 {
     return guarded([&]() {

@@ -59,5 +59,12 @@ int launch_interleave(const float* a, const float* b, float2* out, long long n, 
 int launch_fill_u32(uint32_t* p, uint32_t v0, int64_t n, cudaStream_t s);
 int launch_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n,
                   double* out_sum_v2, unsigned long long* out_n, cudaStream_t s);
+// energy histogram of the live particles (Histogram::add), bins += counts,
+// stats += (n_val, sum, n_val_tot, sum_tot)
+int launch_energy_hist(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n, double mass,
+                       double qe, double emin, double emax, int nbins, unsigned long long* bins, double* stats,
+                       cudaStream_t s);
+int launch_axpy_i64(double* acc, const unsigned long long* src, double w, long long n, cudaStream_t s);
+int launch_axpy_f64(double* acc, const double* src, double w, long long n, cudaStream_t s);
 
 }  // namespace mag

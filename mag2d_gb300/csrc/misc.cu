@@ -100,25 +100,116 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t v0, int64_t n)
         p[k] = v0 + (uint32_t)k;
 }
 
-__global__ void k_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n, double* sum,
-                         unsigned long long* cnt)
+// sum of v^2 over live particles (FP64) and their count: per-thread partial
+// sums, a block reduction in shared memory, one atomic per block
+__global__ void __launch_bounds__(256) k_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz,
+                                                int64_t n, double* sum, unsigned long long* cnt)
 {
+    __shared__ double ss[8];
+    __shared__ unsigned long long sc[8];
     double s = 0.0;
     unsigned long long c = 0;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         if (x[k] == kDead) continue;
-        const double a = vx[k], b = vy[k], d = vz[k];
-        s += a * a + b * b + d * d;
+        const float a = vx[k], b = vy[k], d = vz[k];
+        s += (double)fmaf(a, a, fmaf(b, b, d * d));
         ++c;
     }
     for (int o = 16; o > 0; o >>= 1) {
         s += __shfl_xor_sync(0xffffffffu, s, o);
         c += __shfl_xor_sync(0xffffffffu, c, o);
     }
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        atomicAdd(sum, s);
-        atomicAdd(cnt, c);
+        ss[w] = s;
+        sc[w] = c;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        unsigned long long u = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            t += ss[i];
+            u += sc[i];
+        }
+        if (u) {
+            atomicAdd(sum, t);
+            atomicAdd(cnt, u);
+        }
+    }
+}
+
+// Histogram::add (src/histogram.cpp:22-35) of the kinetic energies [eV] of the
+// live particles (BaseSpecies::energy_dist_compute, src/particles.cpp:412-418),
+// in the reference's operation order: bins counted in shared memory; stats =
+// n_val, sum, n_val_tot, sum_tot
+__global__ void __launch_bounds__(256) k_energy_hist(const uint32_t* x, const float* vx, const float* vy,
+                                                     const float* vz, int64_t n, double mass, double qe, double emin,
+                                                     double emax, int nbins, unsigned long long* bins, double* stats)
+{
+    extern __shared__ unsigned int sbin[];
+    __shared__ double s_sum[8], s_tot[8];
+    __shared__ unsigned long long s_nv[8], s_nt[8];
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) sbin[i] = 0;
+    __syncthreads();
+    double sum = 0.0, tot = 0.0;
+    unsigned long long nv = 0, nt = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        if (x[k] == kDead) continue;
+        const double a = vx[k], b = vy[k], d = vz[k];
+        const double f = (a * a + d * d + b * b) * mass * 0.5 / qe;  // operation order of the reference
+        if (f < emax && f > emin) {
+            atomicAdd(&sbin[min((int)((f - emin) * nbins / (emax - emin)), nbins - 1)], 1u);
+            ++nv;
+            sum += f;
+        }
+        ++nt;
+        tot += f;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        nv += __shfl_xor_sync(0xffffffffu, nv, o);
+        nt += __shfl_xor_sync(0xffffffffu, nt, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_sum[w] = sum;
+        s_tot[w] = tot;
+        s_nv[w] = nv;
+        s_nt[w] = nt;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+        if (sbin[i]) atomicAdd(&bins[i], (unsigned long long)sbin[i]);
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        unsigned long long c = 0, d = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            a += s_sum[i];
+            b += s_tot[i];
+            c += s_nv[i];
+            d += s_nt[i];
+        }
+        if (d) {
+            atomicAdd(&stats[0], (double)c);
+            atomicAdd(&stats[1], a);
+            atomicAdd(&stats[2], (double)d);
+            atomicAdd(&stats[3], b);
+        }
+    }
+}
+
+// acc[k] += w * src[k] (averaged fields: Field2D::add of rhoAverage / uAvg)
+__global__ void k_axpy_i64(double* acc, const unsigned long long* src, double w, long long n)
+{
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        acc[k] += w * (double)(long long)src[k];
+}
+__global__ void k_axpy_f64(double* acc, const double* src, double w, long long n)
+{
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        acc[k] += w * src[k];
 }
 
 __global__ void k_interleave(const float* a, const float* b, float2* out, long long n)
@@ -158,7 +249,29 @@ int launch_energy(const uint32_t* x, const float* vx, const float* vy, const flo
                   unsigned long long* out_n, cudaStream_t s)
 {
     if (n == 0) return 0;
-    k_energy<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8), 256, 0, s>>>(x, vx, vy, vz, n, out_sum_v2, out_n);
+    k_energy<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(x, vx, vy, vz, n, out_sum_v2, out_n);
+    return 1;
+}
+
+int launch_energy_hist(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n, double mass,
+                       double qe, double emin, double emax, int nbins, unsigned long long* bins, double* stats,
+                       cudaStream_t s)
+{
+    if (n == 0) return 0;
+    k_energy_hist<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 4), 256, (size_t)nbins * 4, s>>>(
+        x, vx, vy, vz, n, mass, qe, emin, emax, nbins, bins, stats);
+    return 1;
+}
+
+int launch_axpy_i64(double* acc, const unsigned long long* src, double w, long long n, cudaStream_t s)
+{
+    k_axpy_i64<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 8), 256, 0, s>>>(acc, src, w, n);
+    return 1;
+}
+
+int launch_axpy_f64(double* acc, const double* src, double w, long long n, cudaStream_t s)
+{
+    k_axpy_f64<<<(unsigned)std::min<long long>((n + 255) / 256, 152 * 8), 256, 0, s>>>(acc, src, w, n);
     return 1;
 }
 

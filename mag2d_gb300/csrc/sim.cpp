@@ -1005,6 +1005,120 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     sort_due = true;
 }
 
+// Pic::dist_reset (src/pic.cpp:412-420)
+void Sim::dist_reset()
+{
+    const size_t nn = (size_t)nx * nz;
+    dist.resize(sp.size());
+    for (auto& d : dist) {
+        d.bins.alloc(kEnergyBins);
+        d.bins.zero(stream);
+        d.stats.alloc(4);
+        d.stats.zero(stream);
+        d.rho_sum.alloc(nn);
+        d.rho_sum.zero(stream);
+    }
+    u_sum.alloc(nn);
+    u_sum.zero(stream);
+    nsampl = 0;
+}
+
+// Pic::dist_sample (src/pic.cpp:421-428): per species the energy histogram and
+// rho added to rhoAverage (BaseSpecies::dist_sample, src/particles.cpp:385-392),
+// the potential added to uAvg (Fields::u_sample, src/fields.cpp:11-15).  rho is
+// the charge deposit of the particles' current positions.
+void Sim::dist_sample()
+{
+    if (dist.size() != sp.size()) dist_reset();
+    const size_t nn = (size_t)nx * nz;
+    if (rho_scratch.n < nn) rho_scratch.alloc(nn);
+    for (size_t s = 0; s < sp.size(); ++s) {
+        SpeciesState& S = sp[s];
+        if (S.n_slots == 0) continue;
+        launches += launch_energy_hist(S.x.p, S.vx.p, S.vy.p, S.vz.p, S.n_slots, S.prm.mass, kQe, 0.0, S.E_max,
+                                       kEnergyBins, dist[s].bins.p, dist[s].stats.p, stream);
+        rho_scratch.zero(stream);
+        PushArgs pa = push_args((int)s, false);
+        pa.rho = rho_scratch.p;
+        launches += launch_deposit(pa, stream);
+        launches += launch_axpy_i64(dist[s].rho_sum.p, rho_scratch.p, S.prm.charge * std::ldexp(1.0, -2 * kDepositShift),
+                                    (long long)nn, stream);
+    }
+    launches += launch_axpy_f64(u_sum.p, u64.p, 1.0, (long long)nn, stream);
+    ++nsampl;
+    MAG_CK(cudaGetLastError());
+}
+
+void Sim::energy_dist(int s, std::vector<double>& pos, std::vector<double>& val, double stats[4])
+{
+    if (dist.size() != sp.size()) dist_reset();
+    std::vector<unsigned long long> b(kEnergyBins);
+    dist[s].bins.download(b.data(), kEnergyBins, stream);
+    dist[s].stats.download(stats, 4, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
+    const double mn = 0.0, mx = sp[s].E_max;
+    const double norm = stats[0] * (mx - mn) / kEnergyBins;  // Histogram::norm
+    pos.resize(kEnergyBins);
+    val.resize(kEnergyBins);
+    for (int i = 0; i < kEnergyBins; ++i) {
+        pos[i] = mn + (mx - mn) * (i + .5) / kEnergyBins;  // Histogram::position
+        val[i] = (double)b[i] / norm;
+    }
+}
+
+void Sim::average(int which, double* out)
+{
+    if (dist.size() != sp.size()) dist_reset();
+    const size_t nn = (size_t)nx * nz;
+    std::vector<double> h(nn);
+    if (which == 0) u_sum.download(h.data(), nn, stream);
+    else if (which >= 5 && which - 5 < (int)sp.size()) dist[which - 5].rho_sum.download(h.data(), nn, stream);
+    else throw Error(-1, "average: field must be MAG_U or MAG_SPECIES_RHO + species");
+    MAG_CK(cudaStreamSynchronize(stream));
+    const double f = 1.0 / nsampl;  // the reference's print factor 1.0/nsampl
+    for (size_t k = 0; k < nn; ++k) out[k] = h[k] * f;
+}
+
+namespace {
+// Field2D::print (src/Field2D.cpp:30-38): x, z, value per line, a blank line per x row
+void print_field2d(const std::string& path, int nx, int nz, double dx, double dz, double x0, double z0,
+                   const std::vector<double>& v)
+{
+    std::ofstream out(path);
+    if (!out) throw Error(-6, "cannot open " + path + " for writing");
+    for (int j = 0; j < nx; j++) {
+        for (int l = 0; l < nz; l++) out << j * dx + x0 << "\t" << l * dz + z0 << "\t" << v[(size_t)j * nz + l] << std::endl;
+        out << std::endl;
+    }
+}
+}  // namespace
+
+// Pic::print_distribution (src/pic.cpp:450-455) -> BaseSpecies::print_distribution
+// (src/particles.cpp:376-383): <name>_energy_dist.dat and <name>_rho.dat
+void Sim::print_distribution(const std::string& dir)
+{
+    const size_t nn = (size_t)nx * nz;
+    for (size_t s = 0; s < sp.size(); ++s) {
+        std::vector<double> pos, val;
+        double st[4];
+        energy_dist((int)s, pos, val, st);
+        std::ofstream out(dir + "/" + species_prm[s].name + "_energy_dist.dat");
+        if (!out) throw Error(-6, "cannot open " + dir + "/" + species_prm[s].name + "_energy_dist.dat");
+        for (int i = 0; i < kEnergyBins; ++i) out << pos[i] << "\t" << val[i] << std::endl;  // Histogram::print
+        std::vector<double> r(nn);
+        average((int)(5 + s), r.data());
+        print_field2d(dir + "/" + species_prm[s].name + "_rho.dat", nx, nz, dx, dz, x0, z0, r);
+    }
+}
+
+// Pic::print_field (src/pic.cpp:456-459) -> Fields::u_print: uAvg / nsampl
+void Sim::print_field(const std::string& path)
+{
+    std::vector<double> u((size_t)nx * nz);
+    average(0, u.data());
+    print_field2d(path, nx, nz, dx, dz, x0, z0, u);
+}
+
 // BaseSpecies::save (src/particles.cpp:32-57): the live particles as 64-byte
 // t_particle records after the slot and live counts
 void Sim::save_species(int s, const std::string& path)

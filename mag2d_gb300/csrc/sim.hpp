@@ -156,6 +156,15 @@ public:
                        const double* vz);
     void deposit_all();
     void get_rho_fixed(int s, int64_t* out);
+    // sampled distributions (BaseSpecies::dist_sample / dist_reset, Pic::dist_sample)
+    void dist_reset();
+    void dist_sample();
+    int dist_samples() const { return nsampl; }
+    // Histogram of species s: bin centres, print values (data / norm), stats (n_val, sum, n_val_tot, sum_tot)
+    void energy_dist(int s, std::vector<double>& pos, std::vector<double>& val, double stats[4]);
+    void average(int which, double* out);  // MAG_U: uAvg / nsampl; MAG_SPECIES_RHO + s: rhoAverage / nsampl
+    void print_distribution(const std::string& dir);
+    void print_field(const std::string& path);
     void save_species(int s, const std::string& path);  // BaseSpecies::save
     void load_species(int s, const std::string& path);  // BaseSpecies::load
     Counters counters(int s);
@@ -170,6 +179,16 @@ private:
     int emode = 1;
     bool check_mask = true;
     DevArray<int8_t> d_mask;
+    struct DistState {
+        DevArray<unsigned long long> bins;  // energy_dist counts (200 bins over [0, E_max])
+        DevArray<double> stats;             // n_val, sum, n_val_tot, sum_tot
+        DevArray<double> rho_sum;           // sum of sampled rho [C per macro particle]
+    };
+    std::vector<DistState> dist;
+    DevArray<double> u_sum;
+    DevArray<unsigned long long> rho_scratch;
+    int nsampl = 0;
+    static constexpr int kEnergyBins = 200;  // energy_dist(200, 0, E_max), src/particles.hpp:169
     DevArray<uint8_t> d_cellfree;
     DevArray<double> d_volt, u64, urf64, b64, rho64, red;
     DevArray<float> Exf, Ezf, Exf_rf, Ezf_rf, d_Br, d_Bz;

@@ -120,6 +120,19 @@ class Species:
         check(lib().mag_diag(self._pic.h, self.index, ctypes.byref(d)))
         return {k: getattr(d, k) for k, _ in d._fields_}
 
+    def energy_dist(self) -> dict:
+        """Sampled energy histogram (Histogram::print values) and its statistics."""
+        c, v, st = np.zeros(200), np.zeros(200), np.zeros(4)
+        n = check(lib().mag_energy_dist(self._pic.h, self.index, 200, _dp(c), _dp(v), _dp(st)))
+        return {"centers": c[:n], "values": v[:n], "n_val": st[0], "mean": st[1] / st[0] if st[0] else 0.0,
+                "n_val_tot": st[2], "mean_tot": st[3] / st[2] if st[2] else 0.0}
+
+    @property
+    def rho_average(self) -> np.ndarray:
+        out = np.zeros(self._pic.shape)
+        check(lib().mag_get_average(self._pic.h, MAG_SPECIES_RHO + self.index, _dp(out)))
+        return out
+
     def save(self, path) -> None:
         """BaseSpecies::save (src/particles.cpp:32-57)."""
         check(lib().mag_species_save(self._pic.h, self.index, str(path).encode()))
@@ -220,6 +233,24 @@ class Pic:
         ms = np.zeros(4)
         check(lib().mag_advance_timed(self.h, n, _dp(ms)))
         return tuple(ms)
+
+    def dist_reset(self) -> None:
+        check(lib().mag_dist_reset(self.h))
+
+    def dist_sample(self) -> None:
+        check(lib().mag_dist_sample(self.h))
+
+    @property
+    def u_average(self) -> np.ndarray:
+        out = np.zeros(self.shape)
+        check(lib().mag_get_average(self.h, MAG_U, _dp(out)))
+        return out
+
+    def print_distribution(self, directory) -> None:
+        check(lib().mag_print_distribution(self.h, str(directory).encode()))
+
+    def print_field(self, path) -> None:
+        check(lib().mag_print_field(self.h, str(path).encode()))
 
     def solve_status(self) -> dict:
         """Status of the most recent Poisson solve (iterations, residual, status, levels)."""

@@ -88,3 +88,49 @@ def test_particle_reload_at_creation(m, tmp_path):
                            tmp_path / "r2.txt"), spath)
     a.close()
     b.close()
+
+
+def test_sampled_distributions(m, tmp_path):
+    """dist_sample on the GPU: the energy histogram equals Histogram::add of the
+    particles' energies (the reference's formula in FP64 on the same FP32
+    velocities), rhoAverage of one sample is the charge deposit, uAvg the
+    potential; print_distribution writes the reference's file layouts."""
+    from cases import penning_rz
+
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=20000)
+    pic = m.Pic(cpath, spath, seed=2)
+    e = pic.speclist[0]
+    e.set_particles(*parts)
+    pic.advance_init()
+    pic.advance(10)
+    pic.dist_reset()
+    pic.dist_sample()
+    g = e.particles()
+    info = e.info()
+    mass, emax = info["mass"], info["E_max"]
+    vx, vy, vz = (np.asarray(g[k], dtype=np.float32).astype(np.float64) for k in ("vx", "vy", "vz"))
+    f = (vx * vx + vz * vz + vy * vy) * mass * 0.5 / 1.602189e-19
+    inside = (f < emax) & (f > 0.0)
+    bins = np.zeros(200)
+    np.add.at(bins, np.minimum((f[inside] * 200 / emax).astype(int), 199), 1)
+    d = e.energy_dist()
+    norm = inside.sum() * emax / 200
+    assert d["n_val"] == inside.sum() and d["n_val_tot"] == len(f)
+    assert np.abs(d["values"] * norm - bins).sum() <= 4  # bin-edge ties from FMA contraction at most
+    assert abs(d["mean_tot"] - f.mean()) <= 1e-12 * f.mean()
+    q = info["charge"] * 2.0 ** -40
+    assert np.allclose(e.rho_average, e.rho_fixed() * q, rtol=1e-15, atol=0)
+    u1 = pic.field.u
+    assert np.array_equal(pic.u_average, u1)
+    pic.advance(5)
+    pic.dist_sample()
+    u2 = pic.field.u
+    assert np.allclose(pic.u_average, 0.5 * (u1 + u2), rtol=1e-14, atol=1e-14 * np.abs(u1).max())
+    pic.print_distribution(tmp_path)
+    pic.print_field(tmp_path / "potential.dat")
+    lines = (tmp_path / "ELECTRON_energy_dist.dat").read_text().splitlines()
+    assert len(lines) == 200 and len(lines[0].split("\t")) == 2
+    rho_lines = (tmp_path / "ELECTRON_rho.dat").read_text().split("\n")
+    nx, nz = pic.shape
+    assert sum(1 for line in rho_lines if line.count("\t") == 2) == nx * nz
+    pic.close()
