@@ -36,6 +36,12 @@ int launch_push_batch(const PushArgs* d_args, const unsigned* d_chunk_off, int n
                       bool has_b, int vec, int sm_count, cudaStream_t s);
 int launch_deposit(const PushArgs& a, cudaStream_t s);
 int launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
+// ADVANCE_MULTICOLL step of one species (multicoll.cu); ttd = time to the next
+// collision per slot (FP64); qm = charge / mass
+int launch_multicoll(const PushArgs& a, const CollideArgs& c, double* ttd, double dt, double lifetime, double qm,
+                     cudaStream_t s);
+int launch_init_ttd(double* ttd, const uint32_t* id, int64_t first, int64_t n, double lifetime, uint64_t seed,
+                    uint32_t species, uint64_t step, cudaStream_t s);
 // candidate lists of nitems work items (one block each); max_tables = the
 // largest cross-section table size among them (shared-memory staging)
 int launch_collide_batch(const CollideArgs* d_args, int nitems, int max_tables, cudaStream_t s);

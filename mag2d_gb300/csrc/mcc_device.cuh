@@ -255,11 +255,10 @@ __device__ inline void mcc_stage_pointers(const CollideArgs& a, MccStage& st, do
 // Scatter of one particle against a target drawn from the null-collision
 // rates, when every target species is a Maxwellian background (no particles):
 // the partner velocity is rndv (src/particles.hpp:188-192).  Updates
-// (vx, vy, vz); returns MCC_HIT or MCC_NULL.
-static __device__ __forceinline__ int collide_background(const MccSpecies& m, uint64_t seed, uint32_t species,
-                                                      uint32_t pid, uint64_t step, float& vx, float& vy, float& vz)
+// (vx, vy, vz); returns MCC_HIT or MCC_NULL.  Draws from rs.
+static __device__ __forceinline__ int scatter_background(const MccSpecies& m, Stream& rs, float& vx, float& vy,
+                                                         float& vz)
 {
-    Stream rs(seed, species, pid, TAG_COLLIDE, step);
     const int s = mcc_pick_target(m, rs);
     const float sig = (float)m.t_sigma_v[s];
     const float vr2 = rs.normalf() * sig;
@@ -268,6 +267,14 @@ static __device__ __forceinline__ int collide_background(const MccSpecies& m, ui
     bool pu;
     float pvx, pvy, pvz;
     return mcc_collide(m, s, rs, vx, vy, vz, vr2, vz2, vt2, pu, pvx, pvy, pvz);
+}
+
+// the same with the particle's own stream of the step
+static __device__ __forceinline__ int collide_background(const MccSpecies& m, uint64_t seed, uint32_t species,
+                                                         uint32_t pid, uint64_t step, float& vx, float& vy, float& vz)
+{
+    Stream rs(seed, species, pid, TAG_COLLIDE, step);
+    return scatter_background(m, rs, vx, vy, vz);
 }
 
 // One candidate c of the list: the whole of BaseSpecies::scatter for it.

@@ -66,8 +66,17 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
         sm_count = 1;
     config_path = config;
     p = make_param(KeyValueConfig::from_file(config));
-    if (p.mover != ADVANCE_BORIS)
-        throw Error(-1, "mover ADVANCE_MULTICOLL is not provided by this library (Boris mover only)");
+    if (p.mover == ADVANCE_LEAPFROG)
+        throw Error(-1, "mover ADVANCE_LEAPFROG is not provided by this library (ADVANCE_BORIS, ADVANCE_MULTICOLL)");
+    multicoll = p.mover == ADVANCE_MULTICOLL;
+    if (multicoll) {  // the reference's own conditions (src/particles.cpp:812-823)
+        if (p.coord != CARTESIAN) throw Error(-1, "Species<CYLINDRICAL>: advance method not implemented");
+        if (!p.magnetic_field_const || p.Br != 0.0 || p.Bt != 0.0 || p.Bz != 0.0)
+            throw Error(-1, "Species<CARTESIAN>::advance_multicoll() implemented for zero B only");
+        if (p.selfconsistent || p.geometry != GEO_EMPTY)
+            throw Error(-1, "Species<CARTESIAN>::advance_multicoll() implemented for const extern field only:\n"
+                            "\tset selfconsistent=0 and geometry=EMPTY");
+    }
     if (p.use_source) throw Error(-1, "use_source: particle sources are not provided by this library");
     if (p.u_smooth) throw Error(-1, "u_smooth: potential smoothing is not provided by this library");
     parse_species_conf(species_conf, species_prm, inters);
@@ -533,6 +542,7 @@ void Sim::ensure_capacity(int s, int64_t need)
     grow(S.id);
     S.cand.alloc(cap);
     S.cand_rec.alloc(cap);
+    if (multicoll) grow(S.ttd);
     S.bx.release();  // sort buffers are re-made at the next sort
     S.bz.release();
     S.bvx.release();
@@ -556,7 +566,17 @@ void Sim::add_loaded(int s, int64_t n, int kind, double cx, double cz, double ra
     S.n_slots += n;
     S.next_id += (uint32_t)n;
     upload_slots(s);
+    init_ttd(s, o, n);
     sort_due = true;
+}
+
+// time_to_death = lifetime * rexp of new particles (add_particles_*, src/particles.cpp:697)
+void Sim::init_ttd(int s, int64_t first, int64_t n)
+{
+    if (!multicoll || n <= 0) return;
+    SpeciesState& S = sp[s];
+    launches += launch_init_ttd(S.ttd.p, S.id.p, first, n, S.lifetime, seed, (uint32_t)s, S.niter, stream);
+    MAG_CK(cudaGetLastError());
 }
 
 void Sim::add_single(int s, double x, double z, double vx, double vy, double vz)
@@ -578,6 +598,7 @@ void Sim::add_single(int s, double x, double z, double vx, double vy, double vz)
     S.n_slots += 1;
     S.next_id += 1;
     upload_slots(s);
+    init_ttd(s, o, 1);
     sort_due = true;
 }
 
@@ -749,7 +770,7 @@ CollideArgs Sim::collide_args(int s)
 void Sim::sort_species(int s)
 {
     SpeciesState& S = sp[s];
-    if (S.n_slots == 0) return;
+    if (S.n_slots == 0 || multicoll) return;  // the uniform field has no gather to keep local
     if (!S.bx.p) {
         S.bx.alloc(S.cap);
         S.bz.alloc(S.cap);
@@ -825,6 +846,16 @@ void Sim::step(double* ms)
         PushArgs pa = push_args((int)s, false);
         pa.slot = (int)(S.launches & 1);
         pa.fold_slot = S.launches > 0 ? (int)((S.launches - 1) & 1) : -1;
+        if (multicoll) {  // event-driven mover, collisions inside the kernel
+            const CollideArgs ca = collide_args((int)s);
+            if (ca.any_target_slots)
+                throw Error(-1, "ADVANCE_MULTICOLL: collision partners must be background species (no particles)");
+            launches += launch_multicoll(pa, ca, S.ttd.p, S.prm.dt, S.lifetime, S.prm.charge / S.prm.mass, stream);
+            mark(2);
+            S.launches++;
+            S.niter++;
+            continue;
+        }
         launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, false, push_vec, sm_count, stream);
         mark(2);
         if (coll_mode((int)s) == 2) {
@@ -872,7 +903,7 @@ void Sim::advance_init()
         solve(false, 1, false, false);
     }
     for (size_t s = 0; s < sp.size(); ++s) {
-        if (sp[s].n_slots == 0) continue;
+        if (sp[s].n_slots == 0 || multicoll) continue;  // ADVANCE_MULTICOLL has no leapfrog start
         PushArgs pa = push_args((int)s, true);
         launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, true, push_vec, sm_count, stream);
     }
@@ -1002,6 +1033,7 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     S.n_slots = n;
     S.next_id = (uint32_t)n;
     upload_slots(s);
+    init_ttd(s, 0, n);
     sort_due = true;
 }
 
@@ -1131,6 +1163,16 @@ void Sim::save_species(int s, const std::string& path)
     for (auto* v : {&f.x, &f.z, &f.vx, &f.vy, &f.vz}) v->resize(m);
     f.y.assign(m, 0.0);
     f.ttd.assign(m, 0.0);
+    if (multicoll && n) {  // time_to_death of the live particles, in slot order
+        std::vector<double> t(n);
+        std::vector<uint32_t> hx(n);
+        sp[s].ttd.download(t.data(), n, stream);
+        sp[s].x.download(hx.data(), n, stream);
+        MAG_CK(cudaStreamSynchronize(stream));
+        int64_t q = 0;
+        for (int64_t k = 0; k < n && q < m; ++k)
+            if (hx[k] != kDead) f.ttd[q++] = t[k];
+    }
     f.total = (int32_t)std::max<int64_t>(n, m);
     write_particle_file(path, f);
 }
@@ -1155,6 +1197,10 @@ void Sim::load_species(int s, const std::string& path)
         if (f.z[i] < z0 || f.z[i] > zmax) f.z[i] = (zmax - z0) * uni() + z0;
     }
     set_particles(s, (int64_t)f.x.size(), f.x.data(), f.z.data(), f.vx.data(), f.vy.data(), f.vz.data());
+    if (multicoll && !f.ttd.empty()) {  // the file's time_to_death replaces the drawn one
+        sp[s].ttd.upload(f.ttd.data(), f.ttd.size(), stream);
+        MAG_CK(cudaStreamSynchronize(stream));
+    }
 }
 
 void Sim::get_rho_fixed(int s, int64_t* out)

@@ -88,6 +88,7 @@ struct SpeciesState {
     // device particles (x, z fixed point, see device.hpp) and their sort double buffers
     DevArray<uint32_t> x, z, id, cand;
     DevArray<float4> cand_rec;
+    DevArray<double> ttd;  // time to the next collision (ADVANCE_MULTICOLL), FP64
     DevArray<float> vx, vy, vz;
     DevArray<uint32_t> bx, bz, bid;
     DevArray<float> bvx, bvy, bvz;
@@ -143,6 +144,7 @@ public:
     int sort_interval = 20;
     int push_vec = 2;
     int sm_count = 1;
+    bool multicoll = false;  // mover ADVANCE_MULTICOLL
     int solve_blocks = 0;  // blocks of a cooperative solve (0: not yet chosen)
     uint64_t steps_done = 0;
     bool sort_due = true;
@@ -220,6 +222,7 @@ private:
     void sort_species(int s);
     void refresh_rf_pairs();
     void upload_slots(int s);
+    void init_ttd(int s, int64_t first, int64_t n);
     int coll_mode(int s) const;
     bool any_target_slots(int s) const;
 };

@@ -797,7 +797,8 @@ struct orc_sim {
                 if (s->n_particles() > 0) s->rho.reset();
         }
         for (Species* s : sp) {
-            if (c.coord == 1) boris_cyl(*s);
+            if (c.mover == 1) multicoll(*s);
+            else if (c.coord == 1) boris_cyl(*s);
             else boris_cart(*s);
             boundary(*s);
             s->niter++;
@@ -806,6 +807,39 @@ struct orc_sim {
         for (Species* s : sp)
             if (c.selfconsistent) add_rho(*s);
         iter++;
+    }
+    // Species<CARTESIAN>::advance_multicoll (particles.cpp:812-859): free flight in
+    // the constant external field to time_to_death, scatter, redraw; the rest of
+    // dt in free flight (the reference also counts niter and t here, and again in
+    // Species::advance)
+    void multicoll(Species& s)
+    {
+        const double fx = 0.0, fz = c.extern_field;  // Fields::E of the EMPTY geometry (fields.hpp:126-131)
+        const double qm = s.charge / s.mass;
+        const double dt = s.dt;
+        for (Particle& I : s.p) {
+            if (I.empty) continue;
+            double local_time = 0.;
+            double ttd;
+            while (local_time + I.ttd < dt) {
+                ttd = I.ttd;
+                I.vx += fx * qm * ttd;
+                I.vz += fz * qm * ttd;
+                I.x += (I.vx + 0.5 * fx * qm * ttd) * ttd;
+                I.z += (I.vz + 0.5 * fz * qm * ttd) * ttd;
+                local_time += I.ttd;
+                scatter(s, I);
+                I.ttd = s.lifetime * rnd.rexp();
+            }
+            ttd = dt - local_time;
+            I.vx += fx * qm * ttd;
+            I.vz += fz * qm * ttd;
+            I.x += (I.vx + 0.5 * fx * qm * ttd) * ttd;
+            I.z += (I.vz + 0.5 * fz * qm * ttd) * ttd;
+            I.ttd -= ttd;
+        }
+        s.niter++;
+        s.t += dt;
     }
     void add_rho(Species& s)
     {
@@ -826,7 +860,8 @@ struct orc_sim {
             for (Species* s : sp)
                 if (s->n_particles() > 0) add_rho(*s);
         }
-        for (Species* s : sp) boris_init(*s);
+        if (c.mover != 1)  // ADVANCE_MULTICOLL has no leapfrog start (particles.cpp:805-806)
+            for (Species* s : sp) boris_init(*s);
     }
     // svmax_find (particles.cpp:190-206)
     static double svmax_find(const std::vector<Interaction*>& list, double vmax)

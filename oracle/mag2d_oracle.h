@@ -31,6 +31,7 @@ typedef struct {
     int boundary;         /* 0 FREE, 1 PERIODIC */
     int magnetic_field_const;
     double Br, Bz, Bt;
+    int mover;            /* 0 ADVANCE_BORIS, 1 ADVANCE_MULTICOLL (param.cpp mover) */
 } orc_config;
 
 enum { ORC_ELASTIC = 0, ORC_LANGEVIN = 1, ORC_CX = 2, ORC_COULOMB = 3, ORC_SUPERELASTIC = 4 };

@@ -159,6 +159,9 @@ def gen_steps():
                temperature=10000.0, emax=30.0)]
     run_step_case("empty_superelastic", cfg, sp, inter, 150, [75, 150], 11,
                   initscript="add_particles_on_disk ELECTRON 1500 1e-2 1e-2 1e-3\n")
+    # the same electron swarm under the event-driven ADVANCE_MULTICOLL mover
+    run_step_case("multicoll_eedf", dict(cfg, mover="ADVANCE_MULTICOLL"), sp, inter, 60, [30, 60], 17,
+                  initscript="add_particles_everywhere ELECTRON 1000\n")
     # charge exchange with neutrals and Coulomb collisions between two ion species
     cfg = dict(coord="CARTESIAN", boundary="PERIODIC", geometry="EMPTY", x_max=1e-2, z_max=1e-2, x_sampl=9,
                z_sampl=9, selfconsistent=0, rf=0, extern_field=50.0, do_plot=0)

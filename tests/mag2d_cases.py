@@ -165,7 +165,7 @@ class OrcConfig(ctypes.Structure):
         ("electric_field_from_file", ctypes.c_int), ("rf_amplitude", ctypes.c_double),
         ("rf_omega", ctypes.c_double), ("rf_U0", ctypes.c_double), ("boundary", ctypes.c_int),
         ("magnetic_field_const", ctypes.c_int), ("Br", ctypes.c_double), ("Bz", ctypes.c_double),
-        ("Bt", ctypes.c_double),
+        ("Bt", ctypes.c_double), ("mover", ctypes.c_int),
     ]
 
 
@@ -213,6 +213,7 @@ def orc_config(cfg: dict) -> OrcConfig:
         boundary=1 if c["boundary"] == "PERIODIC" else 0,
         magnetic_field_const=int(float(c["magnetic_field_const"])),
         Br=float(c["Br"]), Bz=float(c["Bz"]), Bt=float(c["Bt"]),
+        mover=1 if str(c.get("mover", "ADVANCE_BORIS")) == "ADVANCE_MULTICOLL" else 0,
     )
 
 

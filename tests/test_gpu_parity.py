@@ -354,3 +354,43 @@ def test_push_variants_bit_identical(m, tmp_path, case):
             assert d[k] == out[0][1][k], (vec, k)
         if r is not None:
             assert np.array_equal(r, out[0][2])
+
+
+def test_multicoll_mover_statistics(m, tmp_path):
+    """ADVANCE_MULTICOLL (event-driven free flight to each collision, FP64 time
+    to the next collision): the number of scatter events within 3 sigma of the
+    oracle's and the energy distributions alike (KS p > 0.01), electrons in He
+    with the reference's cross-section tables in a 1000 V/m field."""
+    import json
+
+    from mag2d_cases import write_config, write_species_conf
+
+    d = np.load(Path(__file__).resolve().parent / "golden" / "step_multicoll_eedf.npz")
+    meta = json.loads(str(d["meta"]))
+    cfg, sp, inter = meta["cfg"], meta["species"], meta["inter"]
+    cpath = write_config(cfg, tmp_path / "c.txt")
+    spath = write_species_conf(sp, inter, tmp_path / "s.txt")
+    n, steps = 20000, 60
+    ini = tmp_path / "init.txt"
+    ini.write_text(f"add_particles_everywhere ELECTRON {n}\n")
+    pic = m.Pic(cpath, spath, ini, seed=4)
+    pic.advance_init()
+    pic.advance(steps)
+    g = pic.speclist[1].particles()
+    dg = pic.speclist[1].diag()
+    port = _port_for(m, cfg, sp, inter, cpath, seed=4)
+    port.run_initscript(ini)
+    port.advance_init()
+    port.advance(steps)
+    o = port.particles(1)
+    events = dg["collisions"] + dg["null_collisions"]
+    ref = port.collisions(1)
+    assert ref > 1000
+    assert abs(events - ref) < 3 * math.sqrt(2 * ref), (events, ref)
+    me = 9.11e-31
+    eg = 0.5 * me * (g["vx"] ** 2 + g["vy"] ** 2 + g["vz"] ** 2) / 1.602189e-19
+    lo = o[o[:, 7] == 0]
+    eo = 0.5 * me * (lo[:, 3] ** 2 + lo[:, 4] ** 2 + lo[:, 5] ** 2) / 1.602189e-19
+    _, p = _ks_2samp(eg, eo)
+    assert p > 0.01, (p, eg.mean(), eo.mean())
+    pic.close()
