@@ -102,6 +102,10 @@ int mag_run_initscript(mag_sim* sim, const char* initscript_path);
 
 /* Pic::advance_init (src/pic.cpp:359-384) */
 int mag_advance_init(mag_sim* sim);
+/* the same; deposit = 0 solves from the species' fixed-point deposits as they
+ * are (set by mag_set_rho_fixed, e.g. summed over the processes of a particle
+ * decomposition) instead of depositing the handle's own particles first */
+int mag_advance_init_ex(mag_sim* sim, int deposit);
 
 /* nsteps calls of Pic::advance (src/pic.cpp:330-358).  Asynchronous: returns
  * once the work is queued; errors found on the device are reported by the
@@ -156,6 +160,17 @@ int mag_diag(mag_sim* sim, int species, mag_diag_out* out);
  * (Field2D::accumulate weights, src/Field2D.hpp:45-62, quantised to 2^-20 per
  * axis).  Reflects the deposit of the last step. */
 int mag_get_rho_fixed(mag_sim* sim, int species, int64_t* host_out);
+
+/* Particle decomposition of one instance over several processes (one GPU
+ * each, every one with the full grid): after each mag_advance(sim, 1) every
+ * process sums the species' fixed-point deposits over all processes (an
+ * integer all-reduce, so the sum is bit-identical in any order) and writes
+ * the total back before the next step's Poisson solve.  mag_rho_fixed_ptr
+ * gives the device array (nx*nz int64, on the handle's stream) for an
+ * in-place device all-reduce; mag_set_rho_fixed writes it from the host.  No
+ * reference counterpart (the reference runs on one core). */
+void* mag_rho_fixed_ptr(mag_sim* sim, int species);
+int mag_set_rho_fixed(mag_sim* sim, int species, const int64_t* host_in);
 
 /* Recompute the fixed-point deposit of the current particles of every species
  * (Species::accumulate, src/particles.hpp:358-367) without moving them. */

@@ -88,10 +88,14 @@ def lib() -> ctypes.CDLL:
     L.mag_destroy.restype = None
     L.mag_run_initscript.argtypes = [P, ctypes.c_char_p]
     L.mag_advance_init.argtypes = [P]
+    L.mag_advance_init_ex.argtypes = [P, ctypes.c_int]
     L.mag_advance.argtypes = [P, ctypes.c_uint64]
     L.mag_sync.argtypes = [P]
     L.mag_advance_timed.argtypes = [P, ctypes.c_uint64, D]
     L.mag_solve_status.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
+    L.mag_rho_fixed_ptr.argtypes = [P, ctypes.c_int]
+    L.mag_rho_fixed_ptr.restype = ctypes.c_void_p
+    L.mag_set_rho_fixed.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
     L.mag_dist_reset.argtypes = [P]
     L.mag_dist_sample.argtypes = [P]
     L.mag_dist_samples.argtypes = [P]

@@ -132,6 +132,15 @@ int mag_advance_init(mag_sim* sim)
     });
 }
 
+int mag_advance_init_ex(mag_sim* sim, int deposit)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        sim->s->advance_init(deposit != 0);
+        return MAG_OK;
+    });
+}
+
 int mag_advance(mag_sim* sim, uint64_t nsteps)
 {
     return guarded([&]() {
@@ -310,6 +319,22 @@ int mag_get_rho_fixed(mag_sim* sim, int species, int64_t* host_out)
     return guarded([&]() {
         check_species(sim, species);
         sim->s->get_rho_fixed(species, host_out);
+        return MAG_OK;
+    });
+}
+
+void* mag_rho_fixed_ptr(mag_sim* sim, int species)
+{
+    if (!sim || !sim->s || species < 0 || species >= (int)sim->s->sp.size()) return nullptr;
+    return sim->s->sp[species].rho.p;
+}
+
+int mag_set_rho_fixed(mag_sim* sim, int species, const int64_t* host_in)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (!host_in) throw mag::Error(MAG_EINVAL, "null input");
+        sim->s->set_rho_fixed(species, host_in);
         return MAG_OK;
     });
 }

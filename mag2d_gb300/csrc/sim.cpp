@@ -895,11 +895,11 @@ void Sim::advance(uint64_t nsteps)
 }
 
 // Pic::advance_init (src/pic.cpp:359-384)
-void Sim::advance_init()
+void Sim::advance_init(bool deposit)
 {
     MAG_CK(cudaSetDevice(device));
     if (p.selfconsistent) {
-        deposit_all();
+        if (deposit) deposit_all();
         solve(false, 1, false, false);
     }
     for (size_t s = 0; s < sp.size(); ++s) {
@@ -1201,6 +1201,13 @@ void Sim::load_species(int s, const std::string& path)
         sp[s].ttd.upload(f.ttd.data(), f.ttd.size(), stream);
         MAG_CK(cudaStreamSynchronize(stream));
     }
+}
+
+void Sim::set_rho_fixed(int s, const int64_t* in)
+{
+    MAG_CK(cudaStreamSynchronize(stream));
+    sp[s].rho.upload((const unsigned long long*)in, (size_t)nx * nz, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
 }
 
 void Sim::get_rho_fixed(int s, int64_t* out)

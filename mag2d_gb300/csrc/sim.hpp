@@ -118,7 +118,7 @@ public:
     ~Sim();
 
     void run_initscript(const std::string& path);
-    void advance_init();
+    void advance_init(bool deposit = true);  // deposit = false: solve from the species deposits as they are
     void advance(uint64_t nsteps);
     void advance_timed(uint64_t nsteps, double* ms4);
     int sync();  // returns first device error code (0 = none)
@@ -158,6 +158,7 @@ public:
                        const double* vz);
     void deposit_all();
     void get_rho_fixed(int s, int64_t* out);
+    void set_rho_fixed(int s, const int64_t* in);
     // sampled distributions (BaseSpecies::dist_sample / dist_reset, Pic::dist_sample)
     void dist_reset();
     void dist_sample();

@@ -1,0 +1,160 @@
+"""Multi-process paths on CPU ranks (gloo, world size 2).
+
+Independent instances split into contiguous shares; the particle
+decomposition of one self-consistent instance sums int64 fixed-point deposits
+over the ranks, which must equal the deposit of all particles in one process
+bit for bit (the local deposits are the oracle's quantised CIC deposit)."""
+from __future__ import annotations
+
+import os
+import socket
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, q):
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from mag2d_cases import deposit_fixed, to_fixed
+        from mag2d_gb300.distributed import allreduce_int64, shard_range
+
+        rng = np.random.default_rng(9)
+        n, nx, nz = 10_001, 33, 65
+        xf = to_fixed(rng.random(n) * (nx - 1))
+        zf = to_fixed(rng.random(n) * (nz - 1))
+        mine = shard_range(n, world, rank)
+        local = deposit_fixed(nx, nz, xf[mine.start:mine.stop], zf[mine.start:mine.stop])
+        total = allreduce_int64(local.reshape(-1)).reshape(nx, nz)
+        # replica timing as bench.py reports it: the maximum over ranks
+        t = torch.tensor([1.0 + rank])
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        q.put((rank, total, float(t), len(mine)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_shard_ranges_partition():
+    from mag2d_gb300.distributed import shard_range
+
+    for n in (0, 1, 7, 256, 1001):
+        for world in (1, 2, 3, 8):
+            got = [shard_range(n, world, r) for r in range(world)]
+            assert sum(len(g) for g in got) == n
+            assert all(a.stop == b.start for a, b in zip(got, got[1:]))
+            assert max(len(g) for g in got) - min(len(g) for g in got) <= 1
+
+
+@pytest.mark.timeout(180)
+def test_deposit_allreduce_equals_single_process(built):
+    import multiprocessing as mp
+
+    from mag2d_cases import deposit_fixed, to_fixed
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = [q.get(timeout=150) for _ in procs]
+    for p in procs:
+        p.join(timeout=30)
+        assert p.exitcode == 0
+    rng = np.random.default_rng(9)
+    n, nx, nz = 10_001, 33, 65
+    xf = to_fixed(rng.random(n) * (nx - 1))
+    zf = to_fixed(rng.random(n) * (nz - 1))
+    full = deposit_fixed(nx, nz, xf, zf)
+    for rank, total, tmax, count in out:
+        assert np.array_equal(total, full), rank
+        assert tmax == 2.0
+    assert sorted(c for _, _, _, c in out) == [5000, 5001]
+    assert full.sum() == n << 40
+
+
+def _gpu_worker(rank, world, port, q, tmp):
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import mag2d_gb300 as m
+        from cases import penning_rz
+        from mag2d_gb300.distributed import ParticleDecomposition, shard_range
+
+        cfg, species, inter, cpath, spath, parts = penning_rz(Path(tmp), n=6000)
+        mine = shard_range(6000, world, rank)
+        pic = m.Pic(cpath, spath, seed=1)
+        pic.speclist[0].set_particles(*(a[mine.start:mine.stop] for a in parts))
+        dec = ParticleDecomposition(pic)
+        dec.advance_init()
+        dec.advance(20)
+        g = pic.speclist[0].particles()
+        q.put((rank, mine.start, g["x"], g["z"], g["vz"], g["id"], pic.field.u))
+        pic.close()
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+@pytest.mark.timeout(300)
+def test_particle_decomposition_equals_single_run(built, tmp_path):
+    """Two processes on one GPU each push half of the electrons and sum their
+    int64 deposits every step: the particles and potential equal those of the
+    single-process run of all electrons bit for bit."""
+    import multiprocessing as mp
+
+    import mag2d_gb300 as m
+    from cases import penning_rz
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_gpu_worker, args=(r, 2, port, q, str(tmp_path / f"r{r}"))) for r in range(2)]
+    for r, p in enumerate(procs):
+        (tmp_path / f"r{r}").mkdir()
+        p.start()
+    out = sorted(q.get(timeout=240) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=6000)
+    pic = m.Pic(cpath, spath, seed=1)
+    pic.speclist[0].set_particles(*parts)
+    pic.advance_init()
+    pic.advance(20)
+    g = pic.speclist[0].particles()
+    order = np.argsort(g["id"])
+    g = {k: v[order] for k, v in g.items()}
+    for rank, start, x, z, vz, ids, u in out:
+        gid = ids.astype(np.int64) + start
+        sel = np.searchsorted(g["id"], gid)
+        assert np.array_equal(g["id"][sel], gid)
+        assert np.array_equal(g["x"][sel], x) and np.array_equal(g["z"][sel], z), rank
+        assert np.array_equal(g["vz"][sel], vz), rank
+        assert np.array_equal(pic.field.u, u), rank
+    pic.close()
