@@ -56,6 +56,9 @@ typedef struct {
     int64_t capacity_hint; /* particle slots to reserve per species (0 = grow as needed) */
     int push_vec;          /* consecutive slots per thread of the particle kernel: 1, 2 or 4 (0 = 2);
                               results do not depend on it */
+    int direct_solve;      /* self-consistent Poisson solves by the precomputed inverse of the operator
+                              (built at the first solve): 0 = for grids up to 20000 nodes, 1 = also
+                              larger ones up to the one-block size, -1 = always multigrid */
 } mag_opts;
 
 typedef struct {

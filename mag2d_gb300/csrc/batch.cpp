@@ -45,6 +45,7 @@ Batch::Batch(const std::vector<BatchInstanceDesc>& desc, const SimOptions& base)
         SimOptions o = base;
         o.seed = desc[i].seed;
         o.stream = stream;
+        o.direct_solve = -1;  // the batch solves every instance with its own kernel
         try {
             sims.emplace_back(new Sim(desc[i].config, desc[i].species_conf, o));
             if (!desc[i].initscript.empty()) sims.back()->run_initscript(desc[i].initscript);

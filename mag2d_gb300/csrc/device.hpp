@@ -26,6 +26,7 @@ constexpr int kMaxSpecies = 16;
 constexpr int kMaxInteractions = 64;
 constexpr int kMaxLevels = 12;
 constexpr long long kSingleBlockNodes = 70000;  // grids (and levels) up to this size run on one block
+constexpr long long kGreenMaxNodes = 20000;     // grids up to this size solve by the precomputed inverse
 constexpr int kFracBits = 20;      // fixed-point fraction of a cell in the positions
 constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis (= kFracBits)
 constexpr uint32_t kFracMask = (1u << kFracBits) - 1u;
@@ -162,6 +163,23 @@ struct SortArgs {
     Counters* cnt;
 };
 
+// Direct solve with the precomputed inverse G (nn x nn, column-major by
+// right-hand-side node); u_vac (nullable) is the stored potential of the
+// Dirichlet values of the solve's voltages; bprime, list_j and list_b hold nn
+// entries, tile_count one per 1024 nodes, part nchunks * nn.
+constexpr int kGreenMaxChunks = 32;
+struct GreenArgs {
+    const double* G;
+    const double* u_vac;
+    double* bprime;
+    int* tile_count;
+    int* list_j;
+    double* list_b;
+    int* count;
+    double* part;
+    int nchunks;
+};
+
 struct SolveStatus {
     int iterations;
     int converged;
@@ -195,7 +213,8 @@ struct SolveArgs {
     double* u;              // FP64 solution (in/out, warm start)
     double* b;              // FP64 right-hand side (scratch)
     int rf_solve;           // boundary_solve_rf: FIXED -> 0, FIXED_RF -> voltage
-    int rho_src;            // 0 none, 1 fixed-point species accumulators, 2 FP64 array
+    int rho_src;            // 0 none, 1 fixed-point species accumulators, 2 FP64 array, 3 unit right-hand side
+    long long unit_node;    // rho_src 3: b = 1 at this node, 0 elsewhere (columns of the inverse)
     const unsigned long long* rho_fixed[kMaxSpecies];
     double rho_weight[kMaxSpecies];  // charge * 2^-40
     int nsp;

@@ -57,6 +57,12 @@ int solve_max_blocks(int sm_count);
 // 'threads' threads each; grids up to kSingleBlockNodes nodes)
 int launch_solve_batch(const SolveArgs* d_args, int n, int threads, cudaStream_t s);
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s);
+// direct solve u = G b' with the precomputed inverse G (nn x nn, column j =
+// response to a unit right-hand side at node j); bprime (nn) and part
+// (nchunks x nn) are scratch; writes the faces when a.Exf is set
+int green_chunks(long long nn, int sm_count);
+// Direct solve with the precomputed inverse (GreenArgs).
+int launch_green_solve(const SolveArgs& a, const GreenArgs& g, cudaStream_t s);
 int launch_load_disk(uint32_t* x, uint32_t* z, float* vx, float* vy, float* vz, uint32_t* id, int64_t n,
                      uint32_t id0, int kind, double cx, double cz, double radius, double zlo, double zhi,
                      double x0, double z0, double dx, double dz, double xmax, double zmax, double vsig,

@@ -113,6 +113,15 @@ __device__ __forceinline__ Stencil5 fine_stencil(const SolveArgs& a, int i)
     const double* t = a.st64 + 4 * i;
     return {t[0], t[1], a.k2, a.k2, t[2], t[3]};
 }
+// the reference's scaling of rho into the right-hand side of row i (fields.cpp:283-300)
+__device__ __forceinline__ double rhs_scale(const SolveArgs& a, int i)
+{
+    if (a.coord == 1)
+        return i > 0 ? -1.0 / kEps0d / (kPi * a.dx * a.dx * 2.0 * i * a.dz) * a.mpf
+                     : -1.0 / kEps0d / (kPi * a.dx * a.dx * 0.25 * a.dz) * a.mpf;
+    return -(a.dx * a.dx) / kEps0d / a.dV;
+}
+
 __device__ __forceinline__ double atomic_max_nonneg(double* p, double v)
 {
     return __longlong_as_double(
@@ -438,13 +447,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
             } else if (a.rho_src == 2) {
                 rho = a.rho64[k];
             }
-            double scale;
-            if (a.coord == 1)
-                scale = i > 0 ? -1.0 / kEps0d / (kPi * a.dx * a.dx * 2.0 * i * a.dz) * a.mpf
-                              : -1.0 / kEps0d / (kPi * a.dx * a.dx * 0.25 * a.dz) * a.mpf;
-            else
-                scale = -(a.dx * a.dx) / kEps0d / a.dV;
-            a.b[k] = rho * scale;
+            a.b[k] = a.rho_src == 3 ? ((long long)k == a.unit_node ? 1.0 : 0.0) : rho * rhs_scale(a, i);
         }
         if (a.clear_rho && a.rho_src == 1)
             for (int s = 0; s < a.nsp; ++s) ((unsigned long long*)a.rho_fixed[s])[k] = 0ull;
@@ -565,6 +568,169 @@ __global__ void __launch_bounds__(1024) k_solve_batch(const SolveArgs* __restric
     solve_body(*reinterpret_cast<const SolveArgs*>(raw), t);
 }
 
+// ---- direct solve with the precomputed inverse ----------------------------
+//
+// For grids small enough to keep G = A_ff^-1 in HBM (column j = the solution
+// for a unit right-hand side at node j, zero Dirichlet values), a solve is
+//   u_f = u_vac,f + sum over j with b'_j != 0 of G[:, j] b'_j
+//   u_d = the Dirichlet values
+// where b' = scale_i rho on free nodes and u_vac = G (- sum over fixed
+// neighbours d of A[f][d] u_d) is the potential of the electrodes alone,
+// computed once (the voltages of an instance do not change).  Without a
+// stored u_vac (other Dirichlet values, e.g. the zero ones of the adjoint
+// solve) b' carries the Dirichlet term itself.
+//
+// The nonzero entries of b' are compacted in node order into a list; the
+// product is split into chunks of equal numbers of list entries whose partial
+// sums are added in chunk order, so the result does not depend on scheduling
+// and the work does not depend on where the charge sits.
+
+constexpr int kGreenTile = 1024;  // nodes per block of the right-hand side and its compaction
+
+__device__ __forceinline__ double green_rhs_node(const SolveArgs& a, long long k, bool dirichlet)
+{
+    const int nx = a.nx, nz = a.nz;
+    const int8_t m = a.mask[k];
+    auto value = [&](long long d) {
+        const int8_t md = a.mask[d];
+        return a.rf_solve ? (md == 1 ? a.voltage[d] : 0.0) : (md == 0 ? a.voltage[d] : 0.0);
+    };
+    double b = 0.0;
+    if (is_fixed(m)) {
+        a.u[k] = value(k);
+    } else {
+        const int i = (int)(k / nz), j = (int)(k - (long long)i * nz);
+        double rho = 0.0;
+        if (a.rho_src == 1) {
+            for (int s = 0; s < a.nsp; ++s) rho += a.rho_weight[s] * (double)a.rho_fixed[s][k];
+        } else if (a.rho_src == 2) {
+            rho = a.rho64[k];
+        }
+        b = rho * rhs_scale(a, i);
+        if (dirichlet) {
+            const Stencil5 st = fine_stencil(a, i);
+            if (i > 0 && is_fixed(a.mask[k - nz])) b -= st.w * value(k - nz);
+            if (i + 1 < nx && is_fixed(a.mask[k + nz])) b -= st.e * value(k + nz);
+            if (j > 0 && is_fixed(a.mask[k - 1])) b -= st.s * value(k - 1);
+            if (j + 1 < nz && is_fixed(a.mask[k + 1])) b -= st.n * value(k + 1);
+        }
+    }
+    if (a.clear_rho && a.rho_src == 1)
+        for (int s = 0; s < a.nsp; ++s) ((unsigned long long*)a.rho_fixed[s])[k] = 0ull;
+    return b;
+}
+
+// b' of every node (one node per thread) and the number of nonzero entries of
+// each tile of kGreenTile nodes
+__global__ void __launch_bounds__(kGreenTile) k_green_rhs(const SolveArgs a, bool dirichlet,
+                                                          double* __restrict__ bprime, int* __restrict__ tile_count)
+{
+    const long long nn = (long long)a.nx * a.nz;
+    const long long k = (long long)blockIdx.x * kGreenTile + threadIdx.x;
+    const double b = k < nn ? green_rhs_node(a, k, dirichlet) : 0.0;
+    if (k < nn) bprime[k] = b;
+    const int c = __syncthreads_count(b != 0.0);
+    if (threadIdx.x == 0) tile_count[blockIdx.x] = c;
+}
+
+// the nonzero entries of b' in node order: block t writes its tile's entries
+// after those of tiles 0..t-1; block 0 also writes the total
+__global__ void __launch_bounds__(kGreenTile) k_green_compact(const double* __restrict__ bprime, long long nn,
+                                                              const int* __restrict__ tile_count, int ntiles,
+                                                              int* __restrict__ list_j, double* __restrict__ list_b,
+                                                              int* __restrict__ count)
+{
+    __shared__ int wcount[kGreenTile / 32];
+    __shared__ int s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        int before = 0, total = 0;
+        for (int t = lane; t < ntiles; t += 32) {
+            const int c = tile_count[t];
+            before += t < (int)blockIdx.x ? c : 0;
+            total += c;
+        }
+        before = __reduce_add_sync(0xffffffffu, before);
+        total = __reduce_add_sync(0xffffffffu, total);
+        if (lane == 0) {
+            s_base = before;
+            if (blockIdx.x == 0) *count = total;
+        }
+    }
+    const long long k = (long long)blockIdx.x * kGreenTile + threadIdx.x;
+    const double b = k < nn ? bprime[k] : 0.0;
+    const unsigned m = __ballot_sync(0xffffffffu, b != 0.0);
+    if (lane == 0) wcount[warp] = __popc(m);
+    __syncthreads();
+    int before = s_base;
+    for (int w = 0; w < warp; ++w) before += wcount[w];
+    if (b != 0.0) {
+        const int pos = before + __popc(m & ((1u << lane) - 1u));
+        list_j[pos] = (int)k;
+        list_b[pos] = b;
+    }
+}
+
+// part[c][i] = sum over the list entries q of chunk c of G[j_q][i] b_q, in
+// list order; chunk c of nchunks holds entries [c L / nchunks, (c+1) L / nchunks).
+__global__ void __launch_bounds__(256) k_green_gemv(const double* __restrict__ G, const int* __restrict__ list_j,
+                                                    const double* __restrict__ list_b, const int* __restrict__ count,
+                                                    long long nn, double* __restrict__ part)
+{
+    __shared__ double sb[256];
+    __shared__ int sj[256];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long L = *count, nch = gridDim.y;
+    const long long q0 = L * blockIdx.y / nch, q1 = L * (blockIdx.y + 1) / nch;
+    const bool row = i < nn;
+    const double* __restrict__ gi = G + (row ? i : 0);
+    double acc = 0.0;
+    for (long long t0 = q0; t0 < q1; t0 += 256) {
+        const int total = (int)min(256LL, q1 - t0);
+        if (threadIdx.x < total) {
+            sj[threadIdx.x] = list_j[t0 + threadIdx.x];
+            sb[threadIdx.x] = list_b[t0 + threadIdx.x];
+        }
+        __syncthreads();
+        if (row) {
+            int q = 0;
+            for (; q + 8 <= total; q += 8) {
+                double g[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) g[r] = __ldcs(gi + (long long)sj[q + r] * nn);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) acc = fma(g[r], sb[q + r], acc);
+            }
+            for (; q < total; ++q) acc = fma(__ldcs(gi + (long long)sj[q] * nn), sb[q], acc);
+        }
+        __syncthreads();
+    }
+    if (row) part[(long long)blockIdx.y * nn + i] = acc;
+}
+
+__global__ void __launch_bounds__(64) k_green_sum(const SolveArgs a, const double* __restrict__ part, int nchunks,
+                                                  const double* __restrict__ u_vac)
+{
+    const long long nn = (long long)a.nx * a.nz;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (long long)gridDim.x * blockDim.x) {
+        if (is_fixed(a.mask[k])) continue;
+        double p[kGreenMaxChunks];
+#pragma unroll
+        for (int c = 0; c < kGreenMaxChunks; ++c) p[c] = c < nchunks ? part[(long long)c * nn + k] : 0.0;
+        double u = u_vac ? u_vac[k] : 0.0;
+#pragma unroll
+        for (int c = 0; c < kGreenMaxChunks; ++c)
+            if (c < nchunks) u += p[c];
+        a.u[k] = u;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.status->iterations = 0;
+        a.status->residual = 0.0;
+        a.status->converged = 1;
+        a.status->aborted = 0;
+    }
+}
+
 __global__ void k_faces(const double* __restrict__ u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf)
 {
     const double idx = 1.0 / dx, idz = 1.0 / dz;
@@ -613,6 +779,27 @@ int launch_solve_batch(const SolveArgs* d_args, int n, int threads, cudaStream_t
     if (n <= 0) return 0;
     k_solve_batch<<<n, threads, 0, s>>>(d_args);
     return 1;
+}
+
+int green_chunks(long long nn, int sm_count)
+{
+    const long long rows = (nn + 255) / 256;
+    return (int)std::max<long long>(1, std::min<long long>(kGreenMaxChunks, (8LL * sm_count + rows - 1) / rows));
+}
+
+int launch_green_solve(const SolveArgs& a, const GreenArgs& g, cudaStream_t s)
+{
+    const long long nn = (long long)a.nx * a.nz;
+    const int ntiles = (int)((nn + kGreenTile - 1) / kGreenTile);
+    k_green_rhs<<<ntiles, kGreenTile, 0, s>>>(a, g.u_vac == nullptr, g.bprime, g.tile_count);
+    k_green_compact<<<ntiles, kGreenTile, 0, s>>>(g.bprime, nn, g.tile_count, ntiles, g.list_j, g.list_b, g.count);
+    k_green_gemv<<<dim3((unsigned)((nn + 255) / 256), (unsigned)g.nchunks), 256, 0, s>>>(g.G, g.list_j, g.list_b,
+                                                                                         g.count, nn, g.part);
+    const unsigned g1 = (unsigned)std::min<long long>((nn + 63) / 64, 152 * 16);
+    k_green_sum<<<g1, 64, 0, s>>>(a, g.part, g.nchunks, g.u_vac);
+    int n = 4;
+    if (a.Exf) n += launch_faces(a.u, a.nx, a.nz, a.dx, a.dz, a.Exf, a.Ezf, s);
+    return n;
 }
 
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s)

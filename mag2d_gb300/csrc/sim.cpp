@@ -62,6 +62,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     poisson_max_iter = opts.poisson_max_iter > 0 ? opts.poisson_max_iter : 200;
     sort_interval = opts.sort_interval == 0 ? 20 : opts.sort_interval;
     push_vec = opts.push_vec == 1 || opts.push_vec == 2 || opts.push_vec == 4 ? opts.push_vec : 2;
+    direct_mode = opts.direct_solve;
     if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sm_count < 1)
         sm_count = 1;
     config_path = config;
@@ -346,8 +347,121 @@ SolveStatus Sim::solve(bool rf_solve, int rho_src, bool clear_rho, bool wait)
     return st;
 }
 
+// Inverse of the Poisson operator for the direct solve: column j is the
+// solution for a unit right-hand side at node j with zero Dirichlet values,
+// computed by batched single-block multigrid solves (chunks of columns at a
+// time).  Only for grids of at most kGreenMaxNodes whose inverse fits in a
+// quarter of the free device memory.
+void Sim::build_green()
+{
+    green_tried = true;
+    const long long nn = (long long)nx * nz;
+    if (nn > kGreenMaxNodes && direct_mode != 1) return;
+    if (nn > kSingleBlockNodes) return;  // columns are single-block solves
+    size_t fr = 0, tot = 0;
+    MAG_CK(cudaMemGetInfo(&fr, &tot));
+    const size_t gbytes = (size_t)nn * nn * sizeof(double);
+    if (gbytes > fr / 4) return;
+    setup_solver();
+    green.alloc((size_t)nn * nn);
+    green.zero(stream);
+    DevArray<double> zeros, bscr;
+    zeros.alloc(nn);
+    zeros.zero(stream);
+    const int C = (int)std::max<long long>(1, std::min<long long>(1024, (256LL << 20) / (nn * 40)));
+    bscr.alloc((size_t)C * nn);
+    std::vector<DevArray<float>> e(lv.nlev), r(lv.nlev), t(lv.nlev);
+    for (int l = 0; l < lv.nlev; ++l) {
+        const size_t n = (size_t)lv.nx[l] * lv.nz[l] * C;
+        e[l].alloc(n);
+        r[l].alloc(n);
+        t[l].alloc(n);
+    }
+    DevArray<SolveStatus> st;
+    st.alloc(C);
+    DevArray<SolveArgs> d_args;
+    d_args.alloc(C);
+    std::vector<SolveArgs> args;
+    std::vector<long long> cols;
+    for (long long k = 0; k < nn; ++k)
+        if (!(mask[k] == 0 || mask[k] == 1)) cols.push_back(k);
+    SolveArgs base = solve_args(false, 3, false);
+    base.voltage = zeros.p;
+    base.Exf = nullptr;
+    base.Ezf = nullptr;
+    base.tol = std::min(poisson_tol, 1e-12);
+    for (size_t c0 = 0; c0 < cols.size(); c0 += C) {
+        const int m = (int)std::min<size_t>(C, cols.size() - c0);
+        args.assign(m, base);
+        for (int c = 0; c < m; ++c) {
+            SolveArgs& a = args[c];
+            a.unit_node = cols[c0 + c];
+            a.u = green.p + cols[c0 + c] * nn;
+            a.b = bscr.p + (size_t)c * nn;
+            for (int l = 0; l < lv.nlev; ++l) {
+                const size_t n = (size_t)lv.nx[l] * lv.nz[l];
+                a.lev[l].e = e[l].p + c * n;
+                a.lev[l].r = r[l].p + c * n;
+                a.lev[l].t = t[l].p + c * n;
+            }
+            a.status = st.p + c;
+        }
+        d_args.upload(args.data(), m, stream);
+        launches += launch_solve_batch(d_args.p, m, 512, stream);
+        std::vector<SolveStatus> hs(m);
+        MAG_CK(cudaMemcpyAsync(hs.data(), st.p, m * sizeof(SolveStatus), cudaMemcpyDeviceToHost, stream));
+        MAG_CK(cudaStreamSynchronize(stream));  // args and scratch are reused by the next chunk
+        for (int c = 0; c < m; ++c)
+            if (!hs[c].converged) {
+                green.release();  // a column that did not converge: keep solving by multigrid
+                return;
+            }
+    }
+    MAG_CK(cudaGetLastError());
+    green_chunks_n = green_chunks(nn, sm_count);
+    green_rhs.alloc(nn);
+    green_b.alloc(nn);
+    green_j.alloc(nn + 1 + (nn + 1023) / 1024);
+    green_part.alloc((size_t)green_chunks_n * nn);
+    green_status.alloc(1);
+    // the potential of the electrodes alone
+    green_vac.alloc(nn);
+    SolveArgs v = solve_args(false, 0, false);
+    v.u = green_vac.p;
+    v.Exf = nullptr;
+    v.Ezf = nullptr;
+    v.status = green_status.p;
+    launches += launch_green_solve(v, green_args(false), stream);
+    MAG_CK(cudaGetLastError());
+}
+
+GreenArgs Sim::green_args(bool vacuum) const
+{
+    GreenArgs g{};
+    g.G = green.p;
+    g.u_vac = vacuum ? green_vac.p : nullptr;
+    const long long nn = (long long)nx * nz;
+    g.bprime = green_rhs.p;
+    g.list_j = green_j.p;
+    g.list_b = green_b.p;
+    g.count = green_j.p + nn;
+    g.tile_count = green_j.p + nn + 1;
+    g.part = green_part.p;
+    g.nchunks = green_chunks_n;
+    return g;
+}
+
 void Sim::run_solve(SolveArgs a)
 {
+    if (a.rho_src != 3 && direct_mode >= 0 && p.selfconsistent && !a.rf_solve) {
+        if (!green_tried) build_green();
+        if (green_ready()) {
+            // the stored electrode potential holds for this instance's own voltages
+            launches += launch_green_solve(a, green_args(a.voltage == d_volt.p), stream);
+            MAG_CK(cudaGetLastError());
+            return;
+        }
+    }
     // grids above kSingleBlockNodes: one block of 1024 threads per SM under a
     // cooperative launch; their coarse levels below that size run on block 0
     int nblocks = 1;

@@ -73,6 +73,7 @@ struct SimOptions {
     int poisson_max_iter = 200;
     int64_t capacity_hint = 0;
     int push_vec = 0;       // slots per thread of the particle kernel: 1, 2 or 4 (0: 2)
+    int direct_solve = 0;   // Poisson by the precomputed inverse: 0 automatic (small grids), 1 forced, -1 never
     cudaStream_t stream = nullptr;  // work on this stream instead of one of its own (not destroyed)
 };
 
@@ -146,6 +147,16 @@ public:
     int sm_count = 1;
     bool multicoll = false;  // mover ADVANCE_MULTICOLL
     int solve_blocks = 0;  // blocks of a cooperative solve (0: not yet chosen)
+    int direct_mode = 0;   // SimOptions::direct_solve
+    // the inverse of the Poisson operator for direct solves (built at the first self-consistent solve)
+    DevArray<double> green, green_vac, green_rhs, green_b, green_part;
+    DevArray<int> green_j;  // compacted right-hand side (node, value), its length and the per-tile counts
+    DevArray<SolveStatus> green_status;
+    int green_chunks_n = 0;
+    GreenArgs green_args(bool vacuum) const;
+    bool green_tried = false;
+    bool green_ready() const { return green.p != nullptr; }
+    void build_green();
     uint64_t steps_done = 0;
     bool sort_due = true;
 

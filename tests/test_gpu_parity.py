@@ -53,14 +53,18 @@ def _match(g, o):
     dict(coord="CARTESIAN", geometry="PROBE", x_max=2e-2, z_max=2e-2, x_sampl=65, z_sampl=65, probe_radius=1e-3),
     dict(coord="CARTESIAN", geometry="EMPTY", x_max=2e-2, z_max=2e-2, x_sampl=50, z_sampl=50, extern_field=300.0),
 ], ids=["penning_endcap", "penning_simple", "penning", "rf22pt", "probe", "empty_sor"])
-def test_poisson_matches_direct_solve(m, tmp_path, geom):
+@pytest.mark.parametrize("direct", [-1, 1], ids=["multigrid", "inverse"])
+def test_poisson_matches_direct_solve(m, tmp_path, geom, direct):
+    """Both solvers of a small grid: the multigrid solve and the product with
+    the precomputed inverse of the operator (whose columns are multigrid
+    solves of unit right-hand sides)."""
     from mag2d_cases import QE, write_config, write_species_conf
 
     cfg = dict(selfconsistent=1, rf=0, do_plot=0, macroparticle_factor=100.0, **geom)
     species = [dict(name="E", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11, temperature=1e4, density=1e13)]
     cpath = write_config(cfg, tmp_path / "c.txt")
     spath = write_species_conf(species, [], tmp_path / "s.txt")
-    pic = m.Pic(cpath, spath, seed=1)
+    pic = m.Pic(cpath, spath, seed=1, direct_solve=direct)
     port = _port_for(m, cfg, species, [], cpath)
     rng = np.random.default_rng(5)
     nx, nz = pic.shape
@@ -71,8 +75,32 @@ def test_poisson_matches_direct_solve(m, tmp_path, geom):
     u_ref = port.solve(rho)
     err = np.abs(u_gpu - u_ref).max() / np.abs(u_ref).max()
     assert info["status"] == 0, info
+    assert (info["iterations"] == 0) == (direct == 1), info  # the inverse takes no iterations
     assert err <= 1e-9, (err, info)
     pic.close()
+
+
+def test_inverse_solve_matches_multigrid_in_a_run(m, tmp_path):
+    """A self-consistent Penning run (sparse charge: most right-hand-side
+    entries zero, so most columns of the inverse are skipped): the potential
+    after every one of 20 steps agrees with the multigrid run within 1e-9
+    relative, and two runs with the inverse are bit-identical."""
+    from cases import penning_segments
+
+    c = penning_segments(tmp_path, n=2000)
+    us = {}
+    for tag, direct in (("mg", -1), ("inv", 1), ("inv2", 1)):
+        pic = m.Pic(c[3], c[4], c[5], seed=3, direct_solve=direct)
+        pic.advance_init()
+        seq = []
+        for _ in range(20):
+            pic.advance(1)
+            seq.append(pic.field.u.copy())
+        us[tag] = np.array(seq)
+        pic.close()
+    scale = np.abs(us["mg"]).max()
+    assert np.abs(us["inv"] - us["mg"]).max() <= 1e-9 * scale
+    assert np.array_equal(us["inv"], us["inv2"])
 
 
 def _direct_solve(A, b):
