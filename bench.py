@@ -53,7 +53,8 @@ def _env_rank():
     return r, w, lr
 
 
-def _config(n_gpus: int, n_ions: int = N_IONS, sort_interval: int = 100, workload: str = "multipole") -> dict:
+def _config(n_gpus: int, n_ions: int = N_IONS, sort_interval: int = 100, workload: str = "multipole",
+            step_len: int = 1) -> dict:
     par = f"replicas x{n_gpus}" if n_gpus > 1 else "single GPU"
     if workload == "penning":
         return {"workload": "penning_rz: Penning trap r-z 65x129 grid (r 0-5 mm, z 0-20 mm), end caps -10 V, ring "
@@ -70,7 +71,10 @@ def _config(n_gpus: int, n_ions: int = N_IONS, sort_interval: int = 100, workloa
     return {"workload": "multipole_xy: 22-pole RF ion trap, 257x257 x-y grid, 1e6 ions (3 amu, 0.1 eV), "
                         "He 1e-2 Pa elastic MCC, dt 2 ns", "grid": [GRID, GRID], "particles_per_gpu": n_ions,
             "species": 2, "l2": "flushed between timed steps (512 MB write, then 256 MB read)",
-            "sort_interval": sort_interval, "parallelism": par}
+            "sort_interval": sort_interval, "parallelism": par,
+            "time_steps_per_step": step_len,
+            "step": f"one advance({step_len}) call: {step_len} PIC time steps of every particle (particles are "
+                    "independent without a self-consistent field, so the steps run fused in one launch)"}
 
 
 # ----------------------------------------------------------------------------
@@ -135,9 +139,9 @@ def run_reference(args) -> None:
     base = cpu_baseline(sample_particles=20_000, sample_steps=50)
     v = base["value"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": N_IONS / v * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": N_IONS * (args.step_len or 1) / v * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": _config(args.gpus), "impl": "reference",
+            "config": _config(args.gpus, step_len=args.step_len or 1), "impl": "reference",
             "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -191,14 +195,14 @@ class ClockSampler:
 
 
 def _load_profile_traffic():
-    """DRAM bytes per particle-step of k_push from the committed ncu summary
-    (dram__bytes_read.sum + dram__bytes_write.sum of one launch on 8e6 ions,
-    divided by the particles; traffic grows in proportion to the particles)."""
-    p = ROOT / "profiles" / "k_push_multipole_xy_8e6.md"
+    """DRAM bytes per particle of one k_push_fused launch (50 steps) from the
+    committed ncu summary (dram__bytes_read.sum + dram__bytes_write.sum of one
+    launch on 1e6 ions, divided by the particles)."""
+    p = ROOT / "profiles" / "k_push_fused_multipole_xy_1e6.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_particle_step:"):
+        if line.startswith("dram_bytes_per_particle_launch:"):
             try:
                 return float(line.split(":", 1)[1])
             except ValueError:
@@ -269,9 +273,10 @@ def run_ours(args) -> None:
             flush.zero_()
             torch.sum(clean, dim=0, out=sink)
 
+    L = args.step_len
     for _ in range(args.warmup):
         flush_l2()
-        pic.advance(1)
+        pic.advance(L)
     pic.sync()
     d0 = ion.diag()
     launches0 = pic.kernel_launches
@@ -284,7 +289,7 @@ def run_ours(args) -> None:
         for k in range(args.steps):
             flush_l2()
             starts[k].record(stream)
-            pic.advance(1)
+            pic.advance(L)
             ends[k].record(stream)
         torch.cuda.synchronize()
     if world > 1:
@@ -296,15 +301,16 @@ def run_ours(args) -> None:
     psteps = d1["particle_steps"] - d0["particle_steps"]
 
     # per-kernel device time (events between the kernels of each step), L2 flushed
+    # (one particle launch per call: L steps fused, or a single step)
     kern = np.zeros(4)
     nk = max(3, min(args.steps, 20))
     for _ in range(nk):
         flush_l2()
-        kern += np.array(pic.advance_timed(1))
-    push_ms = kern[2] / nk
+        kern += np.array(pic.advance_timed(L))
+    push_ms = kern[2] / nk  # per particle launch
     live_now = ion.diag()["n_live"]
     bytes_ps = 40 if args.workload == "penning" else BYTES_PER_PARTICLE_STEP  # no id read without collisions
-    alg_bytes = bytes_ps * live_now
+    alg_bytes = bytes_ps * live_now * L
     achieved = alg_bytes / (push_ms * 1e-3) / 1e9
 
     # e2e through the C ABI with host buffers: upload the state from host arrays,
@@ -349,7 +355,7 @@ def run_ours(args) -> None:
             "metric": METRIC, "value": psteps_all / total_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": _config(world, args.particles, args.sort_interval, args.workload),
+            "config": _config(world, args.particles, args.sort_interval, args.workload, L),
             "clocks": clk.summary(),
             "e2e": {"value": e2e_all, "unit": UNIT, "h2d_bytes_per_step": int(5 * 8 * n_host / e2e_chunk),
                     "d2h_bytes_per_step": int(64 / e2e_chunk) + 1,
@@ -358,14 +364,16 @@ def run_ours(args) -> None:
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": (traffic_ps * live_now) if traffic_ps else None,
-                         "traffic_source": "profiles/k_push_multipole_xy_8e6.md, scaled to the live ions",
-                         "kernel": ("k_push<0,2,0,2> (gather + Boris + collision test + boundary)"
+                         "traffic_source": "profiles/k_push_fused_multipole_xy_1e6.md, scaled to the live ions",
+                         "kernel": (f"k_push_fused<0,2,0> ({L} steps per launch: gather + Boris + collision test "
+                                    "+ background scatter + boundary)"
                                     if args.workload == "multipole" else
                                     "k_push<1,1,1,2> (cylindrical gather + Boris + r map + boundary + deposit)"),
                          "alg_bytes_per_launch": alg_bytes, "kernel_ms": push_ms,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured" if peaks else "fallback"},
-            "kernel_ms_per_step": {"sort": kern[0] / nk, "solve": kern[1] / nk, "particles": kern[2] / nk,
-                                   "collide": kern[3] / nk},
+            "kernel_ms_per_step": {"sort": kern[0] / nk / L, "solve": kern[1] / nk / L,
+                                   "particles": kern[2] / nk / L, "collide": kern[3] / nk / L,
+                                   "per": "PIC time step"},
         }
         if args.workload == "penning_large":
             line["poisson_last_solve"] = pic.solve_status()
@@ -537,10 +545,15 @@ def main():
                          "1e8 electrons, B 0.5 T, nu 1e6/s; batched: 256 Penning instances")
     ap.add_argument("--push-vec", type=int, default=0, help="slots per thread of the particle kernel (0: library default)")
     ap.add_argument("--sort-interval", type=int, default=100, help="steps between particle sorts (0: library default, 20)")
+    ap.add_argument("--step-len", type=int, default=None,
+                    help="PIC time steps per timed step (one advance() call); default 50 for the multipole "
+                         "workload, 1 for the self-consistent ones")
     args = ap.parse_args()
     if args.particles is None:
         args.particles = {"penning_large": 100_000_000, "adjoint": 100_000, "penning": 100_000}.get(args.workload,
                                                                                                    N_IONS)
+    if args.step_len is None:
+        args.step_len = 50 if args.workload == "multipole" else 1
     if args.workload == "penning_large":
         if args.sort_interval == 100:
             args.sort_interval = 20

@@ -59,6 +59,10 @@ typedef struct {
     int direct_solve;      /* self-consistent Poisson solves by the precomputed inverse of the operator
                               (built at the first solve): 0 = for grids up to 20000 nodes, 1 = also
                               larger ones up to the one-block size, -1 = always multigrid */
+    int max_fused_steps;   /* where particles are independent over several steps (no self-consistent
+                              field, collision targets without particles), up to this many steps run
+                              as one particle launch, with results identical to single steps
+                              (0 = 64, 1 = never) */
 } mag_opts;
 
 typedef struct {
@@ -119,7 +123,8 @@ int mag_advance(mag_sim* sim, uint64_t nsteps);
  * kernels of every step; ms_out[0..3] receive the summed device time of the
  * particle sort (every sort_interval steps), the Poisson solve, the particle
  * kernels and the collision kernels (timed after all particle kernels, so
- * without their overlap).  Synchronises. */
+ * without their overlap).  Fused steps (mag_opts.max_fused_steps) count their
+ * launch, collisions included, as particle time.  Synchronises. */
 int mag_advance_timed(mag_sim* sim, uint64_t nsteps, double* ms_out);
 
 /* Wait for queued work and report any device-side error flag. */

@@ -100,6 +100,7 @@ int mag_create(const char* config_path, const char* species_conf_path, const cha
             o.capacity_hint = opts->capacity_hint;
             o.push_vec = opts->push_vec;
             o.direct_solve = opts->direct_solve;
+            o.max_fused_steps = opts->max_fused_steps;
         }
         auto h = std::make_unique<mag_sim>();
         h->s = std::unique_ptr<mag::Sim, SimRelease>(new mag::Sim(config_path, species_conf_path, o), SimRelease{true});

@@ -163,6 +163,20 @@ struct SortArgs {
     Counters* cnt;
 };
 
+// Box and cell sizes for converting physical positions to fixed point.
+struct SetParticlesGeom {
+    double x0, xmax, z0, zmax, dx, dz;
+};
+
+// Steps of one fused particle launch: their number and the RF factor of each
+// (rf_amplitude cos(...) + rf_U0 at the species' step counter + k).
+constexpr int kMaxFusedSteps = 64;
+struct FusedSteps {
+    float phase[kMaxFusedSteps];
+    int nsteps;
+    int pad;
+};
+
 // Direct solve with the precomputed inverse G (nn x nn, column-major by
 // right-hand-side node); u_vac (nullable) is the stored potential of the
 // Dirichlet values of the solve's voltages; bprime, list_j and list_b hold nn

@@ -34,6 +34,10 @@ int launch_adj_seed(const uint32_t* x, const float* vz, int64_t n, double coef, 
                     float* lvy, float* lvz, cudaStream_t s);
 int launch_push_batch(const PushArgs* d_args, const unsigned* d_chunk_off, int nitems, int coord, int emode,
                       bool has_b, int vec, int sm_count, cudaStream_t s);
+// fs.nsteps steps of one species in one launch (k_push_fused); c supplies the
+// species' collision data when its collision test is on
+int launch_push_fused(const PushArgs& a, const CollideArgs& c, const FusedSteps& fs, int coord, int sm_count,
+                      cudaStream_t s);
 int launch_deposit(const PushArgs& a, cudaStream_t s);
 int launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
 // ADVANCE_MULTICOLL step of one species (multicoll.cu); ttd = time to the next
@@ -69,6 +73,9 @@ int launch_load_disk(uint32_t* x, uint32_t* z, float* vx, float* vy, float* vz, 
                      uint64_t seed, uint32_t species, int coord, cudaStream_t s);
 int launch_interleave(const float* a, const float* b, float2* out, long long n, cudaStream_t s);
 int launch_fill_u32(uint32_t* p, uint32_t v0, int64_t n, cudaStream_t s);
+// staged = x, z, vx, vy, vz of n particles (FP64, one array after the other)
+int launch_set_particles(const double* staged, int64_t n, const SetParticlesGeom& g, uint32_t* x, uint32_t* z,
+                         float* vx, float* vy, float* vz, uint32_t* id, cudaStream_t s);
 int launch_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n,
                   double* out_sum_v2, unsigned long long* out_n, cudaStream_t s);
 // energy histogram of the live particles (Histogram::add), bins += counts,

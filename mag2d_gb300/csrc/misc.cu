@@ -100,6 +100,26 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t v0, int64_t n)
         p[k] = v0 + (uint32_t)k;
 }
 
+// Host particle arrays (FP64, staged in device memory) to the SoA state:
+// fixed-point positions llrint((x - x0) / dx * 2^20) (outside the box: removed),
+// FP32 velocities, ids 0..n-1
+__global__ void k_set_particles(const double* __restrict__ in, int64_t n, SetParticlesGeom g, uint32_t* __restrict__ x,
+                                uint32_t* __restrict__ z, float* __restrict__ vx, float* __restrict__ vy,
+                                float* __restrict__ vz, uint32_t* __restrict__ id)
+{
+    const double one = (double)(1u << kFracBits);
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const double px = in[k], pz = in[n + k];
+        const bool inside = px >= g.x0 && px <= g.xmax && pz >= g.z0 && pz <= g.zmax;
+        x[k] = inside ? (uint32_t)__double2ll_rn(__dmul_rn(__ddiv_rn(__dsub_rn(px, g.x0), g.dx), one)) : kDead;
+        z[k] = inside ? (uint32_t)__double2ll_rn(__dmul_rn(__ddiv_rn(__dsub_rn(pz, g.z0), g.dz), one)) : 0u;
+        vx[k] = (float)in[2 * n + k];
+        vy[k] = (float)in[3 * n + k];
+        vz[k] = (float)in[4 * n + k];
+        id[k] = (uint32_t)k;
+    }
+}
+
 // sum of v^2 over live particles (FP64) and their count: per-thread partial
 // sums, a block reduction in shared memory, one atomic per block
 __global__ void __launch_bounds__(256) k_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz,
@@ -242,6 +262,15 @@ int launch_fill_u32(uint32_t* p, uint32_t v0, int64_t n, cudaStream_t s)
 {
     if (n == 0) return 0;
     k_fill_u32<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(p, v0, n);
+    return 1;
+}
+
+int launch_set_particles(const double* staged, int64_t n, const SetParticlesGeom& g, uint32_t* x, uint32_t* z,
+                         float* vx, float* vy, float* vz, uint32_t* id, cudaStream_t s)
+{
+    if (n == 0) return 0;
+    k_set_particles<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(staged, n, g, x, z, vx, vy,
+                                                                                          vz, id);
     return 1;
 }
 

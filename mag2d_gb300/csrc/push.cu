@@ -19,6 +19,7 @@
 
 #include "device.hpp"
 #include "kernels.hpp"
+#include "mcc_device.cuh"
 #include "philox.hpp"
 
 namespace mag {
@@ -177,14 +178,16 @@ __device__ __forceinline__ int to_fixed_disp(float c)
 
 // One particle of the step, in registers.  Returns alive (false: removed at
 // the boundary or in a closed cell) and cand (the collision test fired).
+// step: the species' step counter; phase: the RF factor of that step.
 template <int COORD, int EMODE, bool BFIELD>
 __device__ __forceinline__ void step_particle(const PushArgs& a, uint32_t& x, uint32_t& z, float& vx, float& vy,
-                                              float& vz, uint32_t id, bool& alive, bool& cand)
+                                              float& vz, uint32_t id, uint64_t step, float phase, bool& alive,
+                                              bool& cand)
 {
     // the test uses only (seed, species, id, step): computed first, off the dependency chain
-    cand = a.coll_threshold != 0u && collision_test_u32(a.seed, a.species, id, a.step) < a.coll_threshold;
+    cand = a.coll_threshold != 0u && collision_test_u32(a.seed, a.species, id, step) < a.coll_threshold;
     float ex, ez;
-    gather_E<EMODE>(a, x, z, a.phase, ex, ez);
+    gather_E<EMODE>(a, x, z, phase, ex, ez);
     // half acceleration, Boris rotation (Birdsall & Langdon), half acceleration
     vx = fmaf(ex, a.hq, vx);
     vz = fmaf(ez, a.hq, vz);
@@ -358,7 +361,7 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
             if (!act || k >= n || x == kDead) continue;
             bool al;
             step_particle<COORD, EMODE, BFIELD>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j), V::at(VZ, j),
-                                                V::at(ID, j), al, cand[j]);
+                                                V::at(ID, j), a.step, a.phase, al, cand[j]);
             if (!al) x = kDead;
             live += al;
             removed += !al;
@@ -382,6 +385,92 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
     if ((threadIdx.x & 31) == 0) {
         if (live) atomicAdd(&a.cnt->live_par[a.slot], (unsigned long long)live);
         if (removed) atomicAdd(&a.cnt->removed, (unsigned long long)removed);
+    }
+}
+
+// Several steps of one species in one launch, for runs whose particles do not
+// interact within those steps: no self-consistent field (the field is the
+// static plus RF one, or the uniform external one), no sort in between, and
+// collision targets that are Maxwellian backgrounds only.  Every particle is
+// then independent of the others, and its state stays in registers for all
+// steps: step k is step_particle with the species' step counter step0 + k and
+// that step's RF factor, and a fired collision test is scattered at once with
+// the same random stream k_collide would use (collide_background), so the
+// result is bit-identical to the same steps launched one by one.
+__device__ __noinline__ int fused_scatter(const MccSpecies& m, uint64_t seed, uint32_t species, uint32_t id,
+                                          uint64_t step, float* v)
+{
+    float vx = v[0], vy = v[1], vz = v[2];
+    const int r = collide_background(m, seed, species, id, step, vx, vy, vz);
+    if (r == MCC_HIT) {
+        v[0] = vx;
+        v[1] = vy;
+        v[2] = vz;
+    }
+    return r;
+}
+
+template <int COORD, int EMODE, bool BFIELD>
+__global__ void __launch_bounds__(256, 3) k_push_fused(const __grid_constant__ PushArgs a,
+                                                    const __grid_constant__ CollideArgs c,
+                                                    const __grid_constant__ FusedSteps fs)
+{
+    __shared__ MccStage st;
+    extern __shared__ double s_tab[];
+    const bool coll = a.coll_threshold != 0u;
+    if (coll) {
+        double* tab = c.n_tables <= kStageTables ? s_tab : nullptr;
+        mcc_stage(c, st, tab);
+        __syncthreads();
+        if (threadIdx.x == 0) mcc_stage_pointers(c, st, tab);
+    }
+    __syncthreads();
+    if (a.fold_slot >= 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+        Counters* cn = a.cnt;
+        cn->live_sum += cn->live_par[a.fold_slot];
+        cn->live_par[a.fold_slot] = 0;
+        cn->ncand_par[a.fold_slot] = 0;
+    }
+    const int K = fs.nsteps;
+    unsigned live = 0, removed = 0, ncoll = 0, nnull = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t x = __ldcs(a.x + k);
+        if (x == kDead) continue;
+        uint32_t z = __ldcs(a.z + k);
+        float v[3] = {__ldcs(a.vx + k), __ldcs(a.vy + k), __ldcs(a.vz + k)};
+        const uint32_t id = coll ? __ldcs(a.id + k) : 0u;
+#pragma unroll 1
+        for (int q = 0; q < K; ++q) {
+            bool al, cand;
+            step_particle<COORD, EMODE, BFIELD>(a, x, z, v[0], v[1], v[2], id, a.step + q, fs.phase[q], al, cand);
+            if (!al) {
+                x = kDead;
+                ++removed;
+                break;
+            }
+            ++live;
+            if (cand) {
+                const int r = fused_scatter(st.m, a.seed, a.species, id, a.step + q, v);
+                ncoll += r == MCC_HIT;
+                nnull += r != MCC_HIT;
+            }
+        }
+        __stcs(a.x + k, x);
+        __stcs(a.z + k, z);
+        __stcs(a.vx + k, v[0]);
+        __stcs(a.vy + k, v[1]);
+        __stcs(a.vz + k, v[2]);
+    }
+    const unsigned full = 0xffffffffu;
+    live = __reduce_add_sync(full, live);
+    removed = __reduce_add_sync(full, removed);
+    ncoll = __reduce_add_sync(full, ncoll);
+    nnull = __reduce_add_sync(full, nnull);
+    if ((threadIdx.x & 31) == 0) {
+        if (live) atomicAdd(&a.cnt->live_par[a.slot], (unsigned long long)live);
+        if (removed) atomicAdd(&a.cnt->removed, (unsigned long long)removed);
+        if (ncoll) atomicAdd(&a.cnt->ncoll, (unsigned long long)ncoll);
+        if (nnull) atomicAdd(&a.cnt->nnull, (unsigned long long)nnull);
     }
 }
 
@@ -459,7 +548,7 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>())
                 if (!act || k >= n || x == kDead) continue;
                 bool al;
                 step_particle<COORD, EMODE, BFIELD>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j), V::at(VZ, j),
-                                                    V::at(ID, j), al, cand[j]);
+                                                    V::at(ID, j), a.step, a.phase, al, cand[j]);
                 if (!al) x = kDead;
                 live += al;
                 removed += !al;
@@ -582,6 +671,43 @@ void launch_push_t(const PushArgs& a, bool init, int vec, int sm_count, cudaStre
     case 0: launch_push_e<COORD, 0>(a, init, vec, sm_count, s); break;
     case 1: launch_push_e<COORD, 1>(a, init, vec, sm_count, s); break;
     default: launch_push_e<COORD, 2>(a, init, vec, sm_count, s); break;
+    }
+}
+
+template <int COORD, int EMODE, bool BFIELD>
+void launch_fused_t(const PushArgs& a, const CollideArgs& c, const FusedSteps& fs, int sm_count, cudaStream_t s)
+{
+    static int per_sm = 0;
+    const size_t smem = a.coll_threshold != 0u && c.n_tables <= kStageTables ? (size_t)c.n_tables * sizeof(double) : 0;
+    if (per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_push_fused<COORD, EMODE, BFIELD>, 256,
+                                                          kStageTables * sizeof(double)) != cudaSuccess ||
+            b < 1)
+            b = 1;
+        per_sm = b;
+    }
+    const int64_t needed = (a.n + 255) / 256;
+    const int64_t resident = (int64_t)per_sm * std::max(sm_count, 1);
+    const int64_t iters = (needed + resident - 1) / resident;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, (needed + iters - 1) / iters);
+    k_push_fused<COORD, EMODE, BFIELD><<<grid, 256, smem, s>>>(a, c, fs);
+}
+
+template <int COORD, int EMODE>
+void launch_fused_e(const PushArgs& a, const CollideArgs& c, const FusedSteps& fs, int sm_count, cudaStream_t s)
+{
+    if (a.has_b) launch_fused_t<COORD, EMODE, true>(a, c, fs, sm_count, s);
+    else launch_fused_t<COORD, EMODE, false>(a, c, fs, sm_count, s);
+}
+
+template <int COORD>
+void launch_fused_c(const PushArgs& a, const CollideArgs& c, const FusedSteps& fs, int sm_count, cudaStream_t s)
+{
+    switch (a.emode) {
+    case 0: launch_fused_e<COORD, 0>(a, c, fs, sm_count, s); break;
+    case 1: launch_fused_e<COORD, 1>(a, c, fs, sm_count, s); break;
+    default: launch_fused_e<COORD, 2>(a, c, fs, sm_count, s); break;
     }
 }
 
@@ -838,6 +964,15 @@ int launch_push(const PushArgs& a, int coord, bool init, int vec, int sm_count, 
     if (a.n == 0) return 0;
     if (coord == 1) launch_push_t<1>(a, init, vec, sm_count, s);
     else launch_push_t<0>(a, init, vec, sm_count, s);
+    return 1;
+}
+
+int launch_push_fused(const PushArgs& a, const CollideArgs& c, const FusedSteps& fs, int coord, int sm_count,
+                      cudaStream_t s)
+{
+    if (a.n == 0 || fs.nsteps <= 0) return 0;
+    if (coord == 1) launch_fused_c<1>(a, c, fs, sm_count, s);
+    else launch_fused_c<0>(a, c, fs, sm_count, s);
     return 1;
 }
 

@@ -63,6 +63,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     sort_interval = opts.sort_interval == 0 ? 20 : opts.sort_interval;
     push_vec = opts.push_vec == 1 || opts.push_vec == 2 || opts.push_vec == 4 ? opts.push_vec : 2;
     direct_mode = opts.direct_solve;
+    max_fused = opts.max_fused_steps <= 0 ? kMaxFusedSteps : std::min(opts.max_fused_steps, kMaxFusedSteps);
     if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sm_count < 1)
         sm_count = 1;
     config_path = config;
@@ -791,13 +792,7 @@ PushArgs Sim::push_args(int s, bool init)
     a.Ezf2 = Ezf2.p;
     a.extern_ez = (float)p.extern_field;
     a.step = S.niter;
-    {  // Fields::E phase at t = niter * dt, in FP64 as the reference (fields.hpp:135-145)
-        const double t = (double)S.niter * S.prm.dt;
-        double ph = p.rf_omega * t;
-        const double y = 10000000 * kPi;
-        if (!(ph >= 0.0 && ph <= y)) ph = ph - y * (double)(int)(ph / y) + (ph < 0 ? y : 0);
-        a.phase = (float)(p.rf_amplitude * std::cos(ph) + p.rf_U0);
-    }
+    a.phase = rf_factor(S.niter, S.prm.dt);
     const double q = S.prm.charge, m = S.prm.mass, dt = S.prm.dt;
     const double rot = init ? -0.5 * q * dt / (2.0 * m) : q * dt / (2.0 * m);
     a.q_dt_2m = (float)rot;
@@ -837,6 +832,16 @@ PushArgs Sim::push_args(int s, bool init)
     a.slot = 0;
     a.fold_slot = -1;
     return a;
+}
+
+// Fields::E phase at t = niter * dt, in FP64 as the reference (fields.hpp:135-145)
+float Sim::rf_factor(uint64_t niter, double dt) const
+{
+    const double t = (double)niter * dt;
+    double ph = p.rf_omega * t;
+    const double y = 10000000 * kPi;
+    if (!(ph >= 0.0 && ph <= y)) ph = ph - y * (double)(int)(ph / y) + (ph < 0 ? y : 0);
+    return (float)(p.rf_amplitude * std::cos(ph) + p.rf_U0);
 }
 
 // 0: no collisions; 2: the particle kernel lists candidates, k_collide runs them
@@ -994,17 +999,86 @@ void Sim::step(double* ms)
     }
 }
 
+// Particles are independent over the next steps when nothing couples them:
+// no self-consistent field, the per-step mover (not ADVANCE_MULTICOLL) and
+// collision targets without particles.  The block ends before the next sort.
+int Sim::fused_steps(uint64_t left) const
+{
+    if (max_fused <= 1 || left <= 1 || p.selfconsistent || multicoll) return 1;
+    for (size_t s = 0; s < sp.size(); ++s)
+        if (sp[s].n_slots > 0 && coll_mode((int)s) != 0 && any_target_slots((int)s)) return 1;
+    uint64_t k = std::min<uint64_t>(left, (uint64_t)max_fused);
+    if (sort_interval > 0) k = std::min<uint64_t>(k, (uint64_t)sort_interval - steps_done % (uint64_t)sort_interval);
+    return (int)std::max<uint64_t>(k, 1);
+}
+
+// nsteps steps of every species as one launch per species (k_push_fused);
+// the same sort, counters and step counters as nsteps calls of step()
+void Sim::fused_block(int nsteps, double* ms)
+{
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    if (ms)
+        for (auto& e : ev) {
+            MAG_CK(cudaEventCreate(&e));
+        }
+    if (ms) MAG_CK(cudaEventRecord(ev[0], stream));
+    if (sort_interval > 0 && (sort_due || steps_done % (uint64_t)sort_interval == 0)) {
+        for (size_t s = 0; s < sp.size(); ++s) sort_species((int)s);
+        sort_due = false;
+    }
+    if (ms) MAG_CK(cudaEventRecord(ev[1], stream));
+    steps_done += (uint64_t)nsteps;
+    rho_override = false;
+    for (size_t s = 0; s < sp.size(); ++s) {
+        SpeciesState& S = sp[s];
+        if (S.n_slots == 0) {
+            S.niter += (uint64_t)nsteps;
+            continue;
+        }
+        PushArgs pa = push_args((int)s, false);
+        pa.slot = (int)(S.launches & 1);
+        pa.fold_slot = S.launches > 0 ? (int)((S.launches - 1) & 1) : -1;
+        const CollideArgs ca = coll_mode((int)s) == 2 ? collide_args((int)s) : CollideArgs{};
+        FusedSteps fs{};
+        fs.nsteps = nsteps;
+        for (int q = 0; q < nsteps; ++q) fs.phase[q] = rf_factor(S.niter + (uint64_t)q, S.prm.dt);
+        launches += launch_push_fused(pa, ca, fs, p.coord == CYLINDRICAL ? 1 : 0, sm_count, stream);
+        S.launches++;
+        S.niter += (uint64_t)nsteps;
+    }
+    if (ms) {
+        MAG_CK(cudaEventRecord(ev[2], stream));
+        MAG_CK(cudaEventSynchronize(ev[2]));
+        float t0 = 0.f, t1 = 0.f;
+        MAG_CK(cudaEventElapsedTime(&t0, ev[0], ev[1]));
+        MAG_CK(cudaEventElapsedTime(&t1, ev[1], ev[2]));
+        ms[0] += t0;
+        ms[2] += t1;
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+}
+
 void Sim::advance_timed(uint64_t nsteps, double* ms4)
 {
     MAG_CK(cudaSetDevice(device));
     for (int k = 0; k < 4; ++k) ms4[k] = 0.0;
-    for (uint64_t k = 0; k < nsteps; ++k) step(ms4);
+    for (uint64_t left = nsteps; left > 0;) {
+        const int k = fused_steps(left);
+        if (k > 1) fused_block(k, ms4);
+        else step(ms4);
+        left -= (uint64_t)k;
+    }
 }
 
 void Sim::advance(uint64_t nsteps)
 {
     MAG_CK(cudaSetDevice(device));
-    for (uint64_t k = 0; k < nsteps; ++k) step();
+    for (uint64_t left = nsteps; left > 0;) {
+        const int k = fused_steps(left);
+        if (k > 1) fused_block(k);
+        else step();
+        left -= (uint64_t)k;
+    }
     MAG_CK(cudaGetLastError());
 }
 
@@ -1123,27 +1197,17 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
                         const double* vz)
 {
     SpeciesState& S = sp[s];
-    MAG_CK(cudaStreamSynchronize(stream));
     S.n_slots = 0;
     ensure_capacity(s, std::max<int64_t>(n, 1));
-    std::vector<uint32_t> hx(n), hz(n);
-    std::vector<float> hvx(n), hvy(n), hvz(n);
-    const double one = (double)(1u << kFracBits);
-    for (int64_t k = 0; k < n; ++k) {
-        const bool inside = x[k] >= x0 && x[k] <= xmax && z[k] >= z0 && z[k] <= zmax;
-        hx[k] = inside ? (uint32_t)std::llrint((x[k] - x0) / dx * one) : kDead;
-        hz[k] = inside ? (uint32_t)std::llrint((z[k] - z0) / dz * one) : 0u;
-        hvx[k] = (float)vx[k];
-        hvy[k] = (float)vy[k];
-        hvz[k] = (float)vz[k];
-    }
-    S.x.upload(hx.data(), n, stream);
-    S.z.upload(hz.data(), n, stream);
-    S.vx.upload(hvx.data(), n, stream);
-    S.vy.upload(hvy.data(), n, stream);
-    S.vz.upload(hvz.data(), n, stream);
-    launches += launch_fill_u32(S.id.p, 0, n, stream);
-    MAG_CK(cudaStreamSynchronize(stream));
+    // the FP64 arrays go to a device staging buffer as they are; the
+    // conversion to the fixed-point SoA runs on the device
+    if (stage64.n < (size_t)(5 * n)) stage64.alloc((size_t)(5 * n));
+    const double* src[5] = {x, z, vx, vy, vz};
+    for (int c = 0; c < 5; ++c)
+        if (n) MAG_CK(cudaMemcpyAsync(stage64.p + (size_t)c * n, src[c], (size_t)n * sizeof(double),
+                                      cudaMemcpyHostToDevice, stream));
+    const SetParticlesGeom g{x0, xmax, z0, zmax, dx, dz};
+    launches += launch_set_particles(stage64.p, n, g, S.x.p, S.z.p, S.vx.p, S.vy.p, S.vz.p, S.id.p, stream);
     S.n_slots = n;
     S.next_id = (uint32_t)n;
     upload_slots(s);

@@ -74,6 +74,7 @@ struct SimOptions {
     int64_t capacity_hint = 0;
     int push_vec = 0;       // slots per thread of the particle kernel: 1, 2 or 4 (0: 2)
     int direct_solve = 0;   // Poisson by the precomputed inverse: 0 automatic (small grids), 1 forced, -1 never
+    int max_fused_steps = 0;  // steps per fused particle launch where particles are independent (0: 64, 1: none)
     cudaStream_t stream = nullptr;  // work on this stream instead of one of its own (not destroyed)
 };
 
@@ -148,7 +149,9 @@ public:
     bool multicoll = false;  // mover ADVANCE_MULTICOLL
     int solve_blocks = 0;  // blocks of a cooperative solve (0: not yet chosen)
     int direct_mode = 0;   // SimOptions::direct_solve
+    int max_fused = kMaxFusedSteps;  // SimOptions::max_fused_steps
     // the inverse of the Poisson operator for direct solves (built at the first self-consistent solve)
+    DevArray<double> stage64;  // host particle arrays on their way to the SoA state
     DevArray<double> green, green_vac, green_rhs, green_b, green_part;
     DevArray<int> green_j;  // compacted right-hand side (node, value), its length and the per-tile counts
     DevArray<SolveStatus> green_status;
@@ -231,6 +234,10 @@ private:
     PushArgs push_args(int s, bool init);
     CollideArgs collide_args(int s);
     void step(double* ms = nullptr);
+    // steps the next fused launch can take (1: step by step), and the launch
+    int fused_steps(uint64_t left) const;
+    void fused_block(int nsteps, double* ms = nullptr);
+    float rf_factor(uint64_t niter, double dt) const;
     void sort_species(int s);
     void refresh_rf_pairs();
     void upload_slots(int s);

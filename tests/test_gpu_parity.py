@@ -298,6 +298,45 @@ def test_sort_does_not_change_results(m, tmp_path):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
+@pytest.mark.parametrize("case", ["multipole_rf_mcc", "penning_external"])
+@pytest.mark.parametrize("fused", [64, 7])
+def test_fused_steps_bit_identical(m, tmp_path, case, fused):
+    """Where particles do not interact (no self-consistent field, background
+    collision targets) several steps run as one launch per species.  The
+    particles, counters and step counters equal those of the same steps run
+    one launch at a time: 22-pole RF field with elastic collisions on a dense
+    background (about 8000 collisions), and the Penning r-z field of the
+    electrodes alone with B (cylindrical mover)."""
+    from cases import multipole_xy, penning_rz
+
+    if case == "multipole_rf_mcc":
+        cfg, species, inter, cpath, spath, parts, _ = multipole_xy(tmp_path, n=20000, n_nodes=65, pressure=10.0)
+        sp = 1
+    else:
+        cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=20000, selfconsistent=0)
+        sp = 0
+    out = []
+    for mf in (1, fused):
+        pic = m.Pic(cpath, spath, seed=9, sort_interval=20, max_fused_steps=mf)
+        ion = pic.speclist[sp]
+        ion.set_particles(*parts)
+        pic.advance_init()
+        pic.advance(3)
+        pic.advance(150)
+        g = ion.particles()
+        order = np.argsort(g["id"])
+        d = ion.diag()
+        out.append(({k: v[order] for k, v in g.items()}, d))
+        pic.close()
+    (a, da), (b, db) = out
+    for k in ("id", "x", "z", "vx", "vy", "vz"):
+        assert np.array_equal(a[k], b[k]), k
+    for k in ("n_live", "collisions", "null_collisions", "removed", "particle_steps", "niter"):
+        assert da[k] == db[k], (k, da[k], db[k])
+    if case == "multipole_rf_mcc":
+        assert da["collisions"] > 1000, da
+
+
 @pytest.mark.parametrize("n", [20_000, 200_000], ids=["500_per_step", "5000_per_step"])
 def test_mcc_candidate_list_path(m, tmp_path, n):
     """Charge exchange with a neutral background and Coulomb collisions with a
