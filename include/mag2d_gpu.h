@@ -265,6 +265,26 @@ int mag_print_field(mag_sim* sim, const char* path);
  * <particle_reload_dir>/particles_<name>.dat at mag_create (src/pic.cpp:138-146). */
 int mag_species_save(mag_sim* sim, int species, const char* path);
 int mag_species_load(mag_sim* sim, int species, const char* path);
+
+/* Particle source of a Cartesian run with use_source = 1
+ * (Species<CARTESIAN>::source5_refresh / source, src/particles.cpp:1052-1226).
+ * mag_advance_init refreshes the source boxes with src_fact, as the
+ * reference's driver does after advance_init (src/test.cpp:56-59);
+ * mag_source_refresh redraws them with another factor.  Every step, after a
+ * species' push, its box particles fly in the external field (with the
+ * species' background collisions) and each crossing of a box face appends a
+ * copy entering the domain through the opposite face at a random tile.
+ * save / load: the source5 file (int32 count, then 64-byte t_particle
+ * records, src/particles.cpp:109-140); load returns MAG_EIO when the file
+ * cannot be opened (the reference warns and continues).  A config with
+ * particle_reload = 1 and use_source = 1 loads
+ * <particle_reload_dir>/particles_source_<name>.dat at mag_create.
+ * mag_source_info: box particles, copies appended so far, copies dropped
+ * (more than 4 face crossings of one box particle in one step). */
+int mag_source_refresh(mag_sim* sim, int factor);
+int mag_source_save(mag_sim* sim, int species, const char* path);
+int mag_source_load(mag_sim* sim, int species, const char* path);
+int mag_source_info(mag_sim* sim, int species, int64_t* n_box, int64_t* injected, int64_t* dropped);
 /* Host-only reading and writing of that file.  read: n_out = live records,
  * total_out = the slot count of the header; arrays of at least cap entries
  * (any may be NULL).  write: y and time_to_death may be NULL (zeros). */

@@ -106,6 +106,11 @@ def lib() -> ctypes.CDLL:
     L.mag_print_field.argtypes = [P, ctypes.c_char_p]
     L.mag_species_save.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
     L.mag_species_load.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
+    L.mag_source_refresh.argtypes = [P, ctypes.c_int]
+    L.mag_source_save.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
+    L.mag_source_load.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
+    L.mag_source_info.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                  ctypes.POINTER(ctypes.c_int64)]
     L.mag_particle_file_read.argtypes = [ctypes.c_char_p, ctypes.c_int64] + [D] * 7 + [
         ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.mag_particle_file_write.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int64] + [D] * 7

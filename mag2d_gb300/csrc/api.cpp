@@ -510,6 +510,54 @@ int mag_species_save(mag_sim* sim, int species, const char* path)
     });
 }
 
+int mag_source_refresh(mag_sim* sim, int factor)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!sim->s->p.use_source) throw mag::Error(MAG_EINVAL, "mag_source_refresh: the config does not set use_source");
+        sim->s->source_refresh(factor);
+        return device_status(sim);
+    });
+}
+
+int mag_source_save(mag_sim* sim, int species, const char* path)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (!path) throw mag::Error(MAG_EINVAL, "null path");
+        sim->s->source_save(species, path);
+        return device_status(sim);
+    });
+}
+
+int mag_source_load(mag_sim* sim, int species, const char* path)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (!path) throw mag::Error(MAG_EINVAL, "null path");
+        if (!sim->s->source_load(species, path)) throw mag::Error(MAG_EIO, std::string("cannot open ") + path);
+        return device_status(sim);
+    });
+}
+
+int mag_source_info(mag_sim* sim, int species, int64_t* n_box, int64_t* injected, int64_t* dropped)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        mag::Sim& s = *sim->s;
+        const mag::SourceState& Q = s.src[species];
+        unsigned long long d = 0;
+        if (Q.dropped.p) {
+            MAG_CK(cudaStreamSynchronize(s.stream));
+            MAG_CK(cudaMemcpy(&d, Q.dropped.p, sizeof d, cudaMemcpyDeviceToHost));
+        }
+        if (n_box) *n_box = Q.n;
+        if (injected) *injected = (int64_t)Q.injected;
+        if (dropped) *dropped = (int64_t)d;
+        return device_status(sim);
+    });
+}
+
 int mag_species_load(mag_sim* sim, int species, const char* path)
 {
     return guarded([&]() {

@@ -163,6 +163,42 @@ struct SortArgs {
     Counters* cnt;
 };
 
+// Source box particles of one species (use_source): positions in the box
+// [0, bx) x [0, bz) (FP64), velocities FP32, and per particle the copies of a
+// step (count, records of x, z, vx, vy, vz relative to the domain origin).
+constexpr int kMaxInject = 4;
+struct SourceArgs {
+    double* x;
+    double* z;
+    float* vx;
+    float* vy;
+    float* vz;
+    int64_t n;
+    int* count;
+    double* rec;
+    unsigned long long* dropped;
+    Counters* cnt;
+    double bx, bz, lx, lz, dt;
+    float hq, ez, tx, ty, tz, sx, sy, sz, prob;
+    int coll, factor;
+    uint32_t species;
+    uint64_t seed, step;
+};
+// where the copies of a step go: the species' arrays from slot base on
+struct SourceAppend {
+    uint32_t* x;
+    uint32_t* z;
+    float* vx;
+    float* vy;
+    float* vz;
+    uint32_t* id;
+    unsigned long long* rho;  // deposit (self-consistent runs) or null
+    int64_t base;
+    uint32_t next_id;
+    int nx, nz;
+    double dx, dz;
+};
+
 // Box and cell sizes for converting physical positions to fixed point.
 struct SetParticlesGeom {
     double x0, xmax, z0, zmax, dx, dz;

@@ -38,6 +38,11 @@ int launch_push_batch(const PushArgs* d_args, const unsigned* d_chunk_off, int n
 // species' collision data when its collision test is on
 int launch_push_fused(const PushArgs& a, const CollideArgs& c, const FusedSteps& fs, int coord, int sm_count,
                       cudaStream_t s);
+// particle source (use_source): box refresh, a step of the box particles with
+// the scan of their copies (offs, total), and the append of the copies
+int launch_source_refresh(const SourceArgs& a, float vsig, cudaStream_t s);
+int launch_source_step(const SourceArgs& a, const CollideArgs& c, int* offs, long long* total, cudaStream_t s);
+int launch_source_append(const SourceArgs& a, const int* offs, const SourceAppend& t, cudaStream_t s);
 int launch_deposit(const PushArgs& a, cudaStream_t s);
 int launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
 // ADVANCE_MULTICOLL step of one species (multicoll.cu); ttd = time to the next

@@ -19,5 +19,8 @@ struct ParticleFile {
 
 ParticleFile read_particle_file(const std::string& path);
 void write_particle_file(const std::string& path, const ParticleFile& f);
+// the source box file (int32 count, then records); false when it cannot be opened
+bool read_source_file(const std::string& path, ParticleFile& f);
+void write_source_file(const std::string& path, const ParticleFile& f);
 
 }  // namespace mag

@@ -41,7 +41,17 @@ MAG_HD U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
 }
 
 // Stream tags keep the draw families of one particle disjoint.
-enum : uint32_t { TAG_COLLIDE_TEST = 0, TAG_COLLIDE = 1, TAG_LOAD = 2, TAG_PARTNER = 3, TAG_MULTICOLL = 4, TAG_TTD = 5 };
+enum : uint32_t {
+    TAG_COLLIDE_TEST = 0,
+    TAG_COLLIDE = 1,
+    TAG_LOAD = 2,
+    TAG_PARTNER = 3,
+    TAG_MULTICOLL = 4,
+    TAG_TTD = 5,
+    TAG_SOURCE_INIT = 6,  // source box particles: initial positions and velocities
+    TAG_SOURCE = 7,       // source box particles: collision test and scatter of a step
+    TAG_SOURCE_TILE = 8   // source box particles: the tile of each copy of a step
+};
 
 // Draw block 'k' (4 words) of particle 'id' at 'step' for species 'sp'.
 MAG_HD U4 draw(uint64_t seed, uint32_t sp, uint32_t id, uint64_t step, uint32_t tag, uint32_t k)

@@ -79,7 +79,10 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
             throw Error(-1, "Species<CARTESIAN>::advance_multicoll() implemented for const extern field only:\n"
                             "\tset selfconsistent=0 and geometry=EMPTY");
     }
-    if (p.use_source) throw Error(-1, "use_source: particle sources are not provided by this library");
+    if (p.use_source && p.coord != CARTESIAN)  // declared but never defined in the reference (particles.hpp:311)
+        throw Error(-1, "use_source: Species<CYLINDRICAL>::source is not defined in the reference");
+    if (p.use_source && multicoll)
+        throw Error(-1, "use_source: the source box with ADVANCE_MULTICOLL is not provided by this library");
     if (p.u_smooth) throw Error(-1, "u_smooth: potential smoothing is not provided by this library");
     parse_species_conf(species_conf, species_prm, inters);
     if (species_prm.empty()) throw Error(-1, "species_conf defines no species");
@@ -105,9 +108,12 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     setup_species();
     if (opts.capacity_hint > 0)
         for (size_t s = 0; s < sp.size(); ++s) ensure_capacity((int)s, opts.capacity_hint);
+    src.resize(sp.size());
     if (p.particle_reload)  // Pic constructor (src/pic.cpp:138-146): every species from particle_reload_dir
-        for (size_t s = 0; s < sp.size(); ++s)
+        for (size_t s = 0; s < sp.size(); ++s) {
             load_species((int)s, p.particle_reload_dir + "/particles_" + species_prm[s].name + ".dat");
+            if (p.use_source) source_load((int)s, p.particle_reload_dir + "/particles_source_" + species_prm[s].name + ".dat");
+        }
     MAG_CK(cudaStreamSynchronize(stream));
     int e = sync();
     if (e != 0) throw Error(e, "initial field solve failed (device status " + std::to_string(e) + ")");
@@ -987,6 +993,7 @@ void Sim::step(double* ms)
         }
         S.launches++;
         S.niter++;
+        if (p.use_source) source_step((int)s);  // Pic::advance (src/pic.cpp:344-348)
     }
     if (ms) {
         MAG_CK(cudaEventSynchronize(ev.back()));
@@ -1004,7 +1011,7 @@ void Sim::step(double* ms)
 // collision targets without particles.  The block ends before the next sort.
 int Sim::fused_steps(uint64_t left) const
 {
-    if (max_fused <= 1 || left <= 1 || p.selfconsistent || multicoll) return 1;
+    if (max_fused <= 1 || left <= 1 || p.selfconsistent || multicoll || p.use_source) return 1;
     for (size_t s = 0; s < sp.size(); ++s)
         if (sp[s].n_slots > 0 && coll_mode((int)s) != 0 && any_target_slots((int)s)) return 1;
     uint64_t k = std::min<uint64_t>(left, (uint64_t)max_fused);
@@ -1095,6 +1102,7 @@ void Sim::advance_init(bool deposit)
         PushArgs pa = push_args((int)s, true);
         launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, true, push_vec, sm_count, stream);
     }
+    if (p.use_source) source_refresh(p.src_fact);  // the driver's refresh after advance_init (src/test.cpp:56-59)
     MAG_CK(cudaGetLastError());
 }
 
@@ -1424,6 +1432,171 @@ void Sim::energy(int s, double& sum_v2, unsigned long long& n)
         MAG_CK(cudaMemcpy(&sum_v2, d.p, 8, cudaMemcpyDeviceToHost));
         MAG_CK(cudaMemcpy(&n, c.p, 8, cudaMemcpyDeviceToHost));
     }
+}
+
+// ---- particle source --------------------------------------------------
+
+SourceArgs Sim::source_args(int s, bool init)
+{
+    SpeciesState& S = sp[s];
+    SourceState& Q = src[s];
+    SourceArgs a{};
+    a.x = Q.x.p;
+    a.z = Q.z.p;
+    a.vx = Q.vx.p;
+    a.vy = Q.vy.p;
+    a.vz = Q.vz.p;
+    a.n = Q.n;
+    a.count = Q.count.p;
+    a.rec = Q.rec.p;
+    a.dropped = Q.dropped.p;
+    a.cnt = S.cnt.p;
+    a.lx = xmax - x0;
+    a.lz = zmax - z0;
+    a.factor = std::max(Q.factor, 1);
+    a.bx = a.lx / a.factor;
+    a.bz = a.lz / a.factor;
+    a.dt = S.prm.dt;
+    const PushArgs pa = push_args(s, init);
+    a.hq = pa.hq;
+    a.ez = pa.extern_ez;
+    a.tx = pa.tx;
+    a.ty = pa.ty;
+    a.tz = pa.tz;
+    a.sx = pa.sx;
+    a.sy = pa.sy;
+    a.sz = pa.sz;
+    a.prob = (float)S.prob;
+    a.coll = !init && coll_mode(s) != 0 ? 1 : 0;
+    a.species = (uint32_t)s;
+    a.seed = seed;
+    a.step = S.niter;
+    return a;
+}
+
+// Species<CARTESIAN>::source5_refresh (src/particles.cpp:1052-1082) for every
+// species that holds particles: N / factor box particles, N = density V.
+void Sim::source_refresh(int factor)
+{
+    if (factor < 1) throw Error(-1, "source refresh: factor must be >= 1");
+    if (p.coord != CARTESIAN) throw Error(-1, "use_source: Species<CYLINDRICAL>::source is not defined in the reference");
+    src.resize(sp.size());
+    for (size_t s = 0; s < sp.size(); ++s) {
+        SpeciesState& S = sp[s];
+        SourceState& Q = src[s];
+        Q.factor = factor;
+        if (S.n_slots == 0) continue;  // "checks if we simulate this species as particles"
+        if (coll_mode((int)s) != 0 && any_target_slots((int)s))
+            throw Error(-1, "use_source: source box collisions with particle partners are not provided by this library");
+        const int64_t n = (int64_t)(unsigned)(S.prm.density * p.V / factor);
+        Q.n = n;
+        for (auto* a : {&Q.x, &Q.z}) a->alloc(std::max<int64_t>(n, 1));
+        for (auto* a : {&Q.vx, &Q.vy, &Q.vz}) a->alloc(std::max<int64_t>(n, 1));
+        Q.count.alloc(std::max<int64_t>(n, 1));
+        Q.offs.alloc(std::max<int64_t>(n, 1));
+        Q.rec.alloc((size_t)std::max<int64_t>(n, 1) * kMaxInject * 5);
+        Q.total.alloc(1);
+        Q.dropped.alloc(1);
+        Q.dropped.zero(stream);
+        launches += launch_source_refresh(source_args((int)s, true), (float)(S.v_max / std::sqrt(2.0)), stream);
+    }
+    MAG_CK(cudaStreamSynchronize(stream));
+}
+
+// Species<CARTESIAN>::source (src/particles.cpp:1165-1226) after the species'
+// push: the box step, then its copies appended to the species (the count is
+// read back to size the arrays).
+void Sim::source_step(int s)
+{
+    SourceState& Q = src[s];
+    if (Q.n == 0) return;
+    SpeciesState& S = sp[s];
+    const SourceArgs a = source_args(s, false);
+    const CollideArgs c = a.coll ? collide_args(s) : CollideArgs{};
+    launches += launch_source_step(a, c, Q.offs.p, Q.total.p, stream);
+    long long total = 0;
+    MAG_CK(cudaMemcpyAsync(&total, Q.total.p, sizeof total, cudaMemcpyDeviceToHost, stream));
+    MAG_CK(cudaStreamSynchronize(stream));
+    if (total <= 0) return;
+    ensure_capacity(s, S.n_slots + total);
+    SourceAppend t{};
+    t.x = S.x.p;
+    t.z = S.z.p;
+    t.vx = S.vx.p;
+    t.vy = S.vy.p;
+    t.vz = S.vz.p;
+    t.id = S.id.p;
+    t.rho = p.selfconsistent ? S.rho.p : nullptr;
+    t.base = S.n_slots;
+    t.next_id = S.next_id;
+    t.nx = nx;
+    t.nz = nz;
+    t.dx = dx;
+    t.dz = dz;
+    launches += launch_source_append(a, Q.offs.p, t, stream);
+    S.n_slots += total;
+    S.next_id += (uint32_t)total;
+    Q.injected += (uint64_t)total;
+    upload_slots(s);
+}
+
+// BaseSpecies::source5_save (src/particles.cpp:109-120)
+void Sim::source_save(int s, const std::string& path)
+{
+    SourceState& Q = src[s];
+    ParticleFile f;
+    const int64_t n = Q.n;
+    for (auto* v : {&f.x, &f.z, &f.vx, &f.vy, &f.vz}) v->resize(n);
+    std::vector<float> v3[3];
+    for (auto& v : v3) v.resize(n);
+    if (n) {
+        Q.x.download(f.x.data(), n, stream);
+        Q.z.download(f.z.data(), n, stream);
+        Q.vx.download(v3[0].data(), n, stream);
+        Q.vy.download(v3[1].data(), n, stream);
+        Q.vz.download(v3[2].data(), n, stream);
+    }
+    MAG_CK(cudaStreamSynchronize(stream));
+    for (int64_t i = 0; i < n; ++i) {
+        f.vx[i] = v3[0][i];
+        f.vy[i] = v3[1][i];
+        f.vz[i] = v3[2][i];
+    }
+    write_source_file(path, f);
+}
+
+// BaseSpecies::source5_load (src/particles.cpp:122-140): false (and the box
+// unchanged) when the file cannot be opened, as the reference only warns
+bool Sim::source_load(int s, const std::string& path)
+{
+    ParticleFile f;
+    if (!read_source_file(path, f)) return false;
+    SourceState& Q = src[s];
+    const int64_t n = (int64_t)f.x.size();
+    if (Q.factor == 0) Q.factor = std::max(p.src_fact, 1);
+    Q.n = n;
+    for (auto* a : {&Q.x, &Q.z}) a->alloc(std::max<int64_t>(n, 1));
+    for (auto* a : {&Q.vx, &Q.vy, &Q.vz}) a->alloc(std::max<int64_t>(n, 1));
+    Q.count.alloc(std::max<int64_t>(n, 1));
+    Q.offs.alloc(std::max<int64_t>(n, 1));
+    Q.rec.alloc((size_t)std::max<int64_t>(n, 1) * kMaxInject * 5);
+    Q.total.alloc(1);
+    Q.dropped.alloc(1);
+    Q.dropped.zero(stream);
+    std::vector<float> v3[3];
+    for (auto& v : v3) v.resize(n);
+    for (int64_t i = 0; i < n; ++i) {
+        v3[0][i] = (float)f.vx[i];
+        v3[1][i] = (float)f.vy[i];
+        v3[2][i] = (float)f.vz[i];
+    }
+    Q.x.upload(f.x.data(), n, stream);
+    Q.z.upload(f.z.data(), n, stream);
+    Q.vx.upload(v3[0].data(), n, stream);
+    Q.vy.upload(v3[1].data(), n, stream);
+    Q.vz.upload(v3[2].data(), n, stream);
+    MAG_CK(cudaStreamSynchronize(stream));
+    return true;
 }
 
 }  // namespace mag

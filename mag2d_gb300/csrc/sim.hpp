@@ -104,6 +104,18 @@ struct SpeciesState {
     int inter_off = 0;                 // first entry of this species in the device interaction list
 };
 
+// Source box of one species (use_source, Species<CARTESIAN>::source2_particles)
+struct SourceState {
+    DevArray<double> x, z, rec;
+    DevArray<float> vx, vy, vz;
+    DevArray<int> count, offs;
+    DevArray<long long> total;
+    DevArray<unsigned long long> dropped;
+    int64_t n = 0;
+    int factor = 0;
+    uint64_t injected = 0;  // copies appended to the species so far
+};
+
 struct SolverLevels {
     int nlev = 0;
     std::vector<int> nx, nz;
@@ -124,6 +136,14 @@ public:
     void advance(uint64_t nsteps);
     void advance_timed(uint64_t nsteps, double* ms4);
     int sync();  // returns first device error code (0 = none)
+    // particle source (use_source): source5_refresh of every species with
+    // particles, one step of a species' box, source5_save / source5_load
+    std::vector<SourceState> src;
+    void source_refresh(int factor);
+    void source_step(int s);
+    SourceArgs source_args(int s, bool init);
+    void source_save(int s, const std::string& path);
+    bool source_load(int s, const std::string& path);
 
     // accessors used by the C ABI
     std::string config_path;  // the config.txt the simulation was made from

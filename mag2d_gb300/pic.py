@@ -141,6 +141,20 @@ class Species:
         """BaseSpecies::load (src/particles.cpp:59-93)."""
         check(lib().mag_species_load(self._pic.h, self.index, str(path).encode()))
 
+    def source_save(self, path) -> None:
+        """BaseSpecies::source5_save (src/particles.cpp:109-120)."""
+        check(lib().mag_source_save(self._pic.h, self.index, str(path).encode()))
+
+    def source_load(self, path) -> None:
+        """BaseSpecies::source5_load (src/particles.cpp:122-140)."""
+        check(lib().mag_source_load(self._pic.h, self.index, str(path).encode()))
+
+    def source_info(self) -> dict:
+        """Source box particles, copies appended to the species so far, copies dropped."""
+        v = [ctypes.c_int64() for _ in range(3)]
+        check(lib().mag_source_info(self._pic.h, self.index, *[ctypes.byref(x) for x in v]))
+        return {"n_box": v[0].value, "injected": v[1].value, "dropped": v[2].value}
+
     def rho_fixed(self) -> np.ndarray:
         nx, nz = self._pic.shape
         out = np.zeros((nx, nz), dtype=np.int64)
@@ -228,6 +242,10 @@ class Pic:
 
     def advance(self, n: int = 1) -> None:
         check(lib().mag_advance(self.h, n))
+
+    def source_refresh(self, factor: int) -> None:
+        """Species<CARTESIAN>::source5_refresh(factor) of every species with particles."""
+        check(lib().mag_source_refresh(self.h, factor))
 
     def advance_timed(self, n: int = 1):
         """advance(n) with CUDA event timing: (sort_ms, solve_ms, particle_ms, collide_ms)."""

@@ -240,6 +240,35 @@ int ref_load(void* h, int sp, const char* path)
     return with_pic(h, [&](auto& p) { p.speclist[sp]->load(path); return (int)p.speclist[sp]->particles.size(); });
 }
 
+// The driver's source refresh after advance_init (src/test.cpp:56-59):
+// Species::source5_refresh(factor) of every species
+int ref_source_refresh(void* h, int factor)
+{
+    RefSim* s = static_cast<RefSim*>(h);
+    return guard([&]() {
+        if (!s->cart) throw std::runtime_error("source5_refresh is defined for CARTESIAN only in the reference\n");
+        for (size_t i = 0; i < s->cart->speclist.size(); ++i)
+            if (s->cart->speclist[i]->particle) s->cart->speclist[i]->source5_refresh(factor);
+        return 0;
+    });
+}
+
+// BaseSpecies::source5_save (src/particles.cpp:109-120) of species sp
+int ref_source_save(void* h, int sp, const char* path)
+{
+    return with_pic(h, [&](auto& p) { p.speclist[sp]->source5_save(path); return 0; });
+}
+
+// live particles of species sp (non-empty slots)
+int ref_n_live(void* h, int sp)
+{
+    return with_pic(h, [&](auto& p) {
+        int n = 0;
+        for (const t_particle& q : p.speclist[sp]->particles) n += q.empty ? 0 : 1;
+        return n;
+    });
+}
+
 int ref_advance_init(void* h)
 {
     return with_pic(h, [&](auto& p) { p.advance_init(); return 0; });

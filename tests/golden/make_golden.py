@@ -326,10 +326,35 @@ def gen_particle_file():
          meta=meta(cfg=cfg))
 
 
+def gen_source():
+    """Species<CARTESIAN>::source5_refresh / source of the reference: the box
+    file after the refresh (source5_save) and the live particle count of the
+    domain every 10 steps while the boundary inflow fills it."""
+    cfg = dict(coord="CARTESIAN", geometry="EMPTY", boundary="FREE", x_max=1e-2, z_max=1e-2, x_sampl=21,
+               z_sampl=21, selfconsistent=0, rf=0, do_plot=0, use_source=1, src_fact=10, extern_field=0.0,
+               magnetic_field_const=1, Bz=0.0, Br=0.0, Bt=0.0, n_particles_total=1e5, density_total=1e13,
+               mover="ADVANCE_BORIS")
+    species = [dict(name="ELECTRON", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-10, density=1e12,
+                    temperature=11604.5)]
+    cp = write_config(cfg, TMP / "src_cfg.txt")
+    sp = write_species_conf(species, [], TMP / "src_sp.txt")
+    ref = Ref(cp, sp, TMP / "o", 7)
+    ref.set_particles(0, np.array([5e-3]), np.array([5e-3]), np.zeros(1), np.zeros(1), np.zeros(1))
+    ref.advance_init()
+    ref.source_refresh(cfg["src_fact"])
+    ref.source_save(0, HERE / "source_ref.dat")
+    steps, live = [0], [ref.n_live(0)]
+    for k in range(30):
+        ref.advance(10)
+        steps.append(10 * (k + 1))
+        live.append(ref.n_live(0))
+    save("source.npz", steps=np.array(steps), live=np.array(live), meta=meta(cfg=cfg, species=species))
+
+
 if __name__ == "__main__":
-    gen_rng()
-    gen_steps()
-    gen_solves()
-    gen_geometry()
-    gen_params_species()
-    gen_particle_file()
+    import sys
+
+    cases = {"rng": gen_rng, "steps": gen_steps, "solves": gen_solves, "geometry": gen_geometry,
+             "params_species": gen_params_species, "particle_file": gen_particle_file, "source": gen_source}
+    for name in (sys.argv[1:] or list(cases)):
+        cases[name]()

@@ -391,6 +391,15 @@ class Ref:
         self.L.ref_grid(self.h, dims, _dp(out))
         return (dims[0], dims[1]), out
 
+    def source_refresh(self, factor: int):
+        self._check(self.L.ref_source_refresh(self.h, factor))
+
+    def source_save(self, sp: int, path):
+        self._check(self.L.ref_source_save(self.h, sp, str(path).encode()))
+
+    def n_live(self, sp: int) -> int:
+        return self._check(self.L.ref_n_live(self.h, sp))
+
     def species_info(self, sp: int):
         buf = ctypes.create_string_buffer(128)
         out = np.zeros(11)

@@ -204,3 +204,23 @@ def test_particle_file_matches_reference_save(built):
     for i in range(len(d["x"])):
         a = 8 + 64 * i
         assert ours[a:a + 57] == ref[a:a + 57], i  # 7 doubles and the empty flag
+
+
+def test_source_golden_fixture():
+    """The reference's source box file and inflow curve (make_golden.py source):
+    N / src_fact box particles inside the box, and a domain filling toward
+    density * V (the source's purpose) without overshoot."""
+    g = np.load(GOLDEN / "source.npz", allow_pickle=True)
+    meta = json.loads(str(g["meta"]))
+    cfg, sp = meta["cfg"], meta["species"][0]
+    raw = (GOLDEN / "source_ref.dat").read_bytes()
+    n = int(np.frombuffer(raw[:4], dtype=np.int32)[0])
+    rec = np.frombuffer(raw[4:], dtype=np.float64).reshape(n, 8)
+    V = cfg["n_particles_total"] / cfg["density_total"]
+    assert n == int(sp["density"] * V / cfg["src_fact"])
+    bx, bz = cfg["x_max"] / cfg["src_fact"], cfg["z_max"] / cfg["src_fact"]
+    assert np.all((rec[:, 0] >= 0) & (rec[:, 0] < bx) & (rec[:, 2] >= 0) & (rec[:, 2] < bz))
+    vsig = np.sqrt(1.380662e-23 * sp["temperature"] / sp["mass"])
+    assert abs(rec[:, 3].std() / vsig - 1) < 0.1 and abs(rec[:, 5].std() / vsig - 1) < 0.1
+    live = g["live"]
+    assert np.all(np.diff(live) > 0) and live[-1] < 1.05 * sp["density"] * V
