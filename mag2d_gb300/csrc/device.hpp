@@ -215,17 +215,17 @@ struct FusedSteps {
 
 // Direct solve with the precomputed inverse G (nn x nn, column-major by
 // right-hand-side node); u_vac (nullable) is the stored potential of the
-// Dirichlet values of the solve's voltages; bprime, list_j and list_b hold nn
-// entries, tile_count one per 1024 nodes, part nchunks * nn.
+// Dirichlet values of the solve's voltages; list_j and list_b hold nn entries
+// (the compacted right-hand side, tile by tile of 1024 nodes), tile_count one
+// per tile, part nchunks * nn.
 constexpr int kGreenMaxChunks = 32;
+constexpr int kGreenMaxTiles = (int)((kSingleBlockNodes + 1023) / 1024);
 struct GreenArgs {
     const double* G;
     const double* u_vac;
-    double* bprime;
     int* tile_count;
     int* list_j;
     double* list_b;
-    int* count;
     double* part;
     int nchunks;
 };

@@ -586,6 +586,7 @@ __global__ void __launch_bounds__(1024) k_solve_batch(const SolveArgs* __restric
 // and the work does not depend on where the charge sits.
 
 constexpr int kGreenTile = 1024;  // nodes per block of the right-hand side and its compaction
+constexpr int kGemvLoads = 8;     // independent column loads in flight per thread of the product
 
 __device__ __forceinline__ double green_rhs_node(const SolveArgs& a, long long k, bool dirichlet)
 {
@@ -620,67 +621,56 @@ __device__ __forceinline__ double green_rhs_node(const SolveArgs& a, long long k
     return b;
 }
 
-// b' of every node (one node per thread) and the number of nonzero entries of
-// each tile of kGreenTile nodes
-__global__ void __launch_bounds__(kGreenTile) k_green_rhs(const SolveArgs a, bool dirichlet,
-                                                          double* __restrict__ bprime, int* __restrict__ tile_count)
+// b' of every node (one node per thread); block t compacts the nonzero
+// entries of its tile of kGreenTile nodes, in node order, to list slots
+// [t kGreenTile, t kGreenTile + tile_count[t]).
+__global__ void __launch_bounds__(kGreenTile) k_green_rhs(const SolveArgs a, bool dirichlet, int* __restrict__ list_j,
+                                                          double* __restrict__ list_b, int* __restrict__ tile_count)
 {
+    __shared__ int wcount[kGreenTile / 32];
     const long long nn = (long long)a.nx * a.nz;
     const long long k = (long long)blockIdx.x * kGreenTile + threadIdx.x;
     const double b = k < nn ? green_rhs_node(a, k, dirichlet) : 0.0;
-    if (k < nn) bprime[k] = b;
-    const int c = __syncthreads_count(b != 0.0);
-    if (threadIdx.x == 0) tile_count[blockIdx.x] = c;
-}
-
-// the nonzero entries of b' in node order: block t writes its tile's entries
-// after those of tiles 0..t-1; block 0 also writes the total
-__global__ void __launch_bounds__(kGreenTile) k_green_compact(const double* __restrict__ bprime, long long nn,
-                                                              const int* __restrict__ tile_count, int ntiles,
-                                                              int* __restrict__ list_j, double* __restrict__ list_b,
-                                                              int* __restrict__ count)
-{
-    __shared__ int wcount[kGreenTile / 32];
-    __shared__ int s_base;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp == 0) {
-        int before = 0, total = 0;
-        for (int t = lane; t < ntiles; t += 32) {
-            const int c = tile_count[t];
-            before += t < (int)blockIdx.x ? c : 0;
-            total += c;
-        }
-        before = __reduce_add_sync(0xffffffffu, before);
-        total = __reduce_add_sync(0xffffffffu, total);
-        if (lane == 0) {
-            s_base = before;
-            if (blockIdx.x == 0) *count = total;
-        }
-    }
-    const long long k = (long long)blockIdx.x * kGreenTile + threadIdx.x;
-    const double b = k < nn ? bprime[k] : 0.0;
     const unsigned m = __ballot_sync(0xffffffffu, b != 0.0);
     if (lane == 0) wcount[warp] = __popc(m);
     __syncthreads();
-    int before = s_base;
-    for (int w = 0; w < warp; ++w) before += wcount[w];
+    int before = 0, total = 0;
+    for (int w = 0; w < kGreenTile / 32; ++w) {
+        const int c = wcount[w];
+        before += w < warp ? c : 0;
+        total += c;
+    }
     if (b != 0.0) {
-        const int pos = before + __popc(m & ((1u << lane) - 1u));
+        const long long pos = (long long)blockIdx.x * kGreenTile + before + __popc(m & ((1u << lane) - 1u));
         list_j[pos] = (int)k;
         list_b[pos] = b;
     }
+    if (threadIdx.x == 0) tile_count[blockIdx.x] = total;
 }
 
 // part[c][i] = sum over the list entries q of chunk c of G[j_q][i] b_q, in
-// list order; chunk c of nchunks holds entries [c L / nchunks, (c+1) L / nchunks).
+// list order; the list is the tiles' entries one after the other (L in all),
+// chunk c of nchunks holds entries [c L / nchunks, (c+1) L / nchunks).
 __global__ void __launch_bounds__(256) k_green_gemv(const double* __restrict__ G, const int* __restrict__ list_j,
-                                                    const double* __restrict__ list_b, const int* __restrict__ count,
-                                                    long long nn, double* __restrict__ part)
+                                                    const double* __restrict__ list_b,
+                                                    const int* __restrict__ tile_count, int ntiles, long long nn,
+                                                    double* __restrict__ part)
 {
     __shared__ double sb[256];
     __shared__ int sj[256];
+    __shared__ int start[kGreenMaxTiles + 1];
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int t = 0; t < ntiles; ++t) {
+            start[t] = acc;
+            acc += tile_count[t];
+        }
+        start[ntiles] = acc;
+    }
+    __syncthreads();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long L = *count, nch = gridDim.y;
+    const long long L = start[ntiles], nch = gridDim.y;
     const long long q0 = L * blockIdx.y / nch, q1 = L * (blockIdx.y + 1) / nch;
     const bool row = i < nn;
     const double* __restrict__ gi = G + (row ? i : 0);
@@ -688,18 +678,26 @@ __global__ void __launch_bounds__(256) k_green_gemv(const double* __restrict__ G
     for (long long t0 = q0; t0 < q1; t0 += 256) {
         const int total = (int)min(256LL, q1 - t0);
         if (threadIdx.x < total) {
-            sj[threadIdx.x] = list_j[t0 + threadIdx.x];
-            sb[threadIdx.x] = list_b[t0 + threadIdx.x];
+            const int q = (int)(t0 + threadIdx.x);
+            int lo = 0, hi = ntiles - 1;  // last tile whose first entry is <= q
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (start[mid] <= q) lo = mid;
+                else hi = mid - 1;
+            }
+            const long long slot = (long long)lo * kGreenTile + (q - start[lo]);
+            sj[threadIdx.x] = list_j[slot];
+            sb[threadIdx.x] = list_b[slot];
         }
         __syncthreads();
         if (row) {
             int q = 0;
-            for (; q + 8 <= total; q += 8) {
-                double g[8];
+            for (; q + kGemvLoads <= total; q += kGemvLoads) {
+                double g[kGemvLoads];
 #pragma unroll
-                for (int r = 0; r < 8; ++r) g[r] = __ldcs(gi + (long long)sj[q + r] * nn);
+                for (int r = 0; r < kGemvLoads; ++r) g[r] = __ldcs(gi + (long long)sj[q + r] * nn);
 #pragma unroll
-                for (int r = 0; r < 8; ++r) acc = fma(g[r], sb[q + r], acc);
+                for (int r = 0; r < kGemvLoads; ++r) acc = fma(g[r], sb[q + r], acc);
             }
             for (; q < total; ++q) acc = fma(__ldcs(gi + (long long)sj[q] * nn), sb[q], acc);
         }
@@ -791,13 +789,12 @@ int launch_green_solve(const SolveArgs& a, const GreenArgs& g, cudaStream_t s)
 {
     const long long nn = (long long)a.nx * a.nz;
     const int ntiles = (int)((nn + kGreenTile - 1) / kGreenTile);
-    k_green_rhs<<<ntiles, kGreenTile, 0, s>>>(a, g.u_vac == nullptr, g.bprime, g.tile_count);
-    k_green_compact<<<ntiles, kGreenTile, 0, s>>>(g.bprime, nn, g.tile_count, ntiles, g.list_j, g.list_b, g.count);
-    k_green_gemv<<<dim3((unsigned)((nn + 255) / 256), (unsigned)g.nchunks), 256, 0, s>>>(g.G, g.list_j, g.list_b,
-                                                                                         g.count, nn, g.part);
+    k_green_rhs<<<ntiles, kGreenTile, 0, s>>>(a, g.u_vac == nullptr, g.list_j, g.list_b, g.tile_count);
+    k_green_gemv<<<dim3((unsigned)((nn + 255) / 256), (unsigned)g.nchunks), 256, 0, s>>>(
+        g.G, g.list_j, g.list_b, g.tile_count, ntiles, nn, g.part);
     const unsigned g1 = (unsigned)std::min<long long>((nn + 63) / 64, 152 * 16);
     k_green_sum<<<g1, 64, 0, s>>>(a, g.part, g.nchunks, g.u_vac);
-    int n = 4;
+    int n = 3;
     if (a.Exf) n += launch_faces(a.u, a.nx, a.nz, a.dx, a.dz, a.Exf, a.Ezf, s);
     return n;
 }

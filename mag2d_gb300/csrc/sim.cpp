@@ -426,9 +426,8 @@ void Sim::build_green()
     }
     MAG_CK(cudaGetLastError());
     green_chunks_n = green_chunks(nn, sm_count);
-    green_rhs.alloc(nn);
     green_b.alloc(nn);
-    green_j.alloc(nn + 1 + (nn + 1023) / 1024);
+    green_j.alloc(nn + (nn + 1023) / 1024);
     green_part.alloc((size_t)green_chunks_n * nn);
     green_status.alloc(1);
     // the potential of the electrodes alone
@@ -448,11 +447,9 @@ GreenArgs Sim::green_args(bool vacuum) const
     g.G = green.p;
     g.u_vac = vacuum ? green_vac.p : nullptr;
     const long long nn = (long long)nx * nz;
-    g.bprime = green_rhs.p;
     g.list_j = green_j.p;
     g.list_b = green_b.p;
-    g.count = green_j.p + nn;
-    g.tile_count = green_j.p + nn + 1;
+    g.tile_count = green_j.p + nn;
     g.part = green_part.p;
     g.nchunks = green_chunks_n;
     return g;

@@ -172,8 +172,8 @@ public:
     int max_fused = kMaxFusedSteps;  // SimOptions::max_fused_steps
     // the inverse of the Poisson operator for direct solves (built at the first self-consistent solve)
     DevArray<double> stage64;  // host particle arrays on their way to the SoA state
-    DevArray<double> green, green_vac, green_rhs, green_b, green_part;
-    DevArray<int> green_j;  // compacted right-hand side (node, value), its length and the per-tile counts
+    DevArray<double> green, green_vac, green_b, green_part;
+    DevArray<int> green_j;  // compacted right-hand side (node, value) and the per-tile counts
     DevArray<SolveStatus> green_status;
     int green_chunks_n = 0;
     GreenArgs green_args(bool vacuum) const;
