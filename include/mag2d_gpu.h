@@ -375,6 +375,40 @@ int mag_batch_instance(mag_batch* b, int i, mag_sim** out);
 void* mag_batch_stream(mag_batch* b);
 int64_t mag_batch_kernel_launches(mag_batch* b);
 
+/* ---- 3D Cartesian run (coord = CARTESIAN3D) --------------------------------
+ * ElMag3D + Species<CARTESIAN3D> (src/fields3d.cpp:1-101, src/species3d.cpp:3-94,
+ * src/Field3D.hpp:40-163), whose prototype code does not build as shipped;
+ * these entry points follow its mathematics: the box faces fixed at 0 V and
+ * the centre node (the "Quadrupole" electrode) at 1 V; -lap(u) = rho / eps0
+ * on the 7-point grid with its spacings (rho = deposited charge x
+ * macroparticle_factor / cell volume); E = -grad u by Field3D's staggered
+ * differences; the leapfrog Boris step with constant B (Br, Bt, Bz as
+ * Bx, By, Bz), FREE or PERIODIC boundary, the 8-corner is_free test, the
+ * trilinear deposit and the null-collision MCC of the 2D path.  Grids are
+ * x_sampl x y_sampl x z_sampl nodes, index (i ny + j) nz + k.
+ * mag3d_grid returns the number of species; dims = nx, ny, nz; spacing =
+ * dx, dy, dz.  mag3d_solve: ElMag3D::solve of the given charge density
+ * [C/m^3] (or of the deposits when rho is NULL), conjugate gradients to
+ * poisson_tol (relative residual).  mag3d_get_field: MAG_U, MAG_RHO (charge
+ * per node [C] as deposited), MAG_MASK (0 fixed, -1 electrode, 2 free).
+ * mag_opts fields used: device, seed, poisson_tol, poisson_max_iter,
+ * capacity_hint. */
+typedef struct mag3d_sim mag3d_sim;
+int mag3d_create(const char* config_path, const char* species_conf_path, const mag_opts* opts, mag3d_sim** out);
+void mag3d_destroy(mag3d_sim* sim);
+int mag3d_grid(mag3d_sim* sim, int* dims, double* spacing);
+int mag3d_set_particles(mag3d_sim* sim, int species, int64_t n, const double* x, const double* y, const double* z,
+                        const double* vx, const double* vy, const double* vz);
+int mag3d_get_particles(mag3d_sim* sim, int species, int64_t cap, double* x, double* y, double* z, double* vx,
+                        double* vy, double* vz, uint32_t* id, int64_t* n_out);
+int mag3d_advance_init(mag3d_sim* sim);
+int mag3d_advance(mag3d_sim* sim, uint64_t nsteps);
+int mag3d_solve(mag3d_sim* sim, const double* rho, mag_solve_info* info);
+int mag3d_get_field(mag3d_sim* sim, int which, double* out);
+int mag3d_get_rho_fixed(mag3d_sim* sim, int species, int64_t* out);
+int mag3d_diag(mag3d_sim* sim, int species, mag_diag_out* out);
+int64_t mag3d_kernel_launches(mag3d_sim* sim);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,22 @@ def lib() -> ctypes.CDLL:
     L.mag_batch_instance.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
     L.mag_batch_stream.argtypes = [P]
     L.mag_batch_stream.restype = ctypes.c_void_p
+    I64 = ctypes.c_int64
+    L.mag3d_create.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(MagOpts), ctypes.POINTER(P)]
+    L.mag3d_destroy.argtypes = [P]
+    L.mag3d_destroy.restype = None
+    L.mag3d_grid.argtypes = [P, ctypes.POINTER(ctypes.c_int), D]
+    L.mag3d_set_particles.argtypes = [P, ctypes.c_int, I64, D, D, D, D, D, D]
+    L.mag3d_get_particles.argtypes = [P, ctypes.c_int, I64, D, D, D, D, D, D, ctypes.POINTER(ctypes.c_uint32),
+                                      ctypes.POINTER(I64)]
+    L.mag3d_advance_init.argtypes = [P]
+    L.mag3d_advance.argtypes = [P, ctypes.c_uint64]
+    L.mag3d_solve.argtypes = [P, D, ctypes.POINTER(MagSolveInfo)]
+    L.mag3d_get_field.argtypes = [P, ctypes.c_int, D]
+    L.mag3d_get_rho_fixed.argtypes = [P, ctypes.c_int, ctypes.POINTER(I64)]
+    L.mag3d_diag.argtypes = [P, ctypes.c_int, ctypes.POINTER(MagDiag)]
+    L.mag3d_kernel_launches.argtypes = [P]
+    L.mag3d_kernel_launches.restype = I64
     L.mag_batch_kernel_launches.argtypes = [P]
     L.mag_batch_kernel_launches.restype = ctypes.c_int64
     L.mag_grid.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), D, D, D, D]

@@ -238,6 +238,59 @@ struct SolveStatus {
     int pad;
 };
 
+// ---- the 3D Cartesian path ------------------------------------------------
+constexpr int kDeposit3Bits = 14;  // 3D CIC weights quantised to 2^-14 per axis (2^42 per particle)
+
+struct Push3Args {
+    uint32_t* x;
+    uint32_t* y;
+    uint32_t* z;
+    float* vx;
+    float* vy;
+    float* vz;
+    uint32_t* id;
+    int64_t n;
+    int nx, ny, nz;
+    uint32_t xmaxf, ymaxf, zmaxf;
+    int periodic, init, has_b;
+    const uint8_t* cellfree;  // (nx-1)(ny-1)(nz-1): the cell has a FREE corner
+    const float* Exf;         // (nx+1) ny nz
+    const float* Eyf;         // nx (ny+1) nz
+    const float* Ezf;         // nx ny (nz+1)
+    float hq, tx, ty, tz, sx, sy, sz;
+    float cx, cy, cz;         // dt / dx, dt / dy, dt / dz
+    unsigned long long* rho;  // deposit (self-consistent runs) or null
+    uint32_t coll_threshold;
+    uint32_t species;
+    uint64_t seed, step;
+    uint32_t* cand;
+    float4* cand_rec;
+    Counters* cnt;
+    int slot, fold_slot;
+};
+
+struct Set3Geom {
+    double xmax, ymax, zmax, dx, dy, dz;
+};
+
+struct Solve3Args {
+    int nx, ny, nz, nsp;
+    const int8_t* mask;  // nonzero: fixed (Dirichlet) node
+    const double* voltage;
+    double *u, *b, *r, *p, *qv, *part;
+    const unsigned long long* rho_fixed[kMaxSpecies];
+    double rho_weight[kMaxSpecies];  // charge * 2^-42
+    const double* rho64;             // charge density [C/m^3] instead of the deposits, or null
+    double rho_scale;                // macroparticle_factor / (dV eps0), or 1 / eps0 with rho64
+    double ix2, iy2, iz2;            // 1 / h^2 per axis
+    double tol;
+    int max_iter, clear_rho;
+    unsigned* bar;
+    int* err;
+    SolveStatus* status;
+};
+
+
 struct GridBarrier {
     unsigned int count;
     unsigned int gen;

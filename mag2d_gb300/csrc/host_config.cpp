@@ -251,7 +251,14 @@ Param make_param(const KeyValueConfig& c)
         p.u_segments.push_back(c.get("u_segment_" + std::to_string(k), p.u_ring));
 
     if (p.x_sampl < 2 || p.z_sampl < 2) throw Error(-1, "Param: x_sampl and z_sampl must be at least 2");
-    if (p.coord == CARTESIAN3D) throw Error(-1, "Param: the CARTESIAN3D path is not part of this library");
+    if (p.coord == CARTESIAN3D) {
+        // the 3D grid's own spacing and cell volume (the 2D formula above
+        // derives dy from V; Field3D takes dy as a grid spacing)
+        if (p.y_sampl < 2) throw Error(-1, "Param: y_sampl must be at least 2 in CARTESIAN3D");
+        p.dy = p.y_max / (p.y_sampl - 1);
+        p.idy = 1.0 / p.dy;
+        p.dV = p.dx * p.dy * p.dz;
+    }
     return p;
 }
 

@@ -43,6 +43,15 @@ int launch_push_fused(const PushArgs& a, const CollideArgs& c, const FusedSteps&
 int launch_source_refresh(const SourceArgs& a, float vsig, cudaStream_t s);
 int launch_source_step(const SourceArgs& a, const CollideArgs& c, int* offs, long long* total, cudaStream_t s);
 int launch_source_append(const SourceArgs& a, const int* offs, const SourceAppend& t, cudaStream_t s);
+// the 3D Cartesian path
+int launch_push3d(const Push3Args& a, int sm_count, cudaStream_t s);
+int launch_deposit3d(const Push3Args& a, cudaStream_t s);
+int launch_faces3d(const double* u, int nx, int ny, int nz, double dx, double dy, double dz, float* Exf, float* Eyf,
+                   float* Ezf, cudaStream_t s);
+int launch_set_particles3d(const double* staged, int64_t n, const Set3Geom& g, uint32_t* x, uint32_t* y, uint32_t* z,
+                           float* vx, float* vy, float* vz, uint32_t* id, cudaStream_t s);
+int solve3d_blocks(int sm_count);
+int launch_solve3d(const Solve3Args& a, int nblocks, cudaStream_t s);
 int launch_deposit(const PushArgs& a, cudaStream_t s);
 int launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
 // ADVANCE_MULTICOLL step of one species (multicoll.cu); ttd = time to the next

@@ -68,6 +68,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
         sm_count = 1;
     config_path = config;
     p = make_param(KeyValueConfig::from_file(config));
+    if (p.coord == CARTESIAN3D) throw Error(-1, "coord = CARTESIAN3D: use the 3D handle (mag3d_create)");
     if (p.mover == ADVANCE_LEAPFROG)
         throw Error(-1, "mover ADVANCE_LEAPFROG is not provided by this library (ADVANCE_BORIS, ADVANCE_MULTICOLL)");
     multicoll = p.mover == ADVANCE_MULTICOLL;
@@ -543,7 +544,13 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
 }
 
 // Speclist (pic.cpp:27-80) and lifetime_init (particles.cpp:142-206)
-void Sim::setup_species()
+void Sim::setup_species() { build_species(species_prm, inters, (size_t)nx * nz, stream, sp, d_inter, d_tables); }
+
+// Species states, null-collision rates and the device interaction list of a
+// species_conf (Speclist, src/pic.cpp:30-110): shared by the 2D and 3D runs.
+void build_species(const std::vector<SpeciesParams>& species_prm, std::vector<InteractionParams>& inters,
+                   size_t grid_nodes, cudaStream_t stream, std::vector<SpeciesState>& sp, DevArray<InterDev>& d_inter,
+                   DevArray<double>& d_tables)
 {
     const int ns = (int)species_prm.size();
     sp.resize(ns);
@@ -558,7 +565,7 @@ void Sim::setup_species()
         S.rates.assign(ns, 0.0);
         S.cnt.alloc(1);
         S.cnt.zero(stream);
-        S.rho.alloc((size_t)nx * nz);
+        S.rho.alloc(grid_nodes);
         S.rho.zero(stream);
     }
     std::vector<InterDev> idev;

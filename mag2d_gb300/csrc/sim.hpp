@@ -126,6 +126,10 @@ struct SolverLevels {
     double k2 = 1.0;
 };
 
+void build_species(const std::vector<SpeciesParams>& species_prm, std::vector<InteractionParams>& inters,
+                   size_t grid_nodes, cudaStream_t stream, std::vector<SpeciesState>& sp, DevArray<InterDev>& d_inter,
+                   DevArray<double>& d_tables);
+
 class Sim {
 public:
     Sim(const std::string& config, const std::string& species_conf, const SimOptions& opts);

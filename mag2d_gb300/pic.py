@@ -438,3 +438,87 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Pic3D:
+    """The 3D Cartesian run (coord = CARTESIAN3D): ElMag3D + Species<CARTESIAN3D>
+    of the reference (src/fields3d.cpp, src/species3d.cpp, src/Field3D.hpp) on
+    the GPU.  Arrays of nodes are (nx, ny, nz), z fastest."""
+
+    def __init__(self, config, species_conf, *, seed: int = 1, device: int = 0, poisson_tol: float = 0.0,
+                 poisson_max_iter: int = 0, capacity_hint: int = 0):
+        opts = MagOpts(device=device, seed=seed, poisson_tol=poisson_tol, poisson_max_iter=poisson_max_iter,
+                       capacity_hint=capacity_hint)
+        h = ctypes.c_void_p()
+        check(lib().mag3d_create(str(config).encode(), str(species_conf).encode(), ctypes.byref(opts),
+                                 ctypes.byref(h)))
+        self.h = h
+        dims = (ctypes.c_int * 3)()
+        sp = np.zeros(3)
+        self.nspecies = check(lib().mag3d_grid(self.h, dims, _dp(sp)))
+        self.shape = (dims[0], dims[1], dims[2])
+        self.spacing = tuple(sp)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().mag3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_particles(self, species: int, x, y, z, vx, vy, vz) -> None:
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z, vx, vy, vz)]
+        check(lib().mag3d_set_particles(self.h, species, len(arrs[0]), *[_dp(a) for a in arrs]))
+
+    def particles(self, species: int) -> dict:
+        cap = max(int(self.diag(species)["n_live"]), 1)
+        n = ctypes.c_int64()
+        arrs = {k: np.zeros(cap) for k in ("x", "y", "z", "vx", "vy", "vz")}
+        ids = np.zeros(cap, dtype=np.uint32)
+        check(lib().mag3d_get_particles(self.h, species, cap, *[_dp(arrs[k]) for k in ("x", "y", "z", "vx", "vy", "vz")],
+                                        ids.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(n)))
+        out = {k: v[: n.value].copy() for k, v in arrs.items()}
+        out["id"] = ids[: n.value].copy()
+        return out
+
+    def advance_init(self) -> None:
+        check(lib().mag3d_advance_init(self.h))
+
+    def advance(self, n: int = 1) -> None:
+        check(lib().mag3d_advance(self.h, n))
+
+    def solve(self, rho: np.ndarray | None = None) -> dict:
+        """ElMag3D::solve of a charge density [C/m^3] (nx, ny, nz), or of the deposits."""
+        info = MagSolveInfo()
+        r = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64)
+        rc = lib().mag3d_solve(self.h, _dp(r) if r is not None else None, ctypes.byref(info))
+        if rc not in (0, -4):
+            check(rc)
+        return {"iterations": info.iterations, "residual": info.residual, "status": info.status}
+
+    def field(self, which: int = MAG_U) -> np.ndarray:
+        out = np.zeros(self.shape)
+        check(lib().mag3d_get_field(self.h, which, _dp(out)))
+        return out
+
+    @property
+    def u(self) -> np.ndarray:
+        return self.field(MAG_U)
+
+    def rho_fixed(self, species: int) -> np.ndarray:
+        out = np.zeros(self.shape, dtype=np.int64)
+        check(lib().mag3d_get_rho_fixed(self.h, species, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return out
+
+    def diag(self, species: int) -> dict:
+        d = MagDiag()
+        check(lib().mag3d_diag(self.h, species, ctypes.byref(d)))
+        return {k: getattr(d, k) for k, _ in d._fields_}
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().mag3d_kernel_launches(self.h))

@@ -351,10 +351,38 @@ def gen_source():
     save("source.npz", steps=np.array(steps), live=np.array(live), meta=meta(cfg=cfg, species=species))
 
 
+def gen_field3d():
+    """Field3D::accumulate / interpolate / grad of the reference's header
+    (oracle/ref/field3d_harness.cpp) at random points of a 9 x 7 x 11 grid."""
+    import ctypes
+
+    L = ctypes.CDLL(str(HERE.parents[1] / "oracle" / "_ref" / "libmag3d_ref.so"))
+    rng = np.random.default_rng(33)
+    nx, ny, nz = 9, 7, 11
+    d = (1.0e-3, 1.5e-3, 0.8e-3)
+    n = 60
+    # within (n - 1.5) cells of the origin: nearer the far face the
+    # reference's grad_component reads one node past its arrays (with weight 0)
+    pts = [rng.uniform(0, (m - 1.5) * h, n) for m, h in zip((nx, ny, nz), d)]
+    pts[0][:3] = [0.0, 2 * d[0], 0.3 * d[0]]  # on the origin plane, a node plane, the clamped half cell
+    pts[2][3:6] = [0.0, 5 * d[2], 0.2 * d[2]]
+    charge = rng.uniform(-2e-19, 2e-19, n)
+    u = rng.normal(0, 1, (nx, ny, nz))
+    rho = np.zeros(nx * ny * nz)
+    interp = np.zeros(n)
+    grad = np.zeros(3 * n)
+    dp = lambda a: np.ascontiguousarray(a).ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    L.ref3d_field(nx, ny, nz, ctypes.c_double(d[0]), ctypes.c_double(d[1]), ctypes.c_double(d[2]), n,
+                  dp(pts[0]), dp(pts[1]), dp(pts[2]), dp(charge), dp(rho), dp(u), dp(interp), dp(grad))
+    save("field3d.npz", shape=np.array([nx, ny, nz]), d=np.array(d), x=pts[0], y=pts[1], z=pts[2], charge=charge,
+         u=u, rho=rho.reshape(nx, ny, nz), interp=interp, grad=grad.reshape(n, 3))
+
+
 if __name__ == "__main__":
     import sys
 
     cases = {"rng": gen_rng, "steps": gen_steps, "solves": gen_solves, "geometry": gen_geometry,
-             "params_species": gen_params_species, "particle_file": gen_particle_file, "source": gen_source}
+             "params_species": gen_params_species, "particle_file": gen_particle_file, "source": gen_source,
+             "field3d": gen_field3d}
     for name in (sys.argv[1:] or list(cases)):
         cases[name]()

@@ -224,3 +224,40 @@ def test_source_golden_fixture():
     assert abs(rec[:, 3].std() / vsig - 1) < 0.1 and abs(rec[:, 5].std() / vsig - 1) < 0.1
     live = g["live"]
     assert np.all(np.diff(live) > 0) and live[-1] < 1.05 * sp["density"] * V
+
+
+def test_field3d_oracle_pinned():
+    """The 3D oracle's accumulate / interpolate / grad against the reference's
+    own Field3D header (golden vectors of oracle/ref/field3d_harness.cpp)."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parents[1] / "oracle"))
+    import mag3d_oracle as o
+
+    g = np.load(GOLDEN / "field3d.npz")
+    shape, d = tuple(int(v) for v in g["shape"]), tuple(g["d"])
+    rho = o.accumulate(shape, d, g["charge"], g["x"], g["y"], g["z"])
+    assert np.abs(rho - g["rho"]).max() <= 1e-13 * np.abs(g["rho"]).max()
+    it = o.interpolate(g["u"], d, g["x"], g["y"], g["z"])
+    assert np.abs(it - g["interp"]).max() <= 1e-13 * np.abs(g["u"]).max()
+    gr = o.grad(g["u"], d, g["x"], g["y"], g["z"])
+    assert np.abs(gr - g["grad"]).max() <= 1e-13 * np.abs(g["grad"]).max()
+
+
+def test_oracle3d_solve_satisfies_the_7_point_equations():
+    pytest.importorskip("scipy")
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parents[1] / "oracle"))
+    import mag3d_oracle as o
+
+    shape, d = (11, 9, 13), (1e-3, 1.2e-3, 0.9e-3)
+    fixed, volt = o.geometry3d(*shape)
+    rho = np.random.default_rng(3).normal(0, 1e-8, shape)
+    u = o.solve(rho, fixed, volt, d)
+    assert np.array_equal(u[fixed], volt[fixed])
+    lap = np.zeros(shape)
+    for a in range(3):
+        lap[1:-1, 1:-1, 1:-1] += (np.roll(u, 1, a) - 2 * u + np.roll(u, -1, a))[1:-1, 1:-1, 1:-1] / d[a] ** 2
+    res = (lap + rho / o.EPS0)[~fixed]
+    assert np.abs(res).max() <= 1e-9 * np.abs(rho / o.EPS0).max()
