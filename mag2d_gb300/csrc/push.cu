@@ -337,11 +337,15 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
     }
     const int64_t n = a.n;
     const int64_t ngroups = (n + VEC - 1) / VEC;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // each block takes one contiguous range of groups: particles sorted by
+    // cell then keep a block's field faces and deposit nodes local (L1, L2)
+    const int64_t per_block = ((ngroups + gridDim.x - 1) / gridDim.x + blockDim.x - 1) / blockDim.x * blockDim.x;
+    const int64_t gbeg = (int64_t)blockIdx.x * per_block, gend = min(ngroups, gbeg + per_block);
     const bool coll = a.coll_threshold != 0u;
     unsigned live = 0, removed = 0;
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g - threadIdx.x < ngroups; g += stride) {
-        const bool act = g < ngroups;
+    for (int64_t g0 = gbeg; g0 < gend; g0 += blockDim.x) {
+        const int64_t g = g0 + threadIdx.x;
+        const bool act = g < gend;
         typename V::U X{}, Z{}, ID{};
         typename V::F VX{}, VY{}, VZ{};
         if (act) {
