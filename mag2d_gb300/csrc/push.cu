@@ -178,11 +178,63 @@ __device__ __forceinline__ int to_fixed_disp(float c)
 
 // One particle of the step, in registers.  Returns alive (false: removed at
 // the boundary or in a closed cell) and cand (the collision test fired).
-// step: the species' step counter; phase: the RF factor of that step.
-template <int COORD, int EMODE, bool BFIELD>
+// CIC deposit of one particle into the fixed-point grid (Field2D::accumulate):
+// four int64 corner weights summing to 2^40.
+struct GlobalDeposit {
+    unsigned long long* rho;
+    int nz;
+    __device__ __forceinline__ void add(int ic, int jc, unsigned long long U, unsigned long long V) const
+    {
+        const unsigned long long one = 1ull << kDepositShift;
+        unsigned long long* r0 = rho + (size_t)ic * nz + jc;
+        atomicAdd(r0, (one - U) * (one - V));
+        atomicAdd(r0 + nz, U * (one - V));
+        atomicAdd(r0 + 1, (one - U) * V);
+        atomicAdd(r0 + nz + 1, U * V);
+    }
+};
+
+// The same into a block's shared tile of kTileRows x kTileCols nodes whose
+// first node is (ai, aj); weights are kept as two 32-bit sums of their low and
+// high 20 bits (a tile receives at most 2^11 particles between flushes, so
+// neither sum overflows).  A particle whose corners fall outside the tile goes
+// to the grid directly.  Integer sums make the result the same either way.
+constexpr int kTileRows = 6, kTileCols = 40;
+struct TileDeposit {
+    unsigned* lo;
+    unsigned* hi;
+    int ai, aj;
+    GlobalDeposit g;
+    __device__ __forceinline__ void add(int ic, int jc, unsigned long long U, unsigned long long V) const
+    {
+        const int r = ic - ai, c = jc - aj;
+        if ((unsigned)r > (unsigned)(kTileRows - 2) || (unsigned)c > (unsigned)(kTileCols - 2)) {
+            g.add(ic, jc, U, V);
+            return;
+        }
+        const unsigned long long one = 1ull << kDepositShift;
+        const unsigned long long w[4] = {(one - U) * (one - V), U * (one - V), (one - U) * V, U * V};
+        const int t[4] = {r * kTileCols + c, (r + 1) * kTileCols + c, r * kTileCols + c + 1,
+                          (r + 1) * kTileCols + c + 1};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            atomicAdd(lo + t[q], (unsigned)(w[q] & 0xFFFFFu));
+            atomicAdd(hi + t[q], (unsigned)(w[q] >> 20));
+        }
+    }
+};
+
+// no deposit (runs without a self-consistent field)
+struct NoDeposit {
+    __device__ __forceinline__ void add(int, int, unsigned long long, unsigned long long) const {}
+};
+
+// step: the species' step counter; phase: the RF factor of that step; dep:
+// where the charge of the new position goes when a.rho is set.
+template <int COORD, int EMODE, bool BFIELD, class Dep>
 __device__ __forceinline__ void step_particle(const PushArgs& a, uint32_t& x, uint32_t& z, float& vx, float& vy,
                                               float& vz, uint32_t id, uint64_t step, float phase, bool& alive,
-                                              bool& cand)
+                                              bool& cand, const Dep& dep)
 {
     // the test uses only (seed, species, id, step): computed first, off the dependency chain
     cand = a.coll_threshold != 0u && collision_test_u32(a.seed, a.species, id, step) < a.coll_threshold;
@@ -241,16 +293,8 @@ __device__ __forceinline__ void step_particle(const PushArgs& a, uint32_t& x, ui
         cand = false;
         return;
     }
-    if (a.rho != nullptr) {
-        const unsigned long long one = 1ull << kDepositShift;
-        const unsigned long long U = x - ((uint32_t)ic << kFracBits);
-        const unsigned long long V = z - ((uint32_t)jc << kFracBits);
-        unsigned long long* r0 = a.rho + (size_t)ic * a.nz + jc;
-        atomicAdd(r0, (one - U) * (one - V));
-        atomicAdd(r0 + a.nz, U * (one - V));
-        atomicAdd(r0 + 1, (one - U) * V);
-        atomicAdd(r0 + a.nz + 1, U * V);
-    }
+    if (a.rho != nullptr)
+        dep.add(ic, jc, x - ((uint32_t)ic << kFracBits), z - ((uint32_t)jc << kFracBits));
 }
 
 // Warp-aggregated append of a collision candidate: slot index and a record
@@ -342,8 +386,19 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
     const int64_t per_block = ((ngroups + gridDim.x - 1) / gridDim.x + blockDim.x - 1) / blockDim.x * blockDim.x;
     const int64_t gbeg = (int64_t)blockIdx.x * per_block, gend = min(ngroups, gbeg + per_block);
     const bool coll = a.coll_threshold != 0u;
+    // the deposit of a chunk (blockDim x VEC consecutive slots, sorted by
+    // cell) goes to a shared tile anchored near the chunk's first particle,
+    // which is added to the grid once per chunk
+    __shared__ unsigned t_lo[kTileRows * kTileCols], t_hi[kTileRows * kTileCols];
+    __shared__ int anchor[2][2];
+    const bool tiled = a.rho != nullptr;
+    if (tiled) {
+        for (int t = threadIdx.x; t < kTileRows * kTileCols; t += blockDim.x) t_lo[t] = t_hi[t] = 0u;
+        if (threadIdx.x == 0) anchor[1][0] = anchor[1][1] = 0;
+    }
     unsigned live = 0, removed = 0;
-    for (int64_t g0 = gbeg; g0 < gend; g0 += blockDim.x) {
+    int par = 0;
+    for (int64_t g0 = gbeg; g0 < gend; g0 += blockDim.x, par ^= 1) {
         const int64_t g = g0 + threadIdx.x;
         const bool act = g < gend;
         typename V::U X{}, Z{}, ID{};
@@ -356,6 +411,22 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
             VZ = V::ldf(a.vz, g);
             if (coll) ID = V::ldu(a.id, g);
         }
+        TileDeposit dep{t_lo, t_hi, 0, 0, GlobalDeposit{a.rho, a.nz}};
+        if (tiled) {
+            if (threadIdx.x == 0) {
+                const uint32_t x0 = V::at(X, 0), z0 = V::at(Z, 0);
+                if (act && x0 != kDead) {
+                    anchor[par][0] = min((int)(x0 >> kFracBits), a.nx - 2) - 2;
+                    anchor[par][1] = min((int)(z0 >> kFracBits), a.nz - 2) - kTileCols / 4;
+                } else {
+                    anchor[par][0] = anchor[par ^ 1][0];
+                    anchor[par][1] = anchor[par ^ 1][1];
+                }
+            }
+            __syncthreads();
+            dep.ai = anchor[par][0];
+            dep.aj = anchor[par][1];
+        }
         bool cand[VEC];
 #pragma unroll
         for (int j = 0; j < VEC; ++j) {
@@ -364,11 +435,23 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
             uint32_t& x = V::at(X, j);
             if (!act || k >= n || x == kDead) continue;
             bool al;
-            step_particle<COORD, EMODE, BFIELD>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j), V::at(VZ, j),
-                                                V::at(ID, j), a.step, a.phase, al, cand[j]);
+            step_particle<COORD, EMODE, BFIELD, TileDeposit>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j),
+                                                             V::at(VZ, j), V::at(ID, j), a.step, a.phase, al,
+                                                             cand[j], dep);
             if (!al) x = kDead;
             live += al;
             removed += !al;
+        }
+        if (tiled) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < kTileRows * kTileCols; t += blockDim.x) {
+                const unsigned lo = t_lo[t], hi = t_hi[t];
+                if (lo | hi) {
+                    t_lo[t] = t_hi[t] = 0u;
+                    const int i = dep.ai + t / kTileCols, jj = dep.aj + t % kTileCols;
+                    atomicAdd(a.rho + (size_t)i * a.nz + jj, ((unsigned long long)hi << 20) + lo);
+                }
+            }
         }
         if (act) {
             V::stu(a.x, g, X);
@@ -446,7 +529,8 @@ __global__ void __launch_bounds__(256, 3) k_push_fused(const __grid_constant__ P
 #pragma unroll 1
         for (int q = 0; q < K; ++q) {
             bool al, cand;
-            step_particle<COORD, EMODE, BFIELD>(a, x, z, v[0], v[1], v[2], id, a.step + q, fs.phase[q], al, cand);
+            step_particle<COORD, EMODE, BFIELD, NoDeposit>(a, x, z, v[0], v[1], v[2], id, a.step + q, fs.phase[q], al,
+                                                           cand, NoDeposit{});
             if (!al) {
                 x = kDead;
                 ++removed;
@@ -551,8 +635,9 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>())
                 uint32_t& x = V::at(X, j);
                 if (!act || k >= n || x == kDead) continue;
                 bool al;
-                step_particle<COORD, EMODE, BFIELD>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j), V::at(VZ, j),
-                                                    V::at(ID, j), a.step, a.phase, al, cand[j]);
+                step_particle<COORD, EMODE, BFIELD, GlobalDeposit>(a, x, V::at(Z, j), V::at(VX, j), V::at(VY, j),
+                                                                   V::at(VZ, j), V::at(ID, j), a.step, a.phase, al,
+                                                                   cand[j], GlobalDeposit{a.rho, a.nz});
                 if (!al) x = kDead;
                 live += al;
                 removed += !al;
