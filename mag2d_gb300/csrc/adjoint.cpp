@@ -72,6 +72,14 @@ AdjointResult Adjoint::run(Sim& sim, const AdjointConfig& cfg)
     if (cfg.nsteps == 0) throw Error(-1, "adjoint run: nsteps must be positive");
     if (!sim.p.magnetic_field_const) throw Error(-1, "adjoint run: a magnetic field table is not supported (constant B only)");
     if (sim.p.use_source) throw Error(-1, "adjoint run: particle sources (use_source) are not supported");
+    // checkpoints copy and restore u: every solve of the run computes every node
+    sim.ensure_full_u();
+    struct RowsGuard {
+        Sim& s;
+        bool old;
+        ~RowsGuard() { s.partial_rows = old; }
+    } guard{sim, sim.partial_rows};
+    sim.partial_rows = false;
     if (sim.emode == 2) throw Error(-1, "adjoint run: RF fields are not supported (static and self-consistent fields only)");
     for (auto& S : sim.sp)
         if (S.threshold != 0)

@@ -228,6 +228,11 @@ struct GreenArgs {
     double* list_b;
     double* part;
     int nchunks;
+    // rows != null: compute only the free nodes within two nodes of a charged
+    // one (rows / row_count in the list's tile layout, charged: one byte per node)
+    int* rows;
+    int* row_count;
+    uint8_t* charged;
 };
 
 struct SolveStatus {

@@ -81,6 +81,9 @@ int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* E
 int green_chunks(long long nn, int sm_count);
 // Direct solve with the precomputed inverse (GreenArgs).
 int launch_green_solve(const SolveArgs& a, const GreenArgs& g, cudaStream_t s);
+// the product (and sum) of the last right-hand side again, every node or the
+// rows of g (the solve's list must be unchanged since)
+int launch_green_product(const SolveArgs& a, const GreenArgs& g, bool partial, cudaStream_t s);
 int launch_load_disk(uint32_t* x, uint32_t* z, float* vx, float* vy, float* vz, uint32_t* id, int64_t n,
                      uint32_t id0, int kind, double cx, double cz, double radius, double zlo, double zhi,
                      double x0, double z0, double dx, double dz, double xmax, double zmax, double vsig,

@@ -625,12 +625,16 @@ __device__ __forceinline__ double green_rhs_node(const SolveArgs& a, long long k
 // entries of its tile of kGreenTile nodes, in node order, to list slots
 // [t kGreenTile, t kGreenTile + tile_count[t]).
 __global__ void __launch_bounds__(kGreenTile) k_green_rhs(const SolveArgs a, bool dirichlet, int* __restrict__ list_j,
-                                                          double* __restrict__ list_b, int* __restrict__ tile_count)
+                                                          double* __restrict__ list_b, int* __restrict__ tile_count,
+                                                          uint8_t* __restrict__ charged)
 {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the previous kernel's results (launched with PDL)
+    asm volatile("griddepcontrol.launch_dependents;");
     __shared__ int wcount[kGreenTile / 32];
     const long long nn = (long long)a.nx * a.nz;
     const long long k = (long long)blockIdx.x * kGreenTile + threadIdx.x;
     const double b = k < nn ? green_rhs_node(a, k, dirichlet) : 0.0;
+    if (charged && k < nn) charged[k] = b != 0.0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned m = __ballot_sync(0xffffffffu, b != 0.0);
     if (lane == 0) wcount[warp] = __popc(m);
@@ -652,40 +656,60 @@ __global__ void __launch_bounds__(kGreenTile) k_green_rhs(const SolveArgs a, boo
 // part[c][i] = sum over the list entries q of chunk c of G[j_q][i] b_q, in
 // list order; the list is the tiles' entries one after the other (L in all),
 // chunk c of nchunks holds entries [c L / nchunks, (c+1) L / nchunks).
-__global__ void __launch_bounds__(256) k_green_gemv(const double* __restrict__ G, const int* __restrict__ list_j,
-                                                    const double* __restrict__ list_b,
-                                                    const int* __restrict__ tile_count, int ntiles, long long nn,
-                                                    double* __restrict__ part)
+// position q of a list stored tile by tile (tile t's entries at t kGreenTile,
+// start[] the first position of every tile)
+__device__ __forceinline__ long long tile_slot(const int* start, int ntiles, int q)
 {
-    __shared__ double sb[256];
-    __shared__ int sj[256];
-    __shared__ int start[kGreenMaxTiles + 1];
+    int lo = 0, hi = ntiles - 1;  // last tile whose first entry is <= q
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return (long long)lo * kGreenTile + (q - start[lo]);
+}
+
+__device__ __forceinline__ void tile_starts(const int* __restrict__ count, int ntiles, int* start)
+{
     if (threadIdx.x == 0) {
         int acc = 0;
         for (int t = 0; t < ntiles; ++t) {
             start[t] = acc;
-            acc += tile_count[t];
+            acc += count[t];
         }
         start[ntiles] = acc;
     }
+}
+
+// rows: null for every node, else the nodes to compute (tile layout, counts
+// in row_count); part is indexed by the row's position in that list
+__global__ void __launch_bounds__(256) k_green_gemv(const double* __restrict__ G, const int* __restrict__ list_j,
+                                                    const double* __restrict__ list_b,
+                                                    const int* __restrict__ tile_count, int ntiles, long long nn,
+                                                    const int* __restrict__ rows, const int* __restrict__ row_count,
+                                                    double* __restrict__ part)
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the previous kernel's results (launched with PDL)
+    asm volatile("griddepcontrol.launch_dependents;");
+    __shared__ double sb[256];
+    __shared__ int sj[256];
+    __shared__ int start[kGreenMaxTiles + 1], rstart[kGreenMaxTiles + 1];
+    tile_starts(tile_count, ntiles, start);
+    if (rows) tile_starts(row_count, ntiles, rstart);
     __syncthreads();
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long R = rows ? rstart[ntiles] : nn;
+    if ((long long)blockIdx.x * blockDim.x >= R) return;  // uniform per block
+    const bool row = r < R;
+    const long long i = !row ? 0 : rows ? rows[tile_slot(rstart, ntiles, (int)r)] : r;
     const long long L = start[ntiles], nch = gridDim.y;
     const long long q0 = L * blockIdx.y / nch, q1 = L * (blockIdx.y + 1) / nch;
-    const bool row = i < nn;
-    const double* __restrict__ gi = G + (row ? i : 0);
+    const double* __restrict__ gi = G + i;
     double acc = 0.0;
     for (long long t0 = q0; t0 < q1; t0 += 256) {
         const int total = (int)min(256LL, q1 - t0);
         if (threadIdx.x < total) {
-            const int q = (int)(t0 + threadIdx.x);
-            int lo = 0, hi = ntiles - 1;  // last tile whose first entry is <= q
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (start[mid] <= q) lo = mid;
-                else hi = mid - 1;
-            }
-            const long long slot = (long long)lo * kGreenTile + (q - start[lo]);
+            const long long slot = tile_slot(start, ntiles, (int)(t0 + threadIdx.x));
             sj[threadIdx.x] = list_j[slot];
             sb[threadIdx.x] = list_b[slot];
         }
@@ -703,18 +727,66 @@ __global__ void __launch_bounds__(256) k_green_gemv(const double* __restrict__ G
         }
         __syncthreads();
     }
-    if (row) part[(long long)blockIdx.y * nn + i] = acc;
+    if (row) part[(long long)blockIdx.y * nn + r] = acc;
+}
+
+// the nodes a particle kernel reads the potential of: every free node within
+// two nodes (in i and j) of a node with charge, tile by tile in node order
+__global__ void __launch_bounds__(kGreenTile) k_green_rows(int nx, int nz, const int8_t* __restrict__ mask,
+                                                           const uint8_t* __restrict__ charged,
+                                                           int* __restrict__ rows, int* __restrict__ row_count)
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the previous kernel's results (launched with PDL)
+    asm volatile("griddepcontrol.launch_dependents;");
+    __shared__ int wcount[kGreenTile / 32];
+    const long long nn = (long long)nx * nz;
+    const long long k = (long long)blockIdx.x * kGreenTile + threadIdx.x;
+    bool need = false;
+    if (k < nn && !is_fixed(mask[k])) {
+        const int i = (int)(k / nz), j = (int)(k - (long long)i * nz);
+        for (int di = -2; di <= 2 && !need; ++di) {
+            const int ii = i + di;
+            if (ii < 0 || ii >= nx) continue;
+            for (int dj = -2; dj <= 2; ++dj) {
+                const int jj = j + dj;
+                if (jj >= 0 && jj < nz && charged[(long long)ii * nz + jj]) {
+                    need = true;
+                    break;
+                }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (lane == 0) wcount[warp] = __popc(m);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < kGreenTile / 32; ++w) {
+        const int c = wcount[w];
+        before += w < warp ? c : 0;
+        total += c;
+    }
+    if (need) rows[(long long)blockIdx.x * kGreenTile + before + __popc(m & ((1u << lane) - 1u))] = (int)k;
+    if (threadIdx.x == 0) row_count[blockIdx.x] = total;
 }
 
 __global__ void __launch_bounds__(64) k_green_sum(const SolveArgs a, const double* __restrict__ part, int nchunks,
-                                                  const double* __restrict__ u_vac)
+                                                  const double* __restrict__ u_vac, const int* __restrict__ rows,
+                                                  const int* __restrict__ row_count, int ntiles)
 {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the previous kernel's results (launched with PDL)
+    asm volatile("griddepcontrol.launch_dependents;");
+    __shared__ int rstart[kGreenMaxTiles + 1];
     const long long nn = (long long)a.nx * a.nz;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (long long)gridDim.x * blockDim.x) {
+    if (rows) tile_starts(row_count, ntiles, rstart);
+    __syncthreads();
+    const long long R = rows ? rstart[ntiles] : nn;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < R; r += (long long)gridDim.x * blockDim.x) {
+        const long long k = rows ? rows[tile_slot(rstart, ntiles, (int)r)] : r;
         if (is_fixed(a.mask[k])) continue;
         double p[kGreenMaxChunks];
 #pragma unroll
-        for (int c = 0; c < kGreenMaxChunks; ++c) p[c] = c < nchunks ? part[(long long)c * nn + k] : 0.0;
+        for (int c = 0; c < kGreenMaxChunks; ++c) p[c] = c < nchunks ? part[(long long)c * nn + r] : 0.0;
         double u = u_vac ? u_vac[k] : 0.0;
 #pragma unroll
         for (int c = 0; c < kGreenMaxChunks; ++c)
@@ -731,6 +803,8 @@ __global__ void __launch_bounds__(64) k_green_sum(const SolveArgs a, const doubl
 
 __global__ void k_faces(const double* __restrict__ u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf)
 {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the previous kernel's results (launched with PDL)
+    asm volatile("griddepcontrol.launch_dependents;");
     const double idx = 1.0 / dx, idz = 1.0 / dz;
     const unsigned n1 = (unsigned)((nx + 1) * nz), n2 = (unsigned)(nx * (nz + 1));
     for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n1 + n2; q += gridDim.x * blockDim.x) {
@@ -785,18 +859,60 @@ int green_chunks(long long nn, int sm_count)
     return (int)std::max<long long>(1, std::min<long long>(kGreenMaxChunks, (8LL * sm_count + rows - 1) / rows));
 }
 
+// A launch with programmatic stream serialisation: the kernel may be scheduled
+// while the previous one on the stream finishes, and waits for it
+// (griddepcontrol.wait) before it reads anything that one wrote.
+template <class... KArgs, class... Args>
+void pdl_launch(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 int launch_green_solve(const SolveArgs& a, const GreenArgs& g, cudaStream_t s)
 {
     const long long nn = (long long)a.nx * a.nz;
     const int ntiles = (int)((nn + kGreenTile - 1) / kGreenTile);
-    k_green_rhs<<<ntiles, kGreenTile, 0, s>>>(a, g.u_vac == nullptr, g.list_j, g.list_b, g.tile_count);
-    k_green_gemv<<<dim3((unsigned)((nn + 255) / 256), (unsigned)g.nchunks), 256, 0, s>>>(
-        g.G, g.list_j, g.list_b, g.tile_count, ntiles, nn, g.part);
-    const unsigned g1 = (unsigned)std::min<long long>((nn + 63) / 64, 152 * 16);
-    k_green_sum<<<g1, 64, 0, s>>>(a, g.part, g.nchunks, g.u_vac);
-    int n = 3;
-    if (a.Exf) n += launch_faces(a.u, a.nx, a.nz, a.dx, a.dz, a.Exf, a.Ezf, s);
+    const bool partial = g.rows != nullptr;
+    pdl_launch(k_green_rhs, dim3(ntiles), dim3(kGreenTile), s, a, g.u_vac == nullptr, g.list_j, g.list_b,
+               g.tile_count, partial ? g.charged : (uint8_t*)nullptr);
+    int n = 1;
+    if (partial) {
+        pdl_launch(k_green_rows, dim3(ntiles), dim3(kGreenTile), s, a.nx, a.nz, a.mask, (const uint8_t*)g.charged,
+                   g.rows, g.row_count);
+        ++n;
+    }
+    n += launch_green_product(a, g, partial, s);
+    if (a.Exf) {
+        const long long nf = (long long)(a.nx + 1) * a.nz + (long long)a.nx * (a.nz + 1);
+        pdl_launch(k_faces, dim3((unsigned)std::min<long long>((nf + 255) / 256, 152 * 8)), dim3(256), s,
+                   (const double*)a.u, a.nx, a.nz, a.dx, a.dz, a.Exf, a.Ezf);
+        ++n;
+    }
     return n;
+}
+
+int launch_green_product(const SolveArgs& a, const GreenArgs& g, bool partial, cudaStream_t s)
+{
+    const long long nn = (long long)a.nx * a.nz;
+    const int ntiles = (int)((nn + kGreenTile - 1) / kGreenTile);
+    const int* rows = partial ? g.rows : nullptr;
+    pdl_launch(k_green_gemv, dim3((unsigned)((nn + 255) / 256), (unsigned)g.nchunks), dim3(256), s, g.G,
+               (const int*)g.list_j, (const double*)g.list_b, (const int*)g.tile_count, ntiles, nn, rows,
+               (const int*)g.row_count, g.part);
+    const unsigned g1 = (unsigned)std::min<long long>((nn + 63) / 64, 152 * 16);
+    pdl_launch(k_green_sum, dim3(g1), dim3(64), s, a, (const double*)g.part, g.nchunks, g.u_vac, rows,
+               (const int*)g.row_count, ntiles);
+    return 2;
 }
 
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s)

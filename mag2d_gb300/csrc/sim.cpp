@@ -429,6 +429,9 @@ void Sim::build_green()
     green_chunks_n = green_chunks(nn, sm_count);
     green_b.alloc(nn);
     green_j.alloc(nn + (nn + 1023) / 1024);
+    const long long ntiles = (nn + 1023) / 1024;
+    green_rows.alloc((size_t)(ntiles * 1024 + ntiles));
+    green_charged.alloc(nn);
     green_part.alloc((size_t)green_chunks_n * nn);
     green_status.alloc(1);
     // the potential of the electrodes alone
@@ -453,17 +456,40 @@ GreenArgs Sim::green_args(bool vacuum) const
     g.tile_count = green_j.p + nn;
     g.part = green_part.p;
     g.nchunks = green_chunks_n;
+    if (vacuum && partial_rows && green_rows.p) {
+        const long long ntiles = (nn + 1023) / 1024;
+        g.rows = green_rows.p;
+        g.row_count = green_rows.p + ntiles * 1024;
+        g.charged = green_charged.p;
+    }
     return g;
+}
+
+// the nodes a partial direct solve left out, from its right-hand side
+void Sim::ensure_full_u()
+{
+    if (!u_partial) return;
+    GreenArgs g = green_args(true);
+    g.rows = nullptr;
+    launches += launch_green_product(green_last, g, false, stream);
+    if (green_last.Exf)
+        launches += launch_faces(green_last.u, nx, nz, dx, dz, green_last.Exf, green_last.Ezf, stream);
+    MAG_CK(cudaGetLastError());
+    u_partial = false;
 }
 
 void Sim::run_solve(SolveArgs a)
 {
+    u_partial = false;  // every path below writes u (a partial direct solve sets it again)
     if (a.rho_src != 3 && direct_mode >= 0 && p.selfconsistent && !a.rf_solve) {
         if (!green_tried) build_green();
         if (green_ready()) {
             // the stored electrode potential holds for this instance's own voltages
-            launches += launch_green_solve(a, green_args(a.voltage == d_volt.p), stream);
+            const GreenArgs g = green_args(a.voltage == d_volt.p);
+            launches += launch_green_solve(a, g, stream);
             MAG_CK(cudaGetLastError());
+            u_partial = g.rows != nullptr;
+            green_last = a;
             return;
         }
     }
@@ -1132,6 +1158,7 @@ SolveStatus Sim::field_solve()
 void Sim::get_field(int which, double* out)
 {
     const size_t nn = (size_t)nx * nz;
+    if (which == 0) ensure_full_u();
     MAG_CK(cudaStreamSynchronize(stream));
     if (which == 0) u64.download(out, nn, stream);
     else if (which == 1) urf64.download(out, nn, stream);
@@ -1163,6 +1190,7 @@ void Sim::get_field(int which, double* out)
 void Sim::set_field(int which, const double* in)
 {
     const size_t nn = (size_t)nx * nz;
+    if (which == 0) u_partial = false;
     if (which == 0) u64.upload(in, nn, stream);
     else if (which == 1) urf64.upload(in, nn, stream);
     else if (which == 2) {
@@ -1251,6 +1279,7 @@ void Sim::dist_reset()
 // the charge deposit of the particles' current positions.
 void Sim::dist_sample()
 {
+    ensure_full_u();
     if (dist.size() != sp.size()) dist_reset();
     const size_t nn = (size_t)nx * nz;
     if (rho_scratch.n < nn) rho_scratch.alloc(nn);

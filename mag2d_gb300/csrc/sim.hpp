@@ -178,6 +178,14 @@ public:
     DevArray<double> stage64;  // host particle arrays on their way to the SoA state
     DevArray<double> green, green_vac, green_b, green_part;
     DevArray<int> green_j;  // compacted right-hand side (node, value) and the per-tile counts
+    // a step's solve computes only the nodes near charge (the particles'
+    // cells); the rest of u follows on demand from the same right-hand side
+    DevArray<int> green_rows;
+    DevArray<uint8_t> green_charged;
+    SolveArgs green_last{};
+    bool u_partial = false;
+    bool partial_rows = true;  // off: every direct solve computes every node
+    void ensure_full_u();
     DevArray<SolveStatus> green_status;
     int green_chunks_n = 0;
     GreenArgs green_args(bool vacuum) const;

@@ -298,6 +298,31 @@ def test_sort_does_not_change_results(m, tmp_path):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
+def test_inverse_solve_partial_rows_cover_the_particles(m, tmp_path):
+    """A step's direct solve computes only the nodes within two of a charged
+    node; reading u (which completes it) every step must not change a single
+    particle: every face the particles read comes from computed nodes."""
+    from cases import penning_rz
+
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=20000)
+    out = []
+    for read_every_step in (False, True):
+        pic = m.Pic(cpath, spath, seed=4, direct_solve=1)
+        pic.speclist[0].set_particles(*parts)
+        pic.advance_init()
+        for _ in range(40):
+            pic.advance(1)
+            if read_every_step:
+                _ = pic.field.u
+        g = pic.speclist[0].particles()
+        order = np.argsort(g["id"])
+        out.append(({k: v[order] for k, v in g.items()}, pic.field.u))
+        pic.close()
+    for k in ("id", "x", "z", "vx", "vy", "vz"):
+        assert np.array_equal(out[0][0][k], out[1][0][k]), k
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 @pytest.mark.parametrize("case", ["multipole_rf_mcc", "penning_external"])
 @pytest.mark.parametrize("fused", [64, 7])
 def test_fused_steps_bit_identical(m, tmp_path, case, fused):
