@@ -22,7 +22,7 @@ void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector
               int& nzc, std::vector<double>& Ac);
 
 // Coarsest levels up to this many nodes are solved exactly with a dense inverse.
-constexpr long long kDenseCoarseMax = 600;
+constexpr long long kDenseCoarseMax = 200;
 
 // Level sizes: halve while both sizes are odd and >= 5 (at most max_levels
 // levels), and stop at the first level of at most kDenseCoarseMax nodes.
