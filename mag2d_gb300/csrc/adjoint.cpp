@@ -74,12 +74,18 @@ AdjointResult Adjoint::run(Sim& sim, const AdjointConfig& cfg)
     if (sim.p.use_source) throw Error(-1, "adjoint run: particle sources (use_source) are not supported");
     // checkpoints copy and restore u: every solve of the run computes every node
     sim.ensure_full_u();
+    // and every replayed step solves from the same start as the forward one
     struct RowsGuard {
         Sim& s;
-        bool old;
-        ~RowsGuard() { s.partial_rows = old; }
-    } guard{sim, sim.partial_rows};
+        bool old_rows, old_extrapolate;
+        ~RowsGuard()
+        {
+            s.partial_rows = old_rows;
+            s.extrapolate_u = old_extrapolate;
+        }
+    } guard{sim, sim.partial_rows, sim.extrapolate_u};
     sim.partial_rows = false;
+    sim.extrapolate_u = false;
     if (sim.emode == 2) throw Error(-1, "adjoint run: RF fields are not supported (static and self-consistent fields only)");
     for (auto& S : sim.sp)
         if (S.threshold != 0)

@@ -322,6 +322,8 @@ struct SolveArgs {
     double* b;              // FP64 right-hand side (scratch)
     int rf_solve;           // boundary_solve_rf: FIXED -> 0, FIXED_RF -> voltage
     int rho_src;            // 0 none, 1 fixed-point species accumulators, 2 FP64 array, 3 unit right-hand side
+    double* u_prev;         // non-null: start from u <- 2 u - u_prev on the free nodes (u_prev <- u) ...
+    int* u_prev_valid;      // ... once *u_prev_valid is set (the first solve only records u_prev and sets it)
     long long unit_node;    // rho_src 3: b = 1 at this node, 0 elsewhere (columns of the inverse)
     const unsigned long long* rho_fixed[kMaxSpecies];
     double rho_weight[kMaxSpecies];  // charge * 2^-40

@@ -431,6 +431,18 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
     const int nx = a.nx, nz = a.nz;
     const unsigned nn = (unsigned)(nx * nz);
     bool ok = true;
+    // 0. start of a step's solve: the linear extrapolation of the last two solutions
+    if (a.u_prev) {
+        const bool valid = *((volatile const int*)a.u_prev_valid) != 0;
+        for (unsigned k = t.tid; k < nn; k += t.nthreads) {
+            if (is_fixed(a.mask[k])) continue;
+            const double u = a.u[k];
+            if (valid) a.u[k] = 2.0 * u - a.u_prev[k];
+            a.u_prev[k] = u;
+        }
+        ok = t.sync();
+        if (t.tid == 0) *a.u_prev_valid = 1;
+    }
     // 1. right-hand side and Dirichlet values (boundary_solve / boundary_solve_rf)
     const FastDiv dnz((unsigned)nz);
     for (unsigned k = t.tid; k < nn; k += t.nthreads) {

@@ -560,6 +560,16 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
     a.omega = lv.nlev == 1 ? (float)(2.0 / (1.0 + std::sin(kPi / std::max(nx, nz)))) : 1.f;
     a.tol = poisson_tol;
     a.max_outer = lv.nlev == 1 ? 20 * poisson_max_iter : poisson_max_iter;
+    if (extrapolate_u && rho_src == 1 && clear_rho && !rf_solve) {
+        // a step's solve starts from 2 u_n - u_(n-1)
+        if (!u_prev.p) {
+            u_prev.alloc((size_t)nx * nz);
+            u_prev_valid.alloc(1);
+            u_prev_valid.zero(stream);
+        }
+        a.u_prev = u_prev.p;
+        a.u_prev_valid = u_prev_valid.p;
+    }
     a.Exf = rf_solve ? Exf_rf.p : Exf.p;
     a.Ezf = rf_solve ? Ezf_rf.p : Ezf.p;
     a.red = red.p;
@@ -1191,6 +1201,7 @@ void Sim::set_field(int which, const double* in)
 {
     const size_t nn = (size_t)nx * nz;
     if (which == 0) u_partial = false;
+    if (which == 0 && u_prev_valid.p) u_prev_valid.zero(stream);  // no history for the next extrapolation
     if (which == 0) u64.upload(in, nn, stream);
     else if (which == 1) urf64.upload(in, nn, stream);
     else if (which == 2) {

@@ -185,6 +185,10 @@ public:
     SolveArgs green_last{};
     bool u_partial = false;
     bool partial_rows = true;  // off: every direct solve computes every node
+    // the multigrid solve of a step starts from 2 u_n - u_(n-1) (when extrapolate_u)
+    DevArray<double> u_prev;
+    DevArray<int> u_prev_valid;
+    bool extrapolate_u = true;
     void ensure_full_u();
     DevArray<SolveStatus> green_status;
     int green_chunks_n = 0;
