@@ -25,7 +25,8 @@ namespace mag {
 constexpr int kMaxSpecies = 16;
 constexpr int kMaxInteractions = 64;
 constexpr int kMaxLevels = 12;
-constexpr long long kSingleBlockNodes = 70000;  // grids (and levels) up to this size run on one block
+constexpr long long kSingleBlockNodes = 70000;  // grids up to this size run on one block
+constexpr long long kSingleBlockLevel = 4096;   // levels of a multi-block solve up to this size run on block 0
 constexpr long long kGreenMaxNodes = 20000;     // grids up to this size solve by the precomputed inverse
 constexpr int kFracBits = 20;      // fixed-point fraction of a cell in the positions
 constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis (= kFracBits)

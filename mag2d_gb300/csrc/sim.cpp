@@ -503,7 +503,7 @@ void Sim::run_solve(SolveArgs a)
         if (nblocks > 1) {
             a.l_single = lv.nlev;
             for (int l = 0; l < lv.nlev; ++l)
-                if ((long long)lv.nx[l] * lv.nz[l] <= kSingleBlockNodes) {
+                if ((long long)lv.nx[l] * lv.nz[l] <= kSingleBlockLevel) {
                     a.l_single = l;
                     break;
                 }
