@@ -384,9 +384,12 @@ __device__ void vcycle_from(const SolveArgs& a, Team& t, int l0, bool& ok)
 }
 
 // One V-cycle.  On a multi-block grid the levels from a.l_single down (at most
-// kSingleBlockNodes nodes each) run on block 0 alone, synchronised by
+// kSingleBlockLevel nodes each) run on block 0 alone, synchronised by
 // __syncthreads, while the other blocks wait at one grid barrier: a coarse
-// level has too little work to pay for the grid barriers of its sweeps.
+// level has too little work to pay for the grid barriers of its sweeps.  The
+// Galerkin levels above it are smoothed with one 4-colour sweep each way (a
+// sweep costs four grid barriers; the outer FP64 iterations do not increase).
+constexpr int kCoarseSweepsGrid = 1;
 __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
 {
     const int L = a.nlev;
@@ -401,7 +404,7 @@ __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
     const int ls = a.l_single;
     for (int l = 0; l < ls && ok; ++l) {
         if (l == 0) smooth_fine(a, t, a.nu1, false, 1.f, ok);
-        else smooth_coarse(a, t, l, a.nu1, false, ok);
+        else smooth_coarse(a, t, l, kCoarseSweepsGrid, false, ok);
         if (!ok) return;
         residual_level(a, t, l, a.lev[l].t);
         ok = t.sync();
@@ -422,7 +425,7 @@ __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
         ok = t.sync();
         if (!ok) return;
         if (l == 0) smooth_fine(a, t, a.nu2, true, 1.f, ok);
-        else smooth_coarse(a, t, l, a.nu2, true, ok);
+        else smooth_coarse(a, t, l, kCoarseSweepsGrid, true, ok);
     }
 }
 
