@@ -333,6 +333,7 @@ struct SolveArgs {
     int clear_rho;
     double mpf, dV;         // macroparticle_factor, cell volume (Cartesian scaling)
     const double* st64;     // fine stencil per row i: (w, e, c, 1/c), FP64 (4 * nx)
+    const double* rscale;   // right-hand-side scaling of rho per row i (nx), or null: computed per node
     const float* st32;      // the same in FP32 for the smoother
     double k2;              // s/n coefficient of the fine stencil
     int nlev;

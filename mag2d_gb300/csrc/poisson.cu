@@ -116,6 +116,7 @@ __device__ __forceinline__ Stencil5 fine_stencil(const SolveArgs& a, int i)
 // the reference's scaling of rho into the right-hand side of row i (fields.cpp:283-300)
 __device__ __forceinline__ double rhs_scale(const SolveArgs& a, int i)
 {
+    if (a.rscale) return a.rscale[i];  // the table holds the same expression (no FP64 division per node)
     if (a.coord == 1)
         return i > 0 ? -1.0 / kEps0d / (kPi * a.dx * a.dx * 2.0 * i * a.dz) * a.mpf
                      : -1.0 / kEps0d / (kPi * a.dx * a.dx * 0.25 * a.dz) * a.mpf;

@@ -339,6 +339,15 @@ void Sim::setup_solver()
     std::vector<float> st32(st.begin(), st.end());
     lv.st64.upload(st.data(), st.size(), stream);
     lv.st32.upload(st32.data(), st32.size(), stream);
+    // the right-hand-side scaling of rho per grid row (fields.cpp:283-300), the
+    // same expression in the same order as the device would evaluate per node
+    std::vector<double> rs(nx);
+    for (int i = 0; i < nx; ++i)
+        rs[i] = p.coord == CYLINDRICAL
+                    ? (i > 0 ? -1.0 / kEps0 / (kPi * dx * dx * 2.0 * i * dz) * p.macroparticle_factor
+                             : -1.0 / kEps0 / (kPi * dx * dx * 0.25 * dz) * p.macroparticle_factor)
+                    : -(dx * dx) / kEps0 / p.dV;
+    lv.rscale.upload(rs.data(), rs.size(), stream);
     MAG_CK(cudaStreamSynchronize(stream));
     solver_ready = true;
 }
@@ -541,6 +550,7 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
     a.mpf = p.macroparticle_factor;
     a.dV = p.dV;
     a.st64 = lv.st64.p;
+    a.rscale = lv.rscale.p;
     a.st32 = lv.st32.p;
     a.k2 = lv.k2;
     a.coarse_inv = lv.coarse_inv.p;

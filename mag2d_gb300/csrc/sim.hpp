@@ -122,6 +122,7 @@ struct SolverLevels {
     std::vector<DevArray<float>> e, r, t, coef, inv_diag;
     DevArray<float> coarse_inv;  // dense inverse of the coarsest level (column-major) or empty
     DevArray<double> st64;       // fine stencil rows (w, e, c)
+    DevArray<double> rscale;     // right-hand-side scaling of rho per row
     DevArray<float> st32;
     double k2 = 1.0;
 };
