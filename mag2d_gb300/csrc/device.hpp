@@ -334,6 +334,7 @@ struct SolveArgs {
     double mpf, dV;         // macroparticle_factor, cell volume (Cartesian scaling)
     const double* st64;     // fine stencil per row i: (w, e, c, 1/c), FP64 (4 * nx)
     const double* rscale;   // right-hand-side scaling of rho per row i (nx), or null: computed per node
+    double idx, idz;        // 1 / dx, 1 / dz
     const float* st32;      // the same in FP32 for the smoother
     double k2;              // s/n coefficient of the fine stencil
     int nlev;

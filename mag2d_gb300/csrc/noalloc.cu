@@ -209,6 +209,8 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
     a.nz = nz;
     a.dx = dx;
     a.dz = dz;
+    a.idx = 1.0 / dx;
+    a.idz = 1.0 / dz;
     a.mask = (const int8_t*)(base + o_mask);
     a.voltage = (const double*)(base + o_volt);
     a.u = u_dev;

@@ -103,6 +103,28 @@ struct FastDiv {
     }
 };
 
+// Face fields of Field2D::grad: Exf[r][j] = -(u[ic][j] - u[ic-1][j]) / dx with
+// ic = clamp(r, 1, nx-1), Ezf[i][c] = -(u[i][jc] - u[i][jc-1]) / dz with
+// jc = clamp(c, 1, nz-1); idx, idz = 1/dx, 1/dz from the host
+__device__ void faces_pass(const double* __restrict__ u, int nx, int nz, double idx, double idz, float* __restrict__ Exf,
+                           float* __restrict__ Ezf, unsigned tid, unsigned nthreads)
+{
+    const FastDiv dz((unsigned)nz), dz1((unsigned)(nz + 1));
+    const unsigned n1 = (unsigned)((nx + 1) * nz), n2 = (unsigned)(nx * (nz + 1));
+    for (unsigned q = tid; q < n1; q += nthreads) {
+        int i = (int)dz.div(q);
+        const int j = (int)(q - (unsigned)i * nz);
+        i = i < 1 ? 1 : (i > nx - 1 ? nx - 1 : i);
+        Exf[q] = (float)(-(u[(size_t)i * nz + j] - u[(size_t)(i - 1) * nz + j]) * idx);
+    }
+    for (unsigned p = tid; p < n2; p += nthreads) {
+        const int i = (int)dz1.div(p);
+        int j = (int)(p - (unsigned)i * (nz + 1));
+        j = j < 1 ? 1 : (j > nz - 1 ? nz - 1 : j);
+        Ezf[p] = (float)(-(u[(size_t)i * nz + j] - u[(size_t)i * nz + j - 1]) * idz);
+    }
+}
+
 // 5-point row of the fine operator (fields.cpp:149-238) of row i, from the
 // per-row table built on the host
 struct Stencil5 {
@@ -539,21 +561,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
         ok = t.sync();
     }
     // 3. face electric field E = -grad u for the particle kernel
-    if (ok && a.Exf != nullptr) {
-        const double idx = 1.0 / a.dx, idz = 1.0 / a.dz;
-        for (unsigned q = t.tid; q < (unsigned)((nx + 1) * nz); q += t.nthreads) {
-            int i = q / nz;
-            const int j = q % nz;
-            i = i < 1 ? 1 : (i > nx - 1 ? nx - 1 : i);
-            a.Exf[q] = (float)(-(a.u[(size_t)i * nz + j] - a.u[(size_t)(i - 1) * nz + j]) * idx);
-        }
-        for (unsigned q = t.tid; q < (unsigned)(nx * (nz + 1)); q += t.nthreads) {
-            const int i = q / (nz + 1);
-            int j = q % (nz + 1);
-            j = j < 1 ? 1 : (j > nz - 1 ? nz - 1 : j);
-            a.Ezf[q] = (float)(-(a.u[(size_t)i * nz + j] - a.u[(size_t)i * nz + j - 1]) * idz);
-        }
-    }
+    if (ok && a.Exf != nullptr) faces_pass(a.u, nx, nz, a.idx, a.idz, a.Exf, a.Ezf, t.tid, t.nthreads);
     if (t.tid == 0) {
         a.status->iterations = it;
         a.status->residual = res;
@@ -817,26 +825,11 @@ __global__ void __launch_bounds__(64) k_green_sum(const SolveArgs a, const doubl
     }
 }
 
-__global__ void k_faces(const double* __restrict__ u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf)
+__global__ void k_faces(const double* __restrict__ u, int nx, int nz, double idx, double idz, float* Exf, float* Ezf)
 {
     asm volatile("griddepcontrol.wait;" ::: "memory");  // the previous kernel's results (launched with PDL)
     asm volatile("griddepcontrol.launch_dependents;");
-    const double idx = 1.0 / dx, idz = 1.0 / dz;
-    const unsigned n1 = (unsigned)((nx + 1) * nz), n2 = (unsigned)(nx * (nz + 1));
-    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n1 + n2; q += gridDim.x * blockDim.x) {
-        if (q < n1) {
-            int i = q / nz;
-            const int j = q % nz;
-            i = i < 1 ? 1 : (i > nx - 1 ? nx - 1 : i);
-            Exf[q] = (float)(-(u[(size_t)i * nz + j] - u[(size_t)(i - 1) * nz + j]) * idx);
-        } else {
-            const unsigned p = q - n1;
-            const int i = p / (nz + 1);
-            int j = p % (nz + 1);
-            j = j < 1 ? 1 : (j > nz - 1 ? nz - 1 : j);
-            Ezf[p] = (float)(-(u[(size_t)i * nz + j] - u[(size_t)i * nz + j - 1]) * idz);
-        }
-    }
+    faces_pass(u, nx, nz, idx, idz, Exf, Ezf, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 }  // namespace
@@ -911,7 +904,7 @@ int launch_green_solve(const SolveArgs& a, const GreenArgs& g, cudaStream_t s)
     if (a.Exf) {
         const long long nf = (long long)(a.nx + 1) * a.nz + (long long)a.nx * (a.nz + 1);
         pdl_launch(k_faces, dim3((unsigned)std::min<long long>((nf + 255) / 256, 152 * 8)), dim3(256), s,
-                   (const double*)a.u, a.nx, a.nz, a.dx, a.dz, a.Exf, a.Ezf);
+                   (const double*)a.u, a.nx, a.nz, a.idx, a.idz, a.Exf, a.Ezf);
         ++n;
     }
     return n;
@@ -935,7 +928,7 @@ int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* E
 {
     const long long n = (long long)(nx + 1) * nz + (long long)nx * (nz + 1);
     const int grid = (int)std::min<long long>((n + 255) / 256, 152 * 8);
-    k_faces<<<grid, 256, 0, s>>>(u, nx, nz, dx, dz, Exf, Ezf);
+    k_faces<<<grid, 256, 0, s>>>(u, nx, nz, 1.0 / dx, 1.0 / dz, Exf, Ezf);
     return 1;
 }
 

@@ -551,6 +551,8 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
     a.dV = p.dV;
     a.st64 = lv.st64.p;
     a.rscale = lv.rscale.p;
+    a.idx = 1.0 / dx;
+    a.idz = 1.0 / dz;
     a.st32 = lv.st32.p;
     a.k2 = lv.k2;
     a.coarse_inv = lv.coarse_inv.p;
