@@ -63,11 +63,10 @@ __device__ __forceinline__ void gather3(const Push3Args& a, uint32_t x, uint32_t
     face_of(x, a.nx, ir, gx);
     face_of(y, a.ny, jr, gy);
     face_of(z, a.nz, kr, gz);
-    const long long nx = a.nx, ny = a.ny, nz = a.nz;
+    const long long ny = a.ny, nz = a.nz;
     ex = trilerp(a.Exf, ny * nz, nz, ir, jc, kc, gx, fy, fz);
     ey = trilerp(a.Eyf, (ny + 1) * nz, nz, ic, jr, kc, fx, gy, fz);
     ez = trilerp(a.Ezf, ny * (nz + 1), nz + 1, ic, jc, kr, fx, fy, gz);
-    (void)nx;
 }
 
 __device__ __forceinline__ bool move3(uint32_t& v, float cells, uint32_t maxf, bool periodic)

@@ -1,6 +1,5 @@
-// Counting sort of a species' particles by cell, with compaction of removed
-// particles (north-star layout: "SoA, counting-sorted by cell every few
-// steps").  After a sort, consecutive threads of the particle kernel touch the
+// Counting sort of a species' particles by cell every sort_interval steps,
+// with compaction of removed particles.  After a sort, consecutive threads of the particle kernel touch the
 // same few cells, so the field gather and the deposit atomics hit L1/L2
 // instead of scattering over the grid.  The order inside a cell is not
 // deterministic; nothing depends on it (random streams are keyed by particle

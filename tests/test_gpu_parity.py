@@ -1,6 +1,6 @@
 """GPU parity tests: the CUDA path through the C ABI against the oracle port.
 
-Tolerances (from the spec bar of the project):
+Tolerances:
   * deposit        — bit-exact against the oracle's fixed-point CIC deposit
   * Poisson solve  — |u_gpu - u_oracle|_inf <= 1e-9 |u_oracle|_inf
   * trajectories   — positions within 1e-5 of the domain size after 1000 steps
