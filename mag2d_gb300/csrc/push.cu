@@ -200,8 +200,12 @@ struct GlobalDeposit {
 // neither sum overflows).  A particle whose corners fall outside the tile goes
 // to the grid directly.  Integer sums make the result the same either way.
 constexpr int kTileRows = 6, kTileCols = 40;
+// Lanes add into kTileCopies interleaved copies of the tile (copy lane % 8,
+// offset by one bank each), so sorted particles of one cell in a warp
+// serialise 8 ways less on the same shared address; the flush adds the copies.
+constexpr int kTileCopies = 8, kTileStride = kTileRows * kTileCols + 1;
 struct TileDeposit {
-    unsigned* lo;
+    unsigned* lo;  // copy c of node t at c * kTileStride + t
     unsigned* hi;
     int ai, aj;
     GlobalDeposit g;
@@ -214,8 +218,9 @@ struct TileDeposit {
         }
         const unsigned long long one = 1ull << kDepositShift;
         const unsigned long long w[4] = {(one - U) * (one - V), U * (one - V), (one - U) * V, U * V};
-        const int t[4] = {r * kTileCols + c, (r + 1) * kTileCols + c, r * kTileCols + c + 1,
-                          (r + 1) * kTileCols + c + 1};
+        const int cp = (threadIdx.x & (kTileCopies - 1)) * kTileStride;
+        const int t[4] = {cp + r * kTileCols + c, cp + (r + 1) * kTileCols + c, cp + r * kTileCols + c + 1,
+                          cp + (r + 1) * kTileCols + c + 1};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             atomicAdd(lo + t[q], (unsigned)(w[q] & 0xFFFFFu));
@@ -389,11 +394,11 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
     // the deposit of a chunk (blockDim x VEC consecutive slots, sorted by
     // cell) goes to a shared tile anchored near the chunk's first particle,
     // which is added to the grid once per chunk
-    __shared__ unsigned t_lo[kTileRows * kTileCols], t_hi[kTileRows * kTileCols];
+    __shared__ unsigned t_lo[kTileCopies * kTileStride], t_hi[kTileCopies * kTileStride];
     __shared__ int anchor[2][2];
     const bool tiled = a.rho != nullptr;
     if (tiled) {
-        for (int t = threadIdx.x; t < kTileRows * kTileCols; t += blockDim.x) t_lo[t] = t_hi[t] = 0u;
+        for (int t = threadIdx.x; t < kTileCopies * kTileStride; t += blockDim.x) t_lo[t] = t_hi[t] = 0u;
         if (threadIdx.x == 0) anchor[1][0] = anchor[1][1] = 0;
     }
     unsigned live = 0, removed = 0;
@@ -445,11 +450,16 @@ __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __gr
         if (tiled) {
             __syncthreads();
             for (int t = threadIdx.x; t < kTileRows * kTileCols; t += blockDim.x) {
-                const unsigned lo = t_lo[t], hi = t_hi[t];
-                if (lo | hi) {
-                    t_lo[t] = t_hi[t] = 0u;
+                unsigned long long sum = 0;
+#pragma unroll
+                for (int c = 0; c < kTileCopies; ++c) {
+                    const int q = c * kTileStride + t;
+                    sum += ((unsigned long long)t_hi[q] << 20) + t_lo[q];
+                    t_lo[q] = t_hi[q] = 0u;
+                }
+                if (sum) {
                     const int i = dep.ai + t / kTileCols, jj = dep.aj + t % kTileCols;
-                    atomicAdd(a.rho + (size_t)i * a.nz + jj, ((unsigned long long)hi << 20) + lo);
+                    atomicAdd(a.rho + (size_t)i * a.nz + jj, sum);
                 }
             }
         }
