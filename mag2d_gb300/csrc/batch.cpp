@@ -155,14 +155,23 @@ void Batch::pack(const Layout& L, Slot& slot)
     SolveArgs* sa = reinterpret_cast<SolveArgs*>(h + L.solve_off);
     CollideArgs* ca = reinterpret_cast<CollideArgs*>(h + L.coll_off);
     std::vector<int> fill(L.push_items.size(), 0);
-    int ns = 0, nc = 0;
+    int nc = 0;
     const int chunk = push_batch_chunk(cfg.push_vec);
+    // solve blocks largest grid first, so that the small instances fill the
+    // second wave of blocks instead of starting large ones late
+    std::vector<std::pair<long long, SolveArgs>> solves;
     for (auto& sp : sims) {
         Sim& s = *sp;
         if (s.p.selfconsistent && (long long)s.nx * s.nz <= kSingleBlockNodes) {
-            sa[ns++] = s.solve_args(false, s.rho_override ? 2 : 1, true);
+            solves.emplace_back((long long)s.nx * s.nz, s.solve_args(false, s.rho_override ? 2 : 1, true));
             s.rho_override = false;
         }
+    }
+    std::stable_sort(solves.begin(), solves.end(),
+                     [](const auto& x, const auto& y) { return x.first > y.first; });
+    for (size_t q = 0; q < solves.size(); ++q) sa[q] = solves[q].second;
+    for (auto& sp : sims) {
+        Sim& s = *sp;
         const int coord = s.p.coord == CYLINDRICAL ? 1 : 0, hb = has_b_field(s) ? 1 : 0;
         int q = 0;
         for (; q < (int)L.push_items.size(); ++q)
