@@ -56,11 +56,11 @@ def _oracle_loss(m, tmp_path, volts, Bz, parts, steps, tag):
     return float(e.mean()) + (len(parts[0]) - len(live)) / len(parts[0])
 
 
-def _adjoint(m, tmp_path, n, steps, volts, Bz):
+def _adjoint(m, tmp_path, n, steps, volts, Bz, direct=0):
     from cases import penning_segments
 
     c = penning_segments(tmp_path, n=n, volts=volts, Bz=Bz, tag="adj")
-    pic = m.Pic(c[3], c[4], c[5], seed=c[6])
+    pic = m.Pic(c[3], c[4], c[5], seed=c[6], direct_solve=direct)
     g0 = pic.speclist[0].particles()
     parts = tuple(np.asarray(g0[k], dtype=np.float64) for k in ("x", "z", "vx", "vy", "vz"))
     info, grad = pic.adjoint(steps, KEYS, checkpoint=64, grad_b=True)
@@ -68,13 +68,15 @@ def _adjoint(m, tmp_path, n, steps, volts, Bz):
     return info, grad, parts
 
 
-def test_adjoint_matches_oracle_finite_differences(m, tmp_path):
+@pytest.mark.parametrize("direct", [0, -1], ids=["inverse", "multigrid"])
+def test_adjoint_matches_oracle_finite_differences(m, tmp_path, direct):
     """Central differences of the oracle (FP64, h = 1e-3 V and 1e-4 T) from the
-    same initial particles: agreement within 1e-3 relative."""
+    same initial particles: agreement within 1e-3 relative, with the forward
+    and transposed solves by the precomputed inverse or by multigrid."""
     n, steps = 20_000, 300
     volts = np.random.default_rng(7).uniform(-15.0, -5.0, 8)
     Bz = 1.0
-    info, grad, parts = _adjoint(m, tmp_path, n, steps, volts, Bz)
+    info, grad, parts = _adjoint(m, tmp_path, n, steps, volts, Bz, direct)
     assert info["n_live"] > 0.9 * info["n0"], info
     scale = np.abs(grad[:8]).max()
     assert scale > 0
