@@ -30,10 +30,17 @@ constexpr long long kBarrierSpinLimit = 20000000;  // ~seconds of __nanosleep(64
 
 // The threads that share a piece of the solve: the whole grid (synchronised
 // by a bounded grid barrier) or one block (synchronised by __syncthreads).
+//
+// The grid barrier counts arrivals on one monotonic counter (zeroed before the
+// launch): barrier number e of the launch is passed when the counter reaches
+// e * nblocks.  Thread 0 of each block adds its arrival with a release
+// reduction (no return value, no reset) and polls with acquire loads, so no
+// block waits for another block's atomic to come back.
 struct Team {
     GridBarrier* bar;
     unsigned nblocks;
     unsigned tid, nthreads;
+    unsigned epoch = 0;  // barriers passed so far (the same in every thread)
     __device__ Team(GridBarrier* b)
         : bar(b), nblocks(gridDim.x), tid(blockIdx.x * blockDim.x + threadIdx.x), nthreads(gridDim.x * blockDim.x)
     {
@@ -53,28 +60,23 @@ struct Team {
         __syncthreads();
         if (nblocks == 1) return true;
         __shared__ int s_ok;
+        ++epoch;
         if (threadIdx.x == 0) {
-            volatile unsigned* genp = &bar->gen;
-            const unsigned g = *genp;
-            __threadfence();
-            const unsigned arrived = atomicAdd(&bar->count, 1u);
+            const unsigned target = epoch * nblocks;
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&bar->count) : "memory");
             int ok = 1;
-            if (arrived == nblocks - 1) {
-                atomicExch(&bar->count, 0u);
-                __threadfence();
-                atomicAdd(&bar->gen, 1u);
-            } else {
-                long long spins = 0;
-                while (*genp == g) {
-                    if (++spins > kBarrierSpinLimit || *((volatile unsigned*)&bar->abort)) {
-                        atomicExch(&bar->abort, 1u);
-                        ok = 0;
-                        break;
-                    }
-                    __nanosleep(64);
+            long long spins = 0;
+            for (;;) {
+                unsigned c;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(&bar->count) : "memory");
+                if ((int)(c - target) >= 0) break;
+                if (++spins > kBarrierSpinLimit || *((volatile unsigned*)&bar->abort)) {
+                    atomicExch(&bar->abort, 1u);
+                    ok = 0;
+                    break;
                 }
+                __nanosleep(32);
             }
-            __threadfence();
             s_ok = ok && !*((volatile unsigned*)&bar->abort);
         }
         __syncthreads();
