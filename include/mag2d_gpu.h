@@ -263,6 +263,21 @@ int mag_print_field(mag_sim* sim, const char* path);
  * species' particles; positions outside the domain are redrawn uniformly in
  * it.  A config with particle_reload = 1 loads every species from
  * <particle_reload_dir>/particles_<name>.dat at mag_create (src/pic.cpp:138-146). */
+/* Electrode voltages (t_grid::voltage, x_sampl * z_sampl values; only the
+ * FIXED and FIXED_RF nodes' entries are used).  The RF Laplace solution and,
+ * without a self-consistent field, the static potential are solved again as
+ * in the Pic constructor (src/pic.cpp:170-186); a self-consistent run solves
+ * with them from its next step.  Not with electric_field_from_file. */
+int mag_set_electrode_voltages(mag_sim* sim, const double* v, int64_t n);
+
+/* Live particles of a species (BaseSpecies::n_particles, src/particles.hpp:248). */
+int mag_n_live(mag_sim* sim, int species, int64_t* n_out);
+
+/* Live particles as 64-byte t_particle records (src/particles.hpp:26-33:
+ * doubles x, y, z, vx, vy, vz, time_to_death, bool empty = false, padding),
+ * at most cap records, in slot order. */
+int mag_get_particles_aos(mag_sim* sim, int species, int64_t cap, void* records, int64_t* n_out);
+
 int mag_species_save(mag_sim* sim, int species, const char* path);
 int mag_species_load(mag_sim* sim, int species, const char* path);
 

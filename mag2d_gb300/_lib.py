@@ -106,6 +106,9 @@ def lib() -> ctypes.CDLL:
     L.mag_print_field.argtypes = [P, ctypes.c_char_p]
     L.mag_species_save.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
     L.mag_species_load.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
+    L.mag_set_electrode_voltages.argtypes = [P, D, ctypes.c_int64]
+    L.mag_n_live.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+    L.mag_get_particles_aos.argtypes = [P, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
     L.mag_source_refresh.argtypes = [P, ctypes.c_int]
     L.mag_source_save.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
     L.mag_source_load.argtypes = [P, ctypes.c_int, ctypes.c_char_p]

@@ -2,6 +2,7 @@
 // C++ exceptions and turns them into a status code plus mag_last_error().
 #include "mag2d_gpu.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -506,6 +507,50 @@ int mag_species_save(mag_sim* sim, int species, const char* path)
         check_species(sim, species);
         if (!path) throw mag::Error(MAG_EINVAL, "null path");
         sim->s->save_species(species, path);
+        return device_status(sim);
+    });
+}
+
+int mag_set_electrode_voltages(mag_sim* sim, const double* v, int64_t n)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!v || n < 0) throw mag::Error(MAG_EINVAL, "null or negative voltage array");
+        sim->s->set_voltages(v, (size_t)n);
+        return device_status(sim);
+    });
+}
+
+int mag_n_live(mag_sim* sim, int species, int64_t* n_out)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (!n_out) throw mag::Error(MAG_EINVAL, "null output");
+        double e2 = 0;
+        unsigned long long n = 0;
+        if (sim->s->sp[species].n_slots > 0) sim->s->energy(species, e2, n);
+        *n_out = (int64_t)n;
+        return device_status(sim);
+    });
+}
+
+int mag_get_particles_aos(mag_sim* sim, int species, int64_t cap, void* records, int64_t* n_out)
+{
+    return guarded([&]() {
+        check_species(sim, species);
+        if (!records && cap > 0) throw mag::Error(MAG_EINVAL, "null output");
+        const int64_t n = std::max<int64_t>(0, std::min<int64_t>(cap, sim->s->sp[species].n_slots));
+        std::vector<double> x(n), z(n), vx(n), vy(n), vz(n);
+        int64_t m = 0;
+        sim->s->get_particles(species, n, x.data(), z.data(), vx.data(), vy.data(), vz.data(), nullptr, &m);
+        unsigned char* out = static_cast<unsigned char*>(records);
+        for (int64_t k = 0; k < m; ++k) {
+            unsigned char* r = out + 64 * k;
+            std::memset(r, 0, 64);
+            const double d[7] = {x[k], 0.0, z[k], vx[k], vy[k], vz[k], 0.0};
+            std::memcpy(r, d, sizeof d);  // empty = false, padding zero
+        }
+        if (n_out) *n_out = m;
         return device_status(sim);
     });
 }

@@ -1490,6 +1490,39 @@ void Sim::energy(int s, double& sum_v2, unsigned long long& n)
     }
 }
 
+// New voltages of the electrodes (t_grid::voltage on its FIXED and FIXED_RF
+// nodes; the free nodes' entries are ignored): the RF Laplace solution and,
+// without a self-consistent field, the static potential are solved again as
+// the Pic constructor does (pic.cpp:170-186); a self-consistent run's next
+// step solves with them (the stored electrode potential of the direct solve
+// is recomputed).
+void Sim::set_voltages(const double* v, size_t n)
+{
+    if (n != (size_t)nx * nz) throw Error(-1, "electrode voltages: one value per node expected");
+    if (p.electric_field_from_file) throw Error(-1, "electrode voltages: the fields come from files");
+    for (size_t k = 0; k < n; ++k)
+        if (mask[k] == 0 || mask[k] == 1) voltage[k] = v[k];
+    MAG_CK(cudaStreamSynchronize(stream));
+    d_volt.upload(voltage.data(), n, stream);
+    if (u_prev_valid.p) u_prev_valid.zero(stream);
+    ensure_full_u();
+    setup_solver();
+    solve(true, 0, false, false);
+    if (!p.selfconsistent) solve(false, 0, false, false);
+    refresh_rf_pairs();
+    if (green_ready()) {  // the potential of the electrodes alone
+        SolveArgs vac = solve_args(false, 0, false);
+        vac.u = green_vac.p;
+        vac.Exf = nullptr;
+        vac.Ezf = nullptr;
+        vac.status = green_status.p;
+        GreenArgs g = green_args(false);
+        g.rows = nullptr;
+        launches += launch_green_solve(vac, g, stream);
+    }
+    MAG_CK(cudaGetLastError());
+}
+
 // ---- particle source --------------------------------------------------
 
 SourceArgs Sim::source_args(int s, bool init)

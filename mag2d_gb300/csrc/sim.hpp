@@ -191,6 +191,7 @@ public:
     DevArray<int> u_prev_valid;
     bool extrapolate_u = true;
     void ensure_full_u();
+    void set_voltages(const double* v, size_t n);
     DevArray<SolveStatus> green_status;
     int green_chunks_n = 0;
     GreenArgs green_args(bool vacuum) const;

@@ -141,6 +141,21 @@ class Species:
         """BaseSpecies::load (src/particles.cpp:59-93)."""
         check(lib().mag_species_load(self._pic.h, self.index, str(path).encode()))
 
+    def n_live(self) -> int:
+        """BaseSpecies::n_particles (src/particles.hpp:248)."""
+        n = ctypes.c_int64()
+        check(lib().mag_n_live(self._pic.h, self.index, ctypes.byref(n)))
+        return n.value
+
+    def particles_aos(self) -> np.ndarray:
+        """Live particles as t_particle records (x, y, z, vx, vy, vz, time_to_death, empty)."""
+        cap = max(int(self.info()["capacity"]), 1)
+        rec = np.zeros((cap, 8), dtype=np.float64)
+        n = ctypes.c_int64()
+        check(lib().mag_get_particles_aos(self._pic.h, self.index, cap, rec.ctypes.data_as(ctypes.c_void_p),
+                                          ctypes.byref(n)))
+        return rec[: n.value].copy()
+
     def source_save(self, path) -> None:
         """BaseSpecies::source5_save (src/particles.cpp:109-120)."""
         check(lib().mag_source_save(self._pic.h, self.index, str(path).encode()))
@@ -242,6 +257,11 @@ class Pic:
 
     def advance(self, n: int = 1) -> None:
         check(lib().mag_advance(self.h, n))
+
+    def set_electrode_voltages(self, v: np.ndarray) -> None:
+        """t_grid::voltage of the fixed nodes (x_sampl, z_sampl); the fields follow."""
+        a = np.ascontiguousarray(v, dtype=np.float64)
+        check(lib().mag_set_electrode_voltages(self.h, _dp(a), a.size))
 
     def source_refresh(self, factor: int) -> None:
         """Species<CARTESIAN>::source5_refresh(factor) of every species with particles."""

@@ -134,3 +134,49 @@ def test_sampled_distributions(m, tmp_path):
     nx, nz = pic.shape
     assert sum(1 for line in rho_lines if line.count("\t") == 2) == nx * nz
     pic.close()
+
+
+@pytest.mark.parametrize("selfconsistent", [0, 1])
+def test_set_electrode_voltages_matches_a_fresh_run(m, tmp_path, selfconsistent):
+    """mag_set_electrode_voltages: the fields of the new voltages equal those of
+    a run made from a config with them (within the solver tolerance)."""
+    from cases import penning_rz
+    from mag2d_cases import write_config
+
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=3000, selfconsistent=selfconsistent)
+    cfg2 = dict(cfg, u_endcap=-17.5)
+    cpath2 = write_config(cfg2, tmp_path / "c2.txt")
+    b = m.Pic(cpath2, spath, seed=2)
+    v_new = b.field.voltage
+    a = m.Pic(cpath, spath, seed=2)
+    a.set_electrode_voltages(v_new)
+    for p in (a, b):
+        p.speclist[0].set_particles(*parts)
+        p.advance_init()
+        p.advance(5)
+    ua, ub = a.field.u, b.field.u
+    assert np.abs(ua - ub).max() <= 1e-9 * np.abs(ub).max()
+    ga, gb = a.speclist[0].particles(), b.speclist[0].particles()
+    oa, ob = np.argsort(ga["id"]), np.argsort(gb["id"])
+    assert np.array_equal(ga["id"][oa], gb["id"][ob])
+    assert np.abs(ga["z"][oa] - gb["z"][ob]).max() <= 1e-9 * 20e-3
+    a.close()
+    b.close()
+
+
+def test_n_live_and_aos_records(m, tmp_path):
+    from cases import penning_rz
+
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=4000)
+    pic = m.Pic(cpath, spath, seed=2)
+    sp = pic.speclist[0]
+    sp.set_particles(*parts)
+    pic.advance_init()
+    pic.advance(30)
+    g = sp.particles()
+    rec = sp.particles_aos()
+    assert sp.n_live() == sp.diag()["n_live"] == len(g["x"]) == len(rec)
+    for c, k in ((0, "x"), (2, "z"), (3, "vx"), (4, "vy"), (5, "vz")):
+        assert np.array_equal(rec[:, c], g[k]), k
+    assert np.all(rec[:, 1] == 0) and np.all(rec[:, 7] == 0)
+    pic.close()
