@@ -296,12 +296,13 @@ struct Solve3Args {
     SolveStatus* status;
 };
 
-
+// State of the grid barrier of a cooperative solve (zeroed before each
+// launch): the monotonic arrival counter and the abort flag a block sets when
+// its bounded wait gives up.
 struct GridBarrier {
     unsigned int count;
-    unsigned int gen;
     unsigned int abort;
-    unsigned int pad;
+    unsigned int pad[2];
 };
 
 struct MGLevelDev {
