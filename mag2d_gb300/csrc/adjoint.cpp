@@ -72,6 +72,7 @@ AdjointResult Adjoint::run(Sim& sim, const AdjointConfig& cfg)
     if (cfg.nsteps == 0) throw Error(-1, "adjoint run: nsteps must be positive");
     if (!sim.p.magnetic_field_const) throw Error(-1, "adjoint run: a magnetic field table is not supported (constant B only)");
     if (sim.p.use_source) throw Error(-1, "adjoint run: particle sources (use_source) are not supported");
+    if (sim.p.u_smooth) throw Error(-1, "adjoint run: potential smoothing (u_smooth) is not supported");
     // checkpoints copy and restore u: every solve of the run computes every node
     sim.ensure_full_u();
     // and every replayed step solves from the same start as the forward one

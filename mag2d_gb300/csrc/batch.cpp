@@ -50,6 +50,8 @@ Batch::Batch(const std::vector<BatchInstanceDesc>& desc, const SimOptions& base)
             sims.emplace_back(new Sim(desc[i].config, desc[i].species_conf, o));
             if (sims.back()->p.use_source)
                 throw Error(-1, "batched runs: use_source (particle source boxes) is not provided; run the instance alone");
+            if (sims.back()->p.u_smooth)
+                throw Error(-1, "batched runs: u_smooth (potential smoothing) is not provided; run the instance alone");
             if (!desc[i].initscript.empty()) sims.back()->run_initscript(desc[i].initscript);
         } catch (const Error& e) {
             throw Error(e.code, "instance " + std::to_string(i) + ": " + e.what());

@@ -75,6 +75,8 @@ int solve_max_blocks(int sm_count);
 // 'threads' threads each; grids up to kSingleBlockNodes nodes)
 int launch_solve_batch(const SolveArgs* d_args, int n, int threads, cudaStream_t s);
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s);
+// Fields::u_smooth(): u = the smoothing of t, a copy of u (nx*nz each)
+int launch_u_smooth(const double* t, double* u, int nx, int nz, cudaStream_t s);
 // direct solve u = G b' with the precomputed inverse G (nn x nn, column j =
 // response to a unit right-hand side at node j); bprime (nn) and part
 // (nchunks x nn) are scratch; writes the faces when a.Exf is set

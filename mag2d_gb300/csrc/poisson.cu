@@ -926,6 +926,43 @@ int launch_green_product(const SolveArgs& a, const GreenArgs& g, bool partial, c
     return 2;
 }
 
+// Fields::u_smooth (fields.cpp:28-111) with its default arguments, on the
+// copy t of u: rows 1..nx-2, columns 1..nz-1 take the 3x3 weights 1, 1/2
+// (edges), 1/4 (corners), added in the reference's order and divided by 4;
+// every other node keeps its value.  The reference addresses neighbours on
+// one contiguous row-major array, so column nz is column 0 of the next row;
+// the one neighbour past the array (row nx-2, column nz-1, its +1/+1
+// neighbour) is taken as 0.  Products by 1/2 and 1/4 are exact, so the
+// explicit round-to-nearest adds reproduce the reference bit for bit.
+__global__ void k_u_smooth(const double* __restrict__ t, double* __restrict__ u, int nx, int nz)
+{
+    const long long n = (long long)nx * nz;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x; f < n; f += stride) {
+        const int i = (int)(f / nz);
+        const int j = (int)(f - (long long)i * nz);
+        if (i < 1 || i > nx - 2 || j < 1) continue;
+        const double last = f + nz + 1 < n ? t[f + nz + 1] : 0.0;
+        double sum = __dadd_rn(t[f], __dmul_rn(t[f - nz], 0.5));
+        sum = __dadd_rn(sum, __dmul_rn(t[f + nz], 0.5));
+        sum = __dadd_rn(sum, __dmul_rn(t[f - 1], 0.5));
+        sum = __dadd_rn(sum, __dmul_rn(t[f + 1], 0.5));
+        sum = __dadd_rn(sum, __dmul_rn(t[f - nz - 1], 0.25));
+        sum = __dadd_rn(sum, __dmul_rn(t[f + nz - 1], 0.25));
+        sum = __dadd_rn(sum, __dmul_rn(t[f - nz + 1], 0.25));
+        sum = __dadd_rn(sum, __dmul_rn(last, 0.25));
+        u[f] = __dmul_rn(sum, 0.25);
+    }
+}
+
+int launch_u_smooth(const double* t, double* u, int nx, int nz, cudaStream_t s)
+{
+    const long long n = (long long)nx * nz;
+    const int grid = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+    k_u_smooth<<<grid, 256, 0, s>>>(t, u, nx, nz);
+    return 1;
+}
+
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s)
 {
     const long long n = (long long)(nx + 1) * nz + (long long)nx * (nz + 1);

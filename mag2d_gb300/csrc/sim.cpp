@@ -72,6 +72,12 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     if (p.mover == ADVANCE_LEAPFROG)
         throw Error(-1, "mover ADVANCE_LEAPFROG is not provided by this library (ADVANCE_BORIS, ADVANCE_MULTICOLL)");
     multicoll = p.mover == ADVANCE_MULTICOLL;
+    if (p.u_smooth) {
+        // the smoothing reads every node, and the extrapolated start of the
+        // next solve would extrapolate smoothed potentials
+        partial_rows = false;
+        extrapolate_u = false;
+    }
     if (multicoll) {  // the reference's own conditions (src/particles.cpp:812-823)
         if (p.coord != CARTESIAN) throw Error(-1, "Species<CYLINDRICAL>: advance method not implemented");
         if (!p.magnetic_field_const || p.Br != 0.0 || p.Bt != 0.0 || p.Bz != 0.0)
@@ -84,7 +90,6 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
         throw Error(-1, "use_source: Species<CYLINDRICAL>::source is not defined in the reference");
     if (p.use_source && multicoll)
         throw Error(-1, "use_source: the source box with ADVANCE_MULTICOLL is not provided by this library");
-    if (p.u_smooth) throw Error(-1, "u_smooth: potential smoothing is not provided by this library");
     parse_species_conf(species_conf, species_prm, inters);
     if (species_prm.empty()) throw Error(-1, "species_conf defines no species");
     if ((int)species_prm.size() > kMaxSpecies) throw Error(-1, "too many species");
@@ -485,6 +490,19 @@ void Sim::ensure_full_u()
         launches += launch_faces(green_last.u, nx, nz, dx, dz, green_last.Exf, green_last.Ezf, stream);
     MAG_CK(cudaGetLastError());
     u_partial = false;
+}
+
+// Fields::u_smooth() where Pic::advance and Pic::advance_init call it
+// (pic.cpp:336, 372): the whole potential, then the faces the push reads
+void Sim::smooth_u()
+{
+    ensure_full_u();
+    const size_t nn = (size_t)nx * nz;
+    if (!u_tmp.p) u_tmp.alloc(nn);
+    MAG_CK(cudaMemcpyAsync(u_tmp.p, u64.p, nn * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    launches += launch_u_smooth(u_tmp.p, u64.p, nx, nz, stream);
+    launches += launch_faces(u64.p, nx, nz, dx, dz, Exf.p, Ezf.p, stream);
+    MAG_CK(cudaGetLastError());
 }
 
 void Sim::run_solve(SolveArgs a)
@@ -1011,7 +1029,10 @@ void Sim::step(double* ms)
     }
     ++steps_done;
     mark(0);
-    if (p.selfconsistent) solve(false, rho_override ? 2 : 1, true, false);
+    if (p.selfconsistent) {
+        solve(false, rho_override ? 2 : 1, true, false);
+        if (p.u_smooth) smooth_u();
+    }
     rho_override = false;
     mark(1);
     for (size_t s = 0; s < sp.size(); ++s) {
@@ -1148,6 +1169,7 @@ void Sim::advance_init(bool deposit)
     if (p.selfconsistent) {
         if (deposit) deposit_all();
         solve(false, 1, false, false);
+        if (p.u_smooth) smooth_u();
     }
     for (size_t s = 0; s < sp.size(); ++s) {
         if (sp[s].n_slots == 0 || multicoll) continue;  // ADVANCE_MULTICOLL has no leapfrog start

@@ -175,8 +175,8 @@ public:
     int solve_blocks = 0;  // blocks of a cooperative solve (0: not yet chosen)
     int direct_mode = 0;   // SimOptions::direct_solve
     int max_fused = kMaxFusedSteps;  // SimOptions::max_fused_steps
-    // the inverse of the Poisson operator for direct solves (built at the first self-consistent solve)
     DevArray<double> stage64;  // host particle arrays on their way to the SoA state
+    // the inverse of the Poisson operator for direct solves (built at the first self-consistent solve)
     DevArray<double> green, green_vac, green_b, green_part;
     DevArray<int> green_j;  // compacted right-hand side (node, value) and the per-tile counts
     // a step's solve computes only the nodes near charge (the particles'
@@ -191,6 +191,9 @@ public:
     DevArray<int> u_prev_valid;
     bool extrapolate_u = true;
     void ensure_full_u();
+    // Fields::u_smooth after a step's solve (u_smooth = 1): u, then its faces
+    DevArray<double> u_tmp;
+    void smooth_u();
     void set_voltages(const double* v, size_t n);
     DevArray<SolveStatus> green_status;
     int green_chunks_n = 0;

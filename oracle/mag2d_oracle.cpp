@@ -402,6 +402,27 @@ double Interaction::coulomb_sigma(double e) const  // particles.cpp:19-26
     return M_PI * Lambda * Lambda * log(lambda_D / Lambda);
 }
 
+// Fields::u_smooth (fields.cpp:28-111) with its default arguments: the 3x3
+// weights 1, 1/2 (edges), 1/4 (corners) summed in the reference's order and
+// divided by 4, from a copy of the input.  The reference indexes uTmp[i][j+1]
+// up to j+1 = lmax on one contiguous allocation (Array.hpp:19-22), i.e. the
+// flat index i*lmax+j+1, which is column 0 of row i+1; the single read one
+// past the array (i = jmax-2, j = lmax-1, neighbour i+1, j+1) is taken as 0.
+void smooth_flat(int nx, int nz, const double* t, double* out)
+{
+    const long long n = (long long)nx * nz;
+    for (long long k = 0; k < n; ++k) out[k] = t[k];
+    auto at = [&](long long f) { return f < n ? t[f] : 0.0; };
+    for (int i = 1; i < nx - 1; i++)
+        for (int j = 1; j <= nz - 1; j++) {
+            const long long f = (long long)i * nz + j;
+            double sum = at(f) + at(f - nz) * 0.5 + at(f + nz) * 0.5 + at(f - 1) * 0.5 + at(f + 1) * 0.5 +
+                         at(f - nz - 1) * 0.25 + at(f + nz - 1) * 0.25 + at(f - nz + 1) * 0.25 +
+                         at(f + nz + 1) * 0.25;
+            out[f] = sum / 4.0;
+        }
+}
+
 }  // namespace
 
 struct orc_sim {
@@ -555,6 +576,13 @@ struct orc_sim {
                     r *= -sqr(dx) / kEps0 / dV;
             }
         lu_solve(rho.d.data(), rf_solve ? uRF.d.data() : u.d.data());
+    }
+
+    // Fields::u_smooth() as Pic::advance / advance_init call it (pic.cpp:336, 372)
+    void smooth_u()
+    {
+        const std::vector<double> t = u.d;
+        smooth_flat(u.jmax, u.lmax, t.data(), u.d.data());
     }
 
     // BaseSpecies::scatter (particles.cpp:208-365)
@@ -792,6 +820,7 @@ struct orc_sim {
     {
         if (c.selfconsistent) {
             boundary_solve(false);
+            if (c.u_smooth) smooth_u();
             rho.reset();
             for (Species* s : sp)
                 if (s->n_particles() > 0) s->rho.reset();
@@ -856,6 +885,7 @@ struct orc_sim {
                     add_rho(*s);
                 }
             boundary_solve(false);
+            if (c.u_smooth) smooth_u();
             rho.reset();
             for (Species* s : sp)
                 if (s->n_particles() > 0) add_rho(*s);
@@ -1322,6 +1352,12 @@ int orc_rng(orc_sim* s, int kind, int n, double arg, double* out)
 }
 
 int64_t orc_collisions(orc_sim* s, int sp) { return s->sp[sp]->ncoll; }
+
+void orc_u_smooth(int nx, int nz, const double* in, double* out)
+{
+    const std::vector<double> t(in, in + (size_t)nx * nz);
+    smooth_flat(nx, nz, t.data(), out);
+}
 
 int64_t orc_deposit_fixed(int nx, int nz, int64_t n, const uint32_t* xf, const uint32_t* zf, const uint8_t* alive,
                           int64_t* acc)

@@ -32,6 +32,7 @@ typedef struct {
     int magnetic_field_const;
     double Br, Bz, Bt;
     int mover;            /* 0 ADVANCE_BORIS, 1 ADVANCE_MULTICOLL (param.cpp mover) */
+    int u_smooth;         /* Fields::u_smooth after each self-consistent solve (param.cpp:53) */
 } orc_config;
 
 enum { ORC_ELASTIC = 0, ORC_LANGEVIN = 1, ORC_CX = 2, ORC_COULOMB = 3, ORC_SUPERELASTIC = 4 };
@@ -83,6 +84,13 @@ int64_t orc_collisions(orc_sim* s, int sp);
  * U = xf - i*2^20, V = zf - j*2^20.  acc is nx*nz int64 (row-major, z
  * fastest), accumulated into.  Particles with alive[i]==0 are skipped.
  * Returns the number deposited. */
+/* Fields::u_smooth (fields.cpp:28-111) with its defaults (no symmetry
+ * averaging, no radius): out = the 3x3 smoothing of in on rows 1..nx-2,
+ * columns 1..nz-1, in elsewhere.  Neighbours are read by row-major flat index,
+ * so column nz wraps to column 0 of the next row, as in the reference; the one
+ * read past the array (row nx-2, column nz-1, its +1/+1 neighbour) reads 0. */
+void orc_u_smooth(int nx, int nz, const double* in, double* out);
+
 int64_t orc_deposit_fixed(int nx, int nz, int64_t n, const uint32_t* xf, const uint32_t* zf,
                           const uint8_t* alive, int64_t* acc);
 

@@ -327,6 +327,28 @@ int ref_solve(void* h, const double* rho, double* u)
     });
 }
 
+// Fields::u_smooth() with its default arguments (fields.cpp:28-111) applied to
+// a caller-given potential; field.u is restored afterwards.
+int ref_u_smooth(void* h, const double* u_in, double* u_out)
+{
+    return with_pic(h, [&](auto& p) {
+        Field2D& u = p.field.u;
+        std::vector<double> keep((size_t)u.jmax * u.lmax);
+        for (int i = 0; i < u.jmax; ++i)
+            for (int j = 0; j < u.lmax; ++j) {
+                keep[(size_t)i * u.lmax + j] = u[i][j];
+                u[i][j] = u_in[(size_t)i * u.lmax + j];
+            }
+        p.field.u_smooth();
+        for (int i = 0; i < u.jmax; ++i)
+            for (int j = 0; j < u.lmax; ++j) {
+                u_out[(size_t)i * u.lmax + j] = u[i][j];
+                u[i][j] = keep[(size_t)i * u.lmax + j];
+            }
+        return 0;
+    });
+}
+
 // Field2D::grad of u (which=0) or uRF (which=1) at n points (Field2D.hpp:80-168)
 int ref_grad(void* h, int which, int n, const double* x, const double* z, double* gx, double* gz)
 {

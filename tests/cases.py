@@ -41,11 +41,11 @@ ME = 9.11e-31
 
 
 def penning_rz(tmp: Path, n: int = 100_000, nr: int = 65, nz: int = 129, selfconsistent: int = 1,
-               mpf: float = 10.0, seed: int = 1, Bz: float = 1.0):
+               mpf: float = 10.0, seed: int = 1, Bz: float = 1.0, u_smooth: int = 0):
     cfg = dict(coord="CYLINDRICAL", boundary="FREE", geometry="PENNING_ENDCAP", r_max=5e-3, z_max=20e-3,
                r_sampl=nr, z_sampl=nz, u_endcap=-10.0, u_ring=0.0, selfconsistent=selfconsistent, rf=0,
                magnetic_field_const=1, Bz=Bz, Br=0.0, Bt=0.0, do_plot=0, macroparticle_factor=mpf,
-               n_particles_total=float(n), density_total=1e13, mover="ADVANCE_BORIS")
+               n_particles_total=float(n), density_total=1e13, mover="ADVANCE_BORIS", u_smooth=u_smooth)
     species = [dict(name="ELECTRON", type="ELECTRON", mass=ME, charge=-QE, dt=1e-11, density=1e13,
                     temperature=11604.5)]
     cpath = write_config(cfg, tmp / "penning.txt")

@@ -8,6 +8,8 @@ present), and stores inputs and outputs as small .npz files:
   rng.npz              SHR3/ziggurat draws (uni, rnor, rexp, iuni, rot, deflect)
   step_<case>.npz      particle states after N reference time steps
   solve_<case>.npz     Fields::boundary_solve of a given rho
+  u_smooth.npz         Fields::u_smooth of given potentials (the step case
+                       step_penning_sc_smooth.npz runs it inside Pic::advance)
   geometry.npz         t_grid mask and voltage of every reference geometry
   params.npz           derived Param values of the reference's config files
   species.npz          parsed species, rates and lifetimes of its species_conf files
@@ -378,11 +380,46 @@ def gen_field3d():
          u=u, rho=rho.reshape(nx, ny, nz), interp=interp, grad=grad.reshape(n, 3))
 
 
+# ---------------------------------------------------------------------------
+def gen_smooth():
+    """Fields::u_smooth on random potentials of a cylindrical and a Cartesian
+    grid, and the self-consistent Penning step case with u_smooth = 1."""
+    out = {}
+    for tag, cfg in (("cyl", dict(coord="CYLINDRICAL", geometry="PENNING_SIMPLE", r_max=1.2e-2, z_max=7.5e-2,
+                                  r_sampl=25, z_sampl=76)),
+                     ("cart", dict(coord="CARTESIAN", geometry="EMPTY", x_max=2e-2, z_max=1e-2, x_sampl=33,
+                                   z_sampl=17))):
+        cfg = dict(cfg, boundary="FREE", selfconsistent=1, rf=0, magnetic_field_const=1, do_plot=0, u_smooth=1)
+        sp = [dict(name="ELECTRON", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11, density=1e15,
+                   temperature=11604.5)]
+        d = TMP / f"smooth_{tag}"
+        d.mkdir(exist_ok=True)
+        ref = Ref(write_config(cfg, d / "config.txt"), write_species_conf(sp, [], d / "species.txt"), d / "out", 1)
+        c = full_config(cfg)
+        shape = (int(float(c["x_sampl"])), int(float(c["z_sampl"])))
+        u = np.random.default_rng(41 if tag == "cyl" else 43).normal(0.0, 1.0, shape)
+        out[f"u_{tag}"] = u
+        out[f"smooth_{tag}"] = ref.u_smooth(u)
+    save("u_smooth.npz", **out)
+    rng = np.random.default_rng(3)
+    n = 400
+    r = 2e-3 * np.sqrt(rng.random(n))
+    z = 3.5e-2 + 5e-3 * (rng.random(n) - 0.5)
+    vth = np.sqrt(KB * 11604.5 / 9.11e-31)
+    parts = (r, z, vth * rng.standard_normal(n), vth * rng.standard_normal(n), vth * rng.standard_normal(n))
+    cfg = dict(coord="CYLINDRICAL", boundary="FREE", geometry="PENNING_SIMPLE", r_max=1.2e-2, z_max=7.5e-2,
+               r_sampl=25, z_sampl=76, selfconsistent=1, rf=0, magnetic_field_const=1, Bz=0.03, do_plot=0,
+               macroparticle_factor=2e4, n_particles_total=4e5, u_smooth=1)
+    sp = [dict(name="ELECTRON", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11, density=1e15,
+               temperature=11604.5)]
+    run_step_case("penning_sc_smooth", cfg, sp, [], 60, [30, 60], 5, setp={0: parts})
+
+
 if __name__ == "__main__":
     import sys
 
     cases = {"rng": gen_rng, "steps": gen_steps, "solves": gen_solves, "geometry": gen_geometry,
              "params_species": gen_params_species, "particle_file": gen_particle_file, "source": gen_source,
-             "field3d": gen_field3d}
+             "field3d": gen_field3d, "smooth": gen_smooth}
     for name in (sys.argv[1:] or list(cases)):
         cases[name]()

@@ -31,7 +31,7 @@ PARAM_DEFAULTS = {
     "extern_field": 100.0, "selfconsistent": 1, "rf": 1, "rf_amplitude": 10.0,
     "rf_U0": 0.0, "rf_freq": 20e6, "electric_field_from_file": 0,
     "magnetic_field_const": 1, "Br": 0.0, "Bz": 0.0, "Bt": 0.0, "do_plot": 0,
-    "mover": "ADVANCE_BORIS", "u_probe": -10.0, "probe_radius": 1e-4,
+    "mover": "ADVANCE_BORIS", "u_probe": -10.0, "probe_radius": 1e-4, "u_smooth": 0,
 }
 
 COLL_TYPES = {"ELASTIC": 0, "LANGEVIN": 1, "CX": 2, "COULOMB": 3, "SUPERELASTIC": 4}
@@ -165,7 +165,7 @@ class OrcConfig(ctypes.Structure):
         ("electric_field_from_file", ctypes.c_int), ("rf_amplitude", ctypes.c_double),
         ("rf_omega", ctypes.c_double), ("rf_U0", ctypes.c_double), ("boundary", ctypes.c_int),
         ("magnetic_field_const", ctypes.c_int), ("Br", ctypes.c_double), ("Bz", ctypes.c_double),
-        ("Bt", ctypes.c_double), ("mover", ctypes.c_int),
+        ("Bt", ctypes.c_double), ("mover", ctypes.c_int), ("u_smooth", ctypes.c_int),
     ]
 
 
@@ -185,6 +185,8 @@ def load_port() -> ctypes.CDLL:
     L.orc_last_error.restype = ctypes.c_char_p
     L.orc_time_advance.restype = ctypes.c_double
     L.orc_collisions.restype = ctypes.c_int64
+    L.orc_u_smooth.restype = None
+    L.orc_u_smooth.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     L.orc_deposit_fixed.restype = ctypes.c_int64
     L.orc_deposit_fixed.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -214,6 +216,7 @@ def orc_config(cfg: dict) -> OrcConfig:
         magnetic_field_const=int(float(c["magnetic_field_const"])),
         Br=float(c["Br"]), Bz=float(c["Bz"]), Bt=float(c["Bt"]),
         mover=1 if str(c.get("mover", "ADVANCE_BORIS")) == "ADVANCE_MULTICOLL" else 0,
+        u_smooth=int(float(c.get("u_smooth", 0))),
     )
 
 
@@ -304,6 +307,12 @@ class Port:
         u = np.zeros_like(rho)
         self._check(self.L.orc_solve(self.h, _dp(rho), _dp(u)))
         return u
+
+    def u_smooth(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.zeros_like(u)
+        self.L.orc_u_smooth(u.shape[0], u.shape[1], u.ctypes.data, out.ctypes.data)
+        return out
 
     def grad(self, which: int, x, z):
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -471,6 +480,13 @@ class Ref:
         u = np.zeros_like(rho)
         self._check(self.L.ref_solve(self.h, _dp(rho), _dp(u)))
         return u
+
+    def u_smooth(self, u: np.ndarray) -> np.ndarray:
+        """Fields::u_smooth() of the reference applied to a given potential."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.zeros_like(u)
+        self._check(self.L.ref_u_smooth(self.h, _dp(u), _dp(out)))
+        return out
 
     def grad(self, which: int, x, z):
         x = np.ascontiguousarray(x, dtype=np.float64)

@@ -94,6 +94,29 @@ def test_step_matches_reference(port_lib, fname, tmp_path):
         assert np.array_equal(port.field(2), d["rho"])
 
 
+@pytest.mark.parametrize("tag", ["cyl", "cart"])
+def test_u_smooth_matches_reference(port_lib, tag):
+    """Fields::u_smooth (fields.cpp:28-111) bit for bit, flat-index wrap of the
+    last column included; the node whose stencil reads one element past the
+    reference's array (row nx-2, column nz-1) is left out of the comparison."""
+    d = np.load(GOLDEN / "u_smooth.npz")
+    u, want = d[f"u_{tag}"], d[f"smooth_{tag}"]
+    out = np.zeros_like(u)
+    port_lib.orc_u_smooth(u.shape[0], u.shape[1], u.ctypes.data, out.ctypes.data)
+    keep = np.ones(u.shape, dtype=bool)
+    keep[-2, -1] = False
+    assert np.array_equal(out[keep], want[keep])
+    # the untouched rows and first column stay as they were
+    assert np.array_equal(out[0], u[0]) and np.array_equal(out[-1], u[-1]) and np.array_equal(out[:, 0], u[:, 0])
+    # the wrap: the last column reads column 0 of the next row
+    i, j, nz = 5, u.shape[1] - 1, u.shape[1]
+    f = u.reshape(-1)
+    k = i * nz + j
+    s = (f[k] + f[k - nz] * 0.5 + f[k + nz] * 0.5 + f[k - 1] * 0.5 + f[k + 1] * 0.5 + f[k - nz - 1] * 0.25
+         + f[k + nz - 1] * 0.25 + f[k - nz + 1] * 0.25 + f[k + nz + 1] * 0.25) / 4.0
+    assert want[i, j] == s
+
+
 @pytest.mark.parametrize("fname", sorted(p.name for p in GOLDEN.glob("solve_*.npz")))
 def test_poisson_solve_matches_reference(port_lib, fname):
     from mag2d_cases import Port
