@@ -61,9 +61,8 @@ int check_species(mag_sim* sim, int s)
     return 0;
 }
 
-int device_status(mag_sim* sim)
+int status_of(int e)
 {
-    const int e = sim->s->sync();
     if (e == 0) return MAG_OK;
     switch (e) {
     case -4: g_last_error = "Poisson solve did not reach its tolerance"; break;
@@ -73,6 +72,8 @@ int device_status(mag_sim* sim)
     }
     return e;
 }
+
+int device_status(mag_sim* sim) { return status_of(sim->s->sync()); }
 
 }  // namespace
 
@@ -303,17 +304,17 @@ int mag_diag(mag_sim* sim, int species, mag_diag_out* out)
         std::memset(out, 0, sizeof *out);
         double e2 = 0;
         unsigned long long n = 0;
-        if (S.n_slots > 0) s.energy(species, e2, n);
+        mag::Counters c{};
+        const int err = s.diag(species, e2, n, c);
         out->n_live = (int64_t)n;
         out->mean_energy_eV = n ? e2 / (double)n * S.prm.mass * 0.5 / mag::kQe : 0.0;
         out->total_charge = (double)n * S.prm.charge * s.p.macroparticle_factor;
-        const mag::Counters c = s.counters(species);
         out->collisions = (int64_t)c.ncoll;
         out->null_collisions = (int64_t)c.nnull;
         out->removed = (int64_t)c.removed;
         out->particle_steps = (int64_t)c.live_sum;
         out->niter = s.niter(species);
-        return device_status(sim);
+        return status_of(err);
     });
 }
 

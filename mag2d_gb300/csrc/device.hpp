@@ -204,6 +204,11 @@ struct SourceAppend {
 struct SetParticlesGeom {
     double x0, xmax, z0, zmax, dx, dz;
 };
+// FP64 particle columns x, z, vx, vy, vz as the kernel reads them: a device
+// staging copy, or the caller's page-locked host arrays read in place
+struct ParticleColumns {
+    const double* v[5];
+};
 
 // Steps of one fused particle launch: their number and the RF factor of each
 // (rf_amplitude cos(...) + rf_U0 at the species' step counter + k).
@@ -242,6 +247,24 @@ struct SolveStatus {
     double residual;
     int aborted;
     int pad;
+};
+
+// Device status of an instance gathered by one kernel into page-locked host
+// memory: the error flag, the last solve's status and every species' counters
+struct StatusSources {
+    const int* err;
+    const SolveStatus* st;
+    const Counters* cnt[kMaxSpecies];
+    int nsp;
+    const double* energy;  // optional: sum of v^2 and (as bits) the live count
+};
+struct StatusHost {
+    int err;
+    int pad;
+    SolveStatus st;
+    Counters c[kMaxSpecies];
+    double sum_v2;
+    unsigned long long n_live;
 };
 
 // ---- the 3D Cartesian path ------------------------------------------------

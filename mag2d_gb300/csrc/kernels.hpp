@@ -93,8 +93,11 @@ int launch_load_disk(uint32_t* x, uint32_t* z, float* vx, float* vy, float* vz, 
 int launch_interleave(const float* a, const float* b, float2* out, long long n, cudaStream_t s);
 int launch_fill_u32(uint32_t* p, uint32_t v0, int64_t n, cudaStream_t s);
 // staged = x, z, vx, vy, vz of n particles (FP64, one array after the other)
-int launch_set_particles(const double* staged, int64_t n, const SetParticlesGeom& g, uint32_t* x, uint32_t* z,
+int launch_set_particles(const ParticleColumns& staged, int64_t n, const SetParticlesGeom& g, uint32_t* x, uint32_t* z,
                          float* vx, float* vy, float* vz, uint32_t* id, cudaStream_t s);
+// error flag, solve status and counters into out (device address of
+// page-locked host memory)
+int launch_gather_status(const StatusSources& src, StatusHost* out, cudaStream_t s);
 int launch_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n,
                   double* out_sum_v2, unsigned long long* out_n, cudaStream_t s);
 // energy histogram of the live particles (Histogram::add), bins += counts,

@@ -100,22 +100,23 @@ __global__ void k_fill_u32(uint32_t* p, uint32_t v0, int64_t n)
         p[k] = v0 + (uint32_t)k;
 }
 
-// Host particle arrays (FP64, staged in device memory) to the SoA state:
-// fixed-point positions llrint((x - x0) / dx * 2^20) (outside the box: removed),
-// FP32 velocities, ids 0..n-1
-__global__ void k_set_particles(const double* __restrict__ in, int64_t n, SetParticlesGeom g, uint32_t* __restrict__ x,
+// Host particle arrays (FP64, staged in device memory or read in place from
+// page-locked host memory) to the SoA state: fixed-point positions
+// llrint((x - x0) / dx * 2^20) (outside the box: removed), FP32 velocities,
+// ids 0..n-1
+__global__ void k_set_particles(ParticleColumns in, int64_t n, SetParticlesGeom g, uint32_t* __restrict__ x,
                                 uint32_t* __restrict__ z, float* __restrict__ vx, float* __restrict__ vy,
                                 float* __restrict__ vz, uint32_t* __restrict__ id)
 {
     const double one = (double)(1u << kFracBits);
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        const double px = in[k], pz = in[n + k];
+        const double px = in.v[0][k], pz = in.v[1][k];
         const bool inside = px >= g.x0 && px <= g.xmax && pz >= g.z0 && pz <= g.zmax;
         x[k] = inside ? (uint32_t)__double2ll_rn(__dmul_rn(__ddiv_rn(__dsub_rn(px, g.x0), g.dx), one)) : kDead;
         z[k] = inside ? (uint32_t)__double2ll_rn(__dmul_rn(__ddiv_rn(__dsub_rn(pz, g.z0), g.dz), one)) : 0u;
-        vx[k] = (float)in[2 * n + k];
-        vy[k] = (float)in[3 * n + k];
-        vz[k] = (float)in[4 * n + k];
+        vx[k] = (float)in.v[2][k];
+        vy[k] = (float)in.v[3][k];
+        vz[k] = (float)in.v[4][k];
         id[k] = (uint32_t)k;
     }
 }
@@ -265,12 +266,32 @@ int launch_fill_u32(uint32_t* p, uint32_t v0, int64_t n, cudaStream_t s)
     return 1;
 }
 
-int launch_set_particles(const double* staged, int64_t n, const SetParticlesGeom& g, uint32_t* x, uint32_t* z,
+int launch_set_particles(const ParticleColumns& staged, int64_t n, const SetParticlesGeom& g, uint32_t* x, uint32_t* z,
                          float* vx, float* vy, float* vz, uint32_t* id, cudaStream_t s)
 {
     if (n == 0) return 0;
     k_set_particles<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(staged, n, g, x, z, vx, vy,
                                                                                           vz, id);
+    return 1;
+}
+
+__global__ void k_gather_status(StatusSources src, StatusHost* out)
+{
+    if (threadIdx.x == 0) {
+        out->err = *src.err;
+        out->st = *src.st;
+        if (src.energy) {
+            out->sum_v2 = src.energy[0];
+            out->n_live = reinterpret_cast<const unsigned long long*>(src.energy)[1];
+        }
+    }
+    for (int s = threadIdx.x; s < src.nsp; s += blockDim.x)
+        if (src.cnt[s]) out->c[s] = *src.cnt[s];
+}
+
+int launch_gather_status(const StatusSources& src, StatusHost* out, cudaStream_t s)
+{
+    k_gather_status<<<1, 32, 0, s>>>(src, out);
     return 1;
 }
 

@@ -132,20 +132,35 @@ Sim::~Sim()
         cudaStreamSynchronize(stream);
         sp.clear();
         lv = SolverLevels{};
+        if (status_host) cudaFreeHost(status_host);
         if (own_stream) cudaStreamDestroy(stream);
     }
 }
 
-int Sim::sync()
+int Sim::sync() { return gather_status(nullptr); }
+
+// Waits for the stream; one kernel gathers the error flag, the solve status,
+// the counters and optionally the energy sums into page-locked host memory
+int Sim::gather_status(const double* energy)
 {
+    if (!status_host) {
+        MAG_CK(cudaHostAlloc((void**)&status_host, sizeof(StatusHost), cudaHostAllocMapped));
+        MAG_CK(cudaHostGetDevicePointer((void**)&status_dev, status_host, 0));
+    }
+    StatusSources src{};
+    src.err = d_err.p;
+    src.st = d_status.p;
+    src.nsp = (int)sp.size();
+    src.energy = energy;
+    for (size_t s = 0; s < sp.size(); ++s) src.cnt[s] = sp[s].cnt.p;
+    launches += launch_gather_status(src, status_dev, stream);
     MAG_CK(cudaStreamSynchronize(stream));
-    int err = 0;
-    MAG_CK(cudaMemcpy(&err, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
-    MAG_CK(cudaMemcpy(&last_solve, d_status.p, sizeof(SolveStatus), cudaMemcpyDeviceToHost));
-    for (auto& s : sp) {
+    int err = status_host->err;
+    last_solve = status_host->st;
+    for (size_t k = 0; k < sp.size(); ++k) {
+        SpeciesState& s = sp[k];
         if (!s.cnt.p) continue;
-        Counters c;
-        MAG_CK(cudaMemcpy(&c, s.cnt.p, sizeof c, cudaMemcpyDeviceToHost));
+        const Counters& c = status_host->c[k];
         if (c.error && !err) err = c.error;
         if (s.n_slots > 0 && (int64_t)c.slots < s.n_slots) s.n_slots = (int64_t)c.slots;
     }
@@ -1278,21 +1293,44 @@ void Sim::get_particles(int s, int64_t cap, double* x, double* z, double* vx, do
     *n_out = m;
 }
 
+// The device address of a page-locked (cudaHostAlloc / cudaHostRegister) host
+// array, which kernels can read in place; false for any other memory
+static bool host_mapped(const void* ptr, const double** dev)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        (void)cudaGetLastError();  // clear the error of an unknown pointer
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return false;
+    *dev = static_cast<const double*>(a.devicePointer);
+    return true;
+}
+
 void Sim::set_particles(int s, int64_t n, const double* x, const double* z, const double* vx, const double* vy,
                         const double* vz)
 {
     SpeciesState& S = sp[s];
     S.n_slots = 0;
     ensure_capacity(s, std::max<int64_t>(n, 1));
-    // the FP64 arrays go to a device staging buffer as they are; the
-    // conversion to the fixed-point SoA runs on the device
-    if (stage64.n < (size_t)(5 * n)) stage64.alloc((size_t)(5 * n));
+    // the conversion to the fixed-point SoA runs on the device: it reads
+    // page-locked host arrays in place, other arrays from a device staging
+    // copy (the stream is synchronised below, so the caller's arrays are no
+    // longer read when this returns)
     const double* src[5] = {x, z, vx, vy, vz};
-    for (int c = 0; c < 5; ++c)
-        if (n) MAG_CK(cudaMemcpyAsync(stage64.p + (size_t)c * n, src[c], (size_t)n * sizeof(double),
-                                      cudaMemcpyHostToDevice, stream));
+    ParticleColumns cols{};
+    bool mapped = n > 0;
+    for (int c = 0; c < 5 && mapped; ++c) mapped = host_mapped(src[c], &cols.v[c]);
+    if (!mapped) {
+        if (stage64.n < (size_t)(5 * n)) stage64.alloc((size_t)(5 * n));
+        for (int c = 0; c < 5; ++c) {
+            cols.v[c] = stage64.p + (size_t)c * n;
+            if (n) MAG_CK(cudaMemcpyAsync(stage64.p + (size_t)c * n, src[c], (size_t)n * sizeof(double),
+                                          cudaMemcpyHostToDevice, stream));
+        }
+    }
     const SetParticlesGeom g{x0, xmax, z0, zmax, dx, dz};
-    launches += launch_set_particles(stage64.p, n, g, S.x.p, S.z.p, S.vx.p, S.vy.p, S.vz.p, S.id.p, stream);
+    launches += launch_set_particles(cols, n, g, S.x.p, S.z.p, S.vx.p, S.vy.p, S.vz.p, S.id.p, stream);
     S.n_slots = n;
     S.next_id = (uint32_t)n;
     upload_slots(s);
@@ -1495,21 +1533,28 @@ uint64_t Sim::niter(int s) { return sp[s].niter; }
 
 void Sim::energy(int s, double& sum_v2, unsigned long long& n)
 {
-    DevArray<double> d;
-    d.alloc(1);
-    d.zero(stream);
-    DevArray<unsigned long long> c;
-    c.alloc(1);
-    c.zero(stream);
+    Counters c;
+    const int e = diag(s, sum_v2, n, c);
+    if (e != 0) throw Error(e, "device error " + std::to_string(e));
+}
+
+// Sum of v^2 and count of the live particles with the species' counters and
+// the device status (returned): one reduction kernel, one gather into
+// page-locked host memory, one synchronisation
+int Sim::diag(int s, double& sum_v2, unsigned long long& n, Counters& c)
+{
+    if (!diag_dev.p) diag_dev.alloc(2);
     SpeciesState& S = sp[s];
-    launches += launch_energy(S.x.p, S.vx.p, S.vy.p, S.vz.p, S.n_slots, d.p, c.p, stream);
-    MAG_CK(cudaStreamSynchronize(stream));
-    sum_v2 = 0;
-    n = 0;
-    if (S.n_slots) {
-        MAG_CK(cudaMemcpy(&sum_v2, d.p, 8, cudaMemcpyDeviceToHost));
-        MAG_CK(cudaMemcpy(&n, c.p, 8, cudaMemcpyDeviceToHost));
-    }
+    MAG_CK(cudaMemsetAsync(diag_dev.p, 0, 2 * sizeof(double), stream));
+    launches += launch_energy(S.x.p, S.vx.p, S.vy.p, S.vz.p, S.n_slots, diag_dev.p,
+                              reinterpret_cast<unsigned long long*>(diag_dev.p + 1), stream);
+    const int err = gather_status(diag_dev.p);
+    sum_v2 = status_host->sum_v2;
+    n = status_host->n_live;
+    c = status_host->c[s];
+    // the last launch's per-step counts are folded by the next launch only
+    if (S.launches > 0) c.live_sum += c.live_par[(S.launches - 1) & 1];
+    return err;
 }
 
 // New voltages of the electrodes (t_grid::voltage on its FIXED and FIXED_RF

@@ -194,6 +194,11 @@ public:
     // Fields::u_smooth after a step's solve (u_smooth = 1): u, then its faces
     DevArray<double> u_tmp;
     void smooth_u();
+    // device status and diagnostics, read back through page-locked host memory
+    DevArray<double> diag_dev;
+    StatusHost* status_host = nullptr;  // written by the device (launch_gather_status)
+    StatusHost* status_dev = nullptr;
+    int gather_status(const double* energy);
     void set_voltages(const double* v, size_t n);
     DevArray<SolveStatus> green_status;
     int green_chunks_n = 0;
@@ -227,6 +232,7 @@ public:
     void load_species(int s, const std::string& path);  // BaseSpecies::load
     Counters counters(int s);
     void energy(int s, double& sum_v2, unsigned long long& n);
+    int diag(int s, double& sum_v2, unsigned long long& n, Counters& c);
     uint64_t niter(int s);
     int solver_levels() const { return lv.nlev; }
 
