@@ -80,8 +80,9 @@ def _config(n_gpus: int, n_ions: int = N_IONS, sort_interval: int = 100, workloa
 # ----------------------------------------------------------------------------
 # CPU baseline: the oracle port on the host cores
 def _cpu_worker(args):
-    """One core: the oracle port on a sample of the workload; returns (particle_steps, seconds)."""
-    n, steps, seed, workload = args
+    """One core: the oracle port on a sample of the workload, warm_steps untimed
+    steps then steps timed ones; returns (particle_steps, seconds)."""
+    n, steps, seed, workload, warm_steps = args
     sys.path.insert(0, str(ROOT / "tests"))
     import numpy as np
 
@@ -105,7 +106,7 @@ def _cpu_worker(args):
             port = Port(cfg, species, inter, mask, volt, seed=seed, loaded_fields=loaded)
         port.set_particles(sp, *parts)
         port.advance_init()
-        port.advance(2)
+        port.advance(max(warm_steps, 1))
         live0 = port.n_live(sp)
         t = port.time_advance(steps)
         live1 = port.n_live(sp)
@@ -113,14 +114,15 @@ def _cpu_worker(args):
 
 
 def cpu_baseline(sample_particles: int = 20_000, sample_steps: int = 100, cores: int | None = None,
-                 workload: str = "multipole") -> dict:
+                 workload: str = "multipole", warm_steps: int = 2) -> dict:
     import multiprocessing as mp
 
     cores = cores or os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(sample_particles, sample_steps, 100 + i, workload) for i in range(cores)])
+        res = pool.map(_cpu_worker, [(sample_particles, sample_steps, 100 + i, workload, warm_steps)
+                                     for i in range(cores)])
     wall = time.perf_counter() - t0
     ps = sum(r[0] for r in res)
     per_core = sum(r[0] / r[1] for r in res) / len(res)
@@ -136,7 +138,12 @@ def run_reference(args) -> None:
     rank, world, _ = _env_rank()
     if rank != 0:
         return
-    base = cpu_baseline(sample_particles=20_000, sample_steps=50)
+    # a bench step is advance(step_len) of the workload; here each one is the
+    # same number of steps of a 20000-ion sample on every host core (after
+    # warmup such steps untimed)
+    spb = args.step_len or 1
+    base = cpu_baseline(sample_particles=20_000, sample_steps=spb * max(args.steps, 1),
+                        warm_steps=spb * max(args.warmup, 1))
     v = base["value"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": N_IONS * (args.step_len or 1) / v * 1e3, "higher_is_better": True,
@@ -354,7 +361,8 @@ def run_ours(args) -> None:
         traffic_ps = _load_profile_traffic() if args.workload == "multipole" else None
         base = None
         if not args.no_cpu_baseline:
-            base = cpu_baseline(sample_particles=20_000, sample_steps=50 if args.workload == "multipole" else 20,
+            # about a second of work on every host core
+            base = cpu_baseline(sample_particles=20_000, sample_steps=1000 if args.workload == "multipole" else 200,
                                 workload=args.workload)
         line = {
             "metric": METRIC, "value": psteps_all / total_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
