@@ -378,7 +378,8 @@ def run_ours(args) -> None:
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
                          "traffic": (traffic_ps * live_now) if traffic_ps else None,
-                         "traffic_source": "profiles/k_push_fused_multipole_xy_1e6.md, scaled to the live ions",
+                         "traffic_source": ("profiles/k_push_fused_multipole_xy_1e6.md, scaled to the live ions"
+                                            if traffic_ps else None),
                          "kernel": (f"k_push_fused<0,2,0> ({L} steps per launch: gather + Boris + collision test "
                                     "+ background scatter + boundary)"
                                     if args.workload == "multipole" else

@@ -255,6 +255,14 @@ int mag_get_average(mag_sim* sim, int which, double* host_out);
  * <name>_rho.dat, and Fields::u_print (potential.dat) at path */
 int mag_print_distribution(mag_sim* sim, const char* dir);
 int mag_print_field(mag_sim* sim, const char* path);
+/* Pic::print_trace (src/pic.cpp:446-451, TrackedParticle::print,
+ * src/particles.cpp:12-17): for every particle an initscript added with
+ * add_tracked_particle, one line "x z vx vz vy" (10 significant digits) is
+ * appended to <dir>/<species>_traj_<slot>.dat, slot being the particle's
+ * index when it was added; a handle's first call truncates the file (the
+ * reference opens it when the particle is added).  A removed particle gets
+ * no line (the reference prints its stale slot). */
+int mag_print_trace(mag_sim* sim, const char* dir);
 
 /* ---- Particle files ---------------------------------------------------------
  * BaseSpecies::save / load (src/particles.cpp:32-93): int32 slot count, int32

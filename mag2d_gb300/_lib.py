@@ -104,6 +104,7 @@ def lib() -> ctypes.CDLL:
     L.mag_get_average.argtypes = [P, ctypes.c_int, D]
     L.mag_print_distribution.argtypes = [P, ctypes.c_char_p]
     L.mag_print_field.argtypes = [P, ctypes.c_char_p]
+    L.mag_print_trace.argtypes = [P, ctypes.c_char_p]
     L.mag_species_save.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
     L.mag_species_load.argtypes = [P, ctypes.c_int, ctypes.c_char_p]
     L.mag_set_electrode_voltages.argtypes = [P, D, ctypes.c_int64]

@@ -492,6 +492,16 @@ int mag_print_distribution(mag_sim* sim, const char* dir)
     });
 }
 
+int mag_print_trace(mag_sim* sim, const char* dir)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!dir) throw mag::Error(MAG_EINVAL, "null directory");
+        sim->s->print_trace(dir);
+        return device_status(sim);
+    });
+}
+
 int mag_print_field(mag_sim* sim, const char* path)
 {
     return guarded([&]() {

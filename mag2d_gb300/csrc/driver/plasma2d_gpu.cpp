@@ -3,7 +3,8 @@
 //   plasma2d_gpu config=config.txt species_conf=species_conf.txt
 //                initscript=initscript.txt output_dir=output [niter=N] [seed=S]
 // Writes out.dat (iteration, wall seconds, live particles of every species)
-// every t_print steps, <species>.dat (niter n_live mean_energy_eV t, the
+// every t_print steps, the tracked particles' <species>_traj_<slot>.dat every
+// 10 steps, <species>.dat (niter n_live mean_energy_eV t, the
 // columns of BaseSpecies::print_status, src/particles.cpp:367-375) and, at
 // the end, potential.dat in the x z value layout of Field2D::print
 // (src/Field2D.cpp:30-44).  The reference's interactive y/n prompt before
@@ -58,11 +59,20 @@ int main(int argc, char** argv)
     }
     std::ofstream out(cl["output_dir"] + "/out.dat");
     const auto t0 = std::chrono::steady_clock::now();
+    // Pic::print_trace every 10 steps (src/test.cpp:66-69) when the initscript tracks particles
+    bool trace = false;
+    {
+        std::ifstream ini(cl["initscript"]);
+        std::string line;
+        while (std::getline(ini, line)) trace = trace || line.find("add_tracked_particle") != std::string::npos;
+    }
     unsigned long done = 0;
     while (done < niter) {
-        const unsigned long chunk = t_print ? std::min(t_print - done % t_print, niter - done) : niter - done;
+        unsigned long chunk = t_print ? std::min(t_print - done % t_print, niter - done) : niter - done;
+        if (trace) chunk = std::min(chunk, 10 - done % 10);
         if (mag_advance(sim, chunk) != MAG_OK) die("advance");
         done += chunk;
+        if (trace && done % 10 == 0 && mag_print_trace(sim, cl["output_dir"].c_str()) != MAG_OK) die("trace");
         if ((t_print && done % t_print == 0) || done == niter) {
             if (mag_sync(sim) != MAG_OK) die("advance");
             const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

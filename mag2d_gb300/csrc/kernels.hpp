@@ -98,6 +98,9 @@ int launch_set_particles(const ParticleColumns& staged, int64_t n, const SetPart
 // error flag, solve status and counters into out (device address of
 // page-locked host memory)
 int launch_gather_status(const StatusSources& src, StatusHost* out, cudaStream_t s);
+// the records of the live particles whose ids are want[0..nwant) (tracked particles)
+int launch_find_ids(const uint32_t* id, const uint32_t* x, const uint32_t* z, const float* vx, const float* vy,
+                    const float* vz, int64_t n, const uint32_t* want, int nwant, uint32_t* rec, cudaStream_t s);
 int launch_energy(const uint32_t* x, const float* vx, const float* vy, const float* vz, int64_t n,
                   double* out_sum_v2, unsigned long long* out_n, cudaStream_t s);
 // energy histogram of the live particles (Histogram::add), bins += counts,

@@ -275,6 +275,38 @@ int launch_set_particles(const ParticleColumns& staged, int64_t n, const SetPart
     return 1;
 }
 
+// rec[6 w ..]: found flag, x, z (fixed point), vx, vy, vz (FP32 bits) of the
+// live particle with id want[w]
+__global__ void k_find_ids(const uint32_t* __restrict__ id, const uint32_t* __restrict__ x,
+                           const uint32_t* __restrict__ z, const float* __restrict__ vx, const float* __restrict__ vy,
+                           const float* __restrict__ vz, int64_t n, const uint32_t* __restrict__ want, int nwant,
+                           uint32_t* __restrict__ rec)
+{
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        if (x[k] == kDead) continue;
+        const uint32_t pid = id[k];
+        for (int w = 0; w < nwant; ++w)
+            if (want[w] == pid) {
+                uint32_t* r = rec + 6 * w;
+                r[0] = 1u;
+                r[1] = x[k];
+                r[2] = z[k];
+                r[3] = __float_as_uint(vx[k]);
+                r[4] = __float_as_uint(vy[k]);
+                r[5] = __float_as_uint(vz[k]);
+            }
+    }
+}
+
+int launch_find_ids(const uint32_t* id, const uint32_t* x, const uint32_t* z, const float* vx, const float* vy,
+                    const float* vz, int64_t n, const uint32_t* want, int nwant, uint32_t* rec, cudaStream_t s)
+{
+    if (n == 0 || nwant == 0) return 0;
+    k_find_ids<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8), 256, 0, s>>>(id, x, z, vx, vy, vz, n, want,
+                                                                                      nwant, rec);
+    return 1;
+}
+
 __global__ void k_gather_status(StatusSources src, StatusHost* out)
 {
     if (threadIdx.x == 0) {

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <fstream>
+#include <iomanip>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -845,7 +846,9 @@ void Sim::run_initscript(const std::string& path)
             add_loaded(species(t[1]), to_int(t[2]), 0, to_num(t[3]), to_num(t[4]), to_num(t[5]), 0, 0);
         } else if (t[0] == "add_tracked_particle") {
             need(7);  // particles.hpp:297-309: y and z components are swapped on input
-            add_single(species(t[1]), to_num(t[2]), to_num(t[3]), to_num(t[4]), to_num(t[6]), to_num(t[5]));
+            const int s = species(t[1]);
+            tracked.push_back({s, sp[s].next_id, sp[s].n_slots, nullptr});
+            add_single(s, to_num(t[2]), to_num(t[3]), to_num(t[4]), to_num(t[6]), to_num(t[5]));
         } else if (t[0] == "add_particles_in_cylinder") {
             // r-z loader: species n r_max z_min z_max, uniform in volume (r = r_max sqrt(u))
             need(6);
@@ -1336,6 +1339,49 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     upload_slots(s);
     init_ttd(s, 0, n);
     sort_due = true;
+}
+
+// Pic::print_trace (src/pic.cpp:446-451): TrackedParticle::print of every
+// tracked particle (particles.cpp:12-17), found by its id
+void Sim::print_trace(const std::string& dir)
+{
+    if (tracked.empty()) return;
+    const double inv = 1.0 / (double)(1u << kFracBits);
+    for (size_t s = 0; s < sp.size(); ++s) {
+        std::vector<uint32_t> want;
+        std::vector<size_t> which;
+        for (size_t k = 0; k < tracked.size(); ++k)
+            if (tracked[k].s == (int)s) {
+                want.push_back(tracked[k].id);
+                which.push_back(k);
+            }
+        if (want.empty()) continue;
+        SpeciesState& S = sp[s];
+        const int nw = (int)want.size();
+        DevArray<uint32_t> d_want, d_rec;
+        d_want.upload(want.data(), want.size(), stream);
+        d_rec.alloc((size_t)nw * 6);
+        MAG_CK(cudaMemsetAsync(d_rec.p, 0, (size_t)nw * 6 * sizeof(uint32_t), stream));
+        launches += launch_find_ids(S.id.p, S.x.p, S.z.p, S.vx.p, S.vy.p, S.vz.p, S.n_slots, d_want.p, nw, d_rec.p,
+                                    stream);
+        std::vector<uint32_t> rec((size_t)nw * 6);
+        d_rec.download(rec.data(), rec.size(), stream);
+        MAG_CK(cudaStreamSynchronize(stream));
+        for (int w = 0; w < nw; ++w) {
+            Tracked& T = tracked[which[w]];
+            if (!T.out) {
+                T.out = std::make_shared<std::ofstream>(dir + "/" + S.prm.name + "_traj_" + std::to_string(T.slot) +
+                                                        ".dat");
+                if (!*T.out) throw Error(-1, "print_trace: cannot open a file in " + dir);
+            }
+            const uint32_t* r = rec.data() + (size_t)w * 6;
+            if (r[0] == 0) continue;  // removed
+            float v[3];
+            std::memcpy(v, r + 3, sizeof v);
+            *T.out << std::setprecision(10) << x0 + (double)r[1] * inv * dx << ' ' << z0 + (double)r[2] * inv * dz
+                   << ' ' << v[0] << ' ' << v[2] << ' ' << v[1] << std::endl;
+        }
+    }
 }
 
 // Pic::dist_reset (src/pic.cpp:412-420)

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <fstream>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -194,6 +196,14 @@ public:
     // Fields::u_smooth after a step's solve (u_smooth = 1): u, then its faces
     DevArray<double> u_tmp;
     void smooth_u();
+    // particles added by add_tracked_particle (TrackedParticle, particles.hpp:297-309)
+    struct Tracked {
+        int s;
+        uint32_t id;
+        int64_t slot;
+        std::shared_ptr<std::ofstream> out;
+    };
+    std::vector<Tracked> tracked;
     // device status and diagnostics, read back through page-locked host memory
     DevArray<double> diag_dev;
     StatusHost* status_host = nullptr;  // written by the device (launch_gather_status)
@@ -228,6 +238,7 @@ public:
     void average(int which, double* out);  // MAG_U: uAvg / nsampl; MAG_SPECIES_RHO + s: rhoAverage / nsampl
     void print_distribution(const std::string& dir);
     void print_field(const std::string& path);
+    void print_trace(const std::string& dir);  // Pic::print_trace
     void save_species(int s, const std::string& path);  // BaseSpecies::save
     void load_species(int s, const std::string& path);  // BaseSpecies::load
     Counters counters(int s);

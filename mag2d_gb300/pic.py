@@ -291,6 +291,11 @@ class Pic:
     def print_field(self, path) -> None:
         check(lib().mag_print_field(self.h, str(path).encode()))
 
+    def print_trace(self, directory) -> None:
+        """Pic::print_trace: one "x z vx vz vy" line per tracked particle
+        (add_tracked_particle) appended to <dir>/<species>_traj_<slot>.dat."""
+        check(lib().mag_print_trace(self.h, str(directory).encode()))
+
     def solve_status(self) -> dict:
         """Status of the most recent Poisson solve (iterations, residual, status, levels)."""
         info = MagSolveInfo()

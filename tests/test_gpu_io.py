@@ -213,3 +213,34 @@ def test_set_particles_from_page_locked_memory(m, tmp_path):
         pic.close()
     for k in out[0]:
         assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_print_trace_of_tracked_particles(m, tmp_path):
+    """Pic::print_trace: a particle added by add_tracked_particle gets one
+    "x z vx vz vy" line per call in <species>_traj_<slot>.dat, equal to its
+    state read back through the particle view."""
+    from mag2d_cases import QE, write_config, write_species_conf
+
+    cfg = dict(coord="CARTESIAN", boundary="PERIODIC", geometry="EMPTY", x_max=2e-2, z_max=2e-2, x_sampl=11,
+               z_sampl=11, selfconsistent=0, rf=0, extern_field=100.0, do_plot=0)
+    sp = [dict(name="ELECTRON", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11, density=1e15,
+               temperature=11604.5)]
+    cpath = write_config(cfg, tmp_path / "c.txt")
+    spath = write_species_conf(sp, [], tmp_path / "s.txt")
+    ini = tmp_path / "init.txt"
+    ini.write_text("add_particles_everywhere ELECTRON 500\nadd_tracked_particle ELECTRON 1e-2 1e-2 1000 2000 3000\n")
+    out = tmp_path / "out"
+    out.mkdir()
+    pic = m.Pic(cpath, spath, ini, seed=1)
+    pic.advance_init()
+    for _ in range(3):
+        pic.advance(10)
+        pic.print_trace(out)
+    lines = (out / "ELECTRON_traj_500.dat").read_text().splitlines()
+    assert len(lines) == 3
+    last = np.array([float(v) for v in lines[-1].split()])
+    g = pic.speclist[0].particles()
+    k = int(np.flatnonzero(g["id"] == 500)[0])
+    want = np.array([g["x"][k], g["z"][k], g["vx"][k], g["vz"][k], g["vy"][k]])
+    assert np.allclose(last, want, rtol=1e-9, atol=0), (last, want)
+    pic.close()
