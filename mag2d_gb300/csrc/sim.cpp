@@ -1297,15 +1297,16 @@ void Sim::get_particles(int s, int64_t cap, double* x, double* z, double* vx, do
 }
 
 // The device address of a page-locked (cudaHostAlloc / cudaHostRegister) host
-// array, which kernels can read in place; false for any other memory
-static bool host_mapped(const void* ptr, const double** dev)
+// array registered with this device, which kernels can read in place; false
+// for any other memory
+static bool host_mapped(const void* ptr, int device, const double** dev)
 {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
         (void)cudaGetLastError();  // clear the error of an unknown pointer
         return false;
     }
-    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return false;
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr || a.device != device) return false;
     *dev = static_cast<const double*>(a.devicePointer);
     return true;
 }
@@ -1323,7 +1324,7 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     const double* src[5] = {x, z, vx, vy, vz};
     ParticleColumns cols{};
     bool mapped = n > 0;
-    for (int c = 0; c < 5 && mapped; ++c) mapped = host_mapped(src[c], &cols.v[c]);
+    for (int c = 0; c < 5 && mapped; ++c) mapped = host_mapped(src[c], device, &cols.v[c]);
     if (!mapped) {
         if (stage64.n < (size_t)(5 * n)) stage64.alloc((size_t)(5 * n));
         for (int c = 0; c < 5; ++c) {
