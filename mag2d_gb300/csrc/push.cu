@@ -375,6 +375,9 @@ template <int COORD, int EMODE, bool BFIELD, int VEC>
 __global__ void __launch_bounds__(256, push_min_blocks<VEC>()) k_push(const __grid_constant__ PushArgs a)
 {
     using V = Vec<VEC>;
+    // launched with programmatic serialisation: everything of the previous
+    // kernel is visible after this wait
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     // a dependent k_collide may be scheduled and stage its tables now; it
     // waits for this whole grid before it reads any result
     asm volatile("griddepcontrol.launch_dependents;");
@@ -749,7 +752,18 @@ void launch_step(const PushArgs& a, int sm_count, cudaStream_t s)
     const int64_t needed = (groups + 255) / 256;
     const int64_t iters = (needed + resident - 1) / resident;
     const unsigned grid = (unsigned)std::max<int64_t>(1, (needed + iters - 1) / iters);
-    k_push<COORD, EMODE, BFIELD, VEC><<<grid, 256, 0, s>>>(a);
+    // programmatic stream serialisation: the blocks are scheduled while the
+    // previous kernel (the face field of the solve) finishes, and wait for it
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_push<COORD, EMODE, BFIELD, VEC>, a);
 }
 
 template <int COORD, int EMODE, bool BFIELD>
