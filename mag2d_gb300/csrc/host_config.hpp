@@ -44,7 +44,8 @@ private:
 
 enum Coord { CARTESIAN = 0, CYLINDRICAL = 1, CARTESIAN3D = 2 };
 enum Boundary { BND_FREE = 0, BND_PERIODIC = 1, BND_MIRROR = 2 };
-enum Mover { ADVANCE_BORIS = 0, ADVANCE_MULTICOLL = 1, ADVANCE_LEAPFROG = 2 };
+// the movers Param accepts (param.cpp:97-105; its ADVANCE_LEAPFROG cannot be selected)
+enum Mover { ADVANCE_BORIS = 0, ADVANCE_MULTICOLL = 1 };
 enum Geometry {
     GEO_EMPTY, GEO_PROBE, GEO_RF_22PT, GEO_RF_8PT, GEO_RF_HAITRAP, GEO_RF_QUAD, GEO_MAC,
     GEO_PENNING, GEO_PENNING_SIMPLE, GEO_TUBE,

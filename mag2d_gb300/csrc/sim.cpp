@@ -70,8 +70,6 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     config_path = config;
     p = make_param(KeyValueConfig::from_file(config));
     if (p.coord == CARTESIAN3D) throw Error(-1, "coord = CARTESIAN3D: use the 3D handle (mag3d_create)");
-    if (p.mover == ADVANCE_LEAPFROG)
-        throw Error(-1, "mover ADVANCE_LEAPFROG is not provided by this library (ADVANCE_BORIS, ADVANCE_MULTICOLL)");
     multicoll = p.mover == ADVANCE_MULTICOLL;
     if (p.u_smooth) {
         // the smoothing reads every node, and the extrapolated start of the

@@ -98,6 +98,7 @@ def test_penning_endcap_geometry(m, tmp_path):
     ("rf = 0\nboundary = MIRROR\ncoord = CARTESIAN\n", "MIRROR"),
     ("rf = 0\ncoord = CYLINDRICAL\nboundary = PERIODIC\n", "only FREE"),
     ("rf = 0\nmover = ADVANCE_WARP\n", "unrecognized mover"),
+    ("rf = 0\nmover = ADVANCE_LEAPFROG\n", "unrecognized mover"),  # param.cpp:97-105 knows two movers
     ("selfconsistent = 1\nrf = 0\nelectric_field_from_file = 1\n", "electric_field_from_file"),
 ])
 def test_param_validation_errors(m, tmp_path, text, msg):
