@@ -370,10 +370,14 @@ def run_ours(args) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": _config(world, args.particles, args.sort_interval, args.workload, L),
             "clocks": clk.summary(),
-            "e2e": {"value": e2e_all, "unit": UNIT, "h2d_bytes_per_step": int(5 * 8 * n_host / e2e_chunk),
-                    "d2h_bytes_per_step": int(64 / e2e_chunk) + 1,
-                    "note": f"e2e step = set_particles from pinned host FP64 arrays + advance({e2e_chunk}) + "
-                            "diag read (best of 5)"},
+            # per bench step (advance(L)): the e2e call uploads the 5 FP64 columns
+            # once per e2e_chunk time steps and reads back the device status
+            # (error flag, solve status, counters of every species, energy sums)
+            "e2e": {"value": e2e_all, "unit": UNIT,
+                    "h2d_bytes_per_step": int(5 * 8 * n_host * L / e2e_chunk),
+                    "d2h_bytes_per_step": int((48 + 88 * len(species)) * L / e2e_chunk),
+                    "note": f"e2e call = set_particles from pinned host FP64 arrays + advance({e2e_chunk}) + "
+                            "diag read (best of 5); bytes per bench step of advance(" + str(L) + ")"},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
