@@ -532,6 +532,10 @@ __global__ void __launch_bounds__(256, 3) k_push_fused(const __grid_constant__ P
         if (threadIdx.x == 0) mcc_stage_pointers(c, st, tab);
     }
     __syncthreads();
+    // launched with programmatic serialisation: the collision tables (set-up
+    // data) are staged while the previous kernel finishes; its results are
+    // read only after this wait
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (a.fold_slot >= 0 && blockIdx.x == 0 && threadIdx.x == 0) {
         Counters* cn = a.cnt;
         cn->live_sum += cn->live_par[a.fold_slot];
@@ -814,7 +818,17 @@ void launch_fused_t(const PushArgs& a, const CollideArgs& c, const FusedSteps& f
     const int64_t resident = (int64_t)per_sm * std::max(sm_count, 1);
     const int64_t iters = (needed + resident - 1) / resident;
     const unsigned grid = (unsigned)std::max<int64_t>(1, (needed + iters - 1) / iters);
-    k_push_fused<COORD, EMODE, BFIELD><<<grid, 256, smem, s>>>(a, c, fs);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_push_fused<COORD, EMODE, BFIELD>, a, c, fs);
 }
 
 template <int COORD, int EMODE>
