@@ -25,8 +25,29 @@ __device__ __forceinline__ int cell_of(uint32_t x, uint32_t z, int nx, int nz)
     return i * (nz - 1) + j;
 }
 
-// Particles of a warp that share a cell add to its counter once (sorted
-// particles arrive in runs of the same cell).
+// Runs of consecutive lanes with the same cell (c < 0: no particle): the
+// lane's run head and, for a head, the run's length.  Particles sorted a few
+// steps ago arrive in such runs; a cell that occurs in two runs of a warp is
+// simply counted twice.
+struct LaneRun {
+    int head, len;
+    bool is_head;
+};
+__device__ __forceinline__ LaneRun lane_run(int c, int lane)
+{
+    const int cprev = __shfl_up_sync(0xffffffffu, c, 1);
+    const bool h = lane == 0 || cprev != c;
+    const unsigned heads = __ballot_sync(0xffffffffu, h);
+    const unsigned upto = lane == 31 ? 0xffffffffu : (2u << lane) - 1u;  // lanes <= lane
+    const unsigned after = heads & ~upto;
+    LaneRun r;
+    r.head = 31 - __clz(heads & upto);
+    r.len = (after ? __ffs(after) - 1 : 32) - lane;
+    r.is_head = h;
+    return r;
+}
+
+// Each run of a warp's particles in one cell adds to its counter once.
 __global__ void k_cell_count(const SortArgs a)
 {
     const long long n = a.n;
@@ -35,11 +56,9 @@ __global__ void k_cell_count(const SortArgs a)
         const long long k = base + threadIdx.x;
         const uint32_t x = k < n ? a.x[k] : kDead;
         const bool valid = x != kDead;
-        const unsigned vm = __ballot_sync(0xffffffffu, valid);
-        if (!valid) continue;
-        const int c = cell_of(x, a.z[k], a.nx, a.nz);
-        const unsigned peers = __match_any_sync(vm, c);
-        if (lane == __ffs(peers) - 1) atomicAdd(&a.count[c], (unsigned)__popc(peers));
+        const int c = valid ? cell_of(x, a.z[k], a.nx, a.nz) : -1;
+        const LaneRun r = lane_run(c, lane);
+        if (valid && r.is_head) atomicAdd(&a.count[c], (unsigned)r.len);
     }
 }
 
@@ -128,7 +147,7 @@ __global__ void __launch_bounds__(256) k_cell_scatter(const SortArgs a, long lon
         float vx[SP], vy[SP], vz[SP];
         long long k[SP];
         int c[SP];
-        unsigned peers[SP];
+        LaneRun run[SP];
         uint32_t old[SP];
 #pragma unroll
         for (int q = 0; q < SP; ++q) {
@@ -146,18 +165,16 @@ __global__ void __launch_bounds__(256) k_cell_scatter(const SortArgs a, long lon
         for (int q = 0; q < SP; ++q) {
             // one atomic per run of equal cells in the warp; lanes take the slots below the old count
             const bool valid = x[q] != kDead;
-            const unsigned vm = __ballot_sync(0xffffffffu, valid);
             c[q] = valid ? cell_of(x[q], z[q], a.nx, a.nz) : -1;
-            peers[q] = __match_any_sync(0xffffffffu, c[q]);
+            run[q] = lane_run(c[q], lane);
             old[q] = 0;
-            if (valid && lane == __ffs(peers[q]) - 1) old[q] = atomicSub(&a.count[c[q]], (unsigned)__popc(peers[q]));
-            (void)vm;
+            if (valid && run[q].is_head) old[q] = atomicSub(&a.count[c[q]], (unsigned)run[q].len);
         }
 #pragma unroll
         for (int q = 0; q < SP; ++q) {
-            const uint32_t o = __shfl_sync(0xffffffffu, old[q], __ffs(peers[q]) - 1);
+            const uint32_t o = __shfl_sync(0xffffffffu, old[q], run[q].head);
             if (x[q] == kDead) continue;
-            const uint32_t rank = __popc(peers[q] & ((1u << lane) - 1u));
+            const uint32_t rank = (uint32_t)(lane - run[q].head);
             const uint32_t pos = __ldg(&a.offset[c[q]]) + o - 1u - rank;
             a.ox[pos] = x[q];
             a.oz[pos] = z[q];
