@@ -216,14 +216,19 @@ int mag_config_species(const char* config_path, const char* species_conf_path, i
  * voltage_host are host arrays (t_grid::mask / voltage).  coord: 0 Cartesian,
  * 1 cylindrical; dV is used by the Cartesian scaling, macroparticle_factor by
  * the cylindrical one.  stream may be NULL (default stream).  With info != NULL
- * the call waits for the solve and reports it; otherwise it returns once queued.
+ * the call waits for the solve and reports it (info->status MAG_OK,
+ * MAG_ENOTCONV or MAG_ETIMEOUT, also the return value).  With info == NULL it
+ * returns once the work is queued and gives no report of the solve at all;
+ * voltage_host is then still being copied, so page-locked voltage_host memory
+ * must stay valid until the stream has reached the solve.
  *
  * Working memory is one static device array of 4 MiB that every GPU loading the
  * library holds until exit; grids above 257 x 257 nodes are rejected with
  * MAG_EINVAL.  The first call on a device looks up the array's device address
- * with that device current, so make it before any stream capture.  All calls
- * share the array and it keeps the last call's contents: calls that overlap on
- * the GPU race. */
+ * with that device current and keeps it for the process, so make it before any
+ * stream capture; the kept address does not survive cudaDeviceReset.  All
+ * calls share the array and it keeps the last call's contents: calls that
+ * overlap on the GPU race. */
 int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, double dz, double macroparticle_factor,
                               double dV, const int8_t* mask_host, const double* voltage_host,
                               const double* rho_dev, double* u_dev, double tol, int max_iter, void* stream,

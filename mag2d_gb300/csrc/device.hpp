@@ -93,7 +93,11 @@ struct PushArgs {
     // magnetic field: constant Boris vectors, or tables Br/Bz (Field2D::interpolate)
     int has_b;                     // 0: B = 0 everywhere, the rotation is the identity
     int btab;
+    // t = q B dt / 2m and s = 2 t / (1 + t^2), each as a float pair hi + lo (lo
+    // the FP32 rounding remainder of the FP64 value), so that the rotation angle
+    // carries no systematic FP32 rounding from one step to the next
     float tx, ty, tz, sx, sy, sz;
+    float tlx, tly, tlz, slx, sly, slz;
     const float* Br;
     const float* Bz;
     int bnx, bnz;

@@ -15,8 +15,14 @@
 //   * at most kNoAllocMaxNodes grid nodes (257 x 257), and the scratch layout
 //     of the grid must fit kNoAllocScratchBytes; larger grids are rejected;
 //   * the first call on a device looks up the device address of the array
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture;
+//     (cudaGetSymbolAddress) with that device current and keeps it for the
+//     process; make that first call before any stream capture.  The kept
+//     address does not survive cudaDeviceReset of that device;
+//   * with info == NULL the call returns once the work is queued and reports
+//     nothing about the solve (convergence or a barrier timeout stays in the
+//     array and the next call clears it); voltage_host is copied
+//     asynchronously, so page-locked voltage_host memory must stay valid until
+//     the stream has reached the solve;
 //   * all calls share the one array and it keeps the contents of the last call;
 //     calls that overlap on the GPU (different streams, or different host
 //     threads on the same device) race on it.
@@ -259,8 +265,12 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
     if (rc != MAG_OK) return rc;
     info->iterations = st.iterations;
     info->residual = st.residual;
-    info->status = st.converged ? MAG_OK : MAG_ENOTCONV;
+    info->status = err != 0 ? err : (st.converged ? MAG_OK : MAG_ENOTCONV);
     info->levels = nlev;
+    if (err == MAG_ETIMEOUT) {
+        g_noalloc_err = "mag_poisson_solve_noalloc: a grid barrier of the solve kernel gave up waiting (timeout)";
+        return err;
+    }
     if (err != 0) {
         g_noalloc_err = "mag_poisson_solve_noalloc: the solve did not reach its tolerance";
         return err;

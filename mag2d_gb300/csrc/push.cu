@@ -113,41 +113,56 @@ __device__ __forceinline__ void gather_E(const PushArgs& a, uint32_t x, uint32_t
     }
 }
 
-__device__ __forceinline__ void boris_vectors(const PushArgs& a, uint32_t x, uint32_t z, float& tx, float& ty,
-                                              float& tz, float& sx, float& sy, float& sz)
+// Boris vectors t and s at (x, z) as hi + lo float pairs: the constants of a
+// uniform B, or the table values (whose lo parts are zero).
+struct BorisVec {
+    float tx, ty, tz, sx, sy, sz;
+    float tlx, tly, tlz, slx, sly, slz;
+};
+__device__ __forceinline__ BorisVec boris_vectors(const PushArgs& a, uint32_t x, uint32_t z)
 {
-    tx = a.tx, ty = a.ty, tz = a.tz, sx = a.sx, sy = a.sy, sz = a.sz;
+    BorisVec b{a.tx, a.ty, a.tz, a.sx, a.sy, a.sz, a.tlx, a.tly, a.tlz, a.slx, a.sly, a.slz};
     if (a.btab) {
         const float xi = mul(sub(fmaf(cells(x), a.gdx, a.gx0), a.b_x0), a.b_ix);
         const float zi = mul(sub(fmaf(cells(z), a.gdz, a.gz0), a.b_z0), a.b_iz);
-        tx = mul(table_interp(a.Br, a.bnx, a.bnz, xi, zi), a.q_dt_2m);
-        tz = mul(table_interp(a.Bz, a.bnx, a.bnz, xi, zi), a.q_dt_2m);
-        ty = 0.f;
-        const float f = __fdiv_rn(2.f, fmaf(tz, tz, fmaf(tx, tx, 1.f)));
-        sx = mul(tx, f);
-        sy = 0.f;
-        sz = mul(tz, f);
+        b.tx = mul(table_interp(a.Br, a.bnx, a.bnz, xi, zi), a.q_dt_2m);
+        b.tz = mul(table_interp(a.Bz, a.bnx, a.bnz, xi, zi), a.q_dt_2m);
+        b.ty = 0.f;
+        const float f = __fdiv_rn(2.f, fmaf(b.tz, b.tz, fmaf(b.tx, b.tx, 1.f)));
+        b.sx = mul(b.tx, f);
+        b.sy = 0.f;
+        b.sz = mul(b.tz, f);
+        b.tlx = b.tly = b.tlz = b.slx = b.sly = b.slz = 0.f;
     }
+    return b;
 }
 
+// v' = v + v x t, v+ = v + v' x s in the orientation of each coordinate
+// system.  Each component is the FP32 sum of the hi-part terms plus the
+// separately summed lo-part terms, so the only rounding left is that of the
+// arithmetic itself, which does not repeat identically from step to step.
+// rot_term = v + (p q - r s) with the lo parts ql, sl of q and s
+__device__ __forceinline__ float rot_term(float v, float p, float q, float r, float s, float ql, float sl)
+{
+    return add(fmaf(-r, s, fmaf(p, q, v)), fmaf(-r, sl, mul(p, ql)));
+}
 template <int COORD>
-__device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float tx, float ty, float tz, float sx,
-                                       float sy, float sz)
+__device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, const BorisVec& b)
 {
     if (COORD == 1) {  // (r, theta, z) orientation, particles.cpp:581-592
-        const float vpr = fmaf(-vz, ty, fmaf(vy, tz, vx));
-        const float vpt = fmaf(-vx, tz, fmaf(vz, tx, vy));
-        const float vpz = fmaf(-vy, tx, fmaf(vx, ty, vz));
-        vx = fmaf(-vpz, sy, fmaf(vpt, sz, vx));
-        vy = fmaf(-vpr, sz, fmaf(vpz, sx, vy));
-        vz = fmaf(-vpt, sx, fmaf(vpr, sy, vz));
+        const float vpr = rot_term(vx, vy, b.tz, vz, b.ty, b.tlz, b.tly);
+        const float vpt = rot_term(vy, vz, b.tx, vx, b.tz, b.tlx, b.tlz);
+        const float vpz = rot_term(vz, vx, b.ty, vy, b.tx, b.tly, b.tlx);
+        vx = rot_term(vx, vpt, b.sz, vpz, b.sy, b.slz, b.sly);
+        vy = rot_term(vy, vpz, b.sx, vpr, b.sz, b.slx, b.slz);
+        vz = rot_term(vz, vpr, b.sy, vpt, b.sx, b.sly, b.slx);
     } else {  // (x, y, z) ~ (r, z, theta), particles.cpp:968-979
-        const float vpr = fmaf(vz, ty, fmaf(-vy, tz, vx));
-        const float vpz = fmaf(vy, tx, fmaf(-vx, ty, vz));
-        const float vpt = fmaf(vx, tz, fmaf(-vz, tx, vy));
-        vx = fmaf(vpz, sy, fmaf(-vpt, sz, vx));
-        vy = fmaf(vpr, sz, fmaf(-vpz, sx, vy));
-        vz = fmaf(vpt, sx, fmaf(-vpr, sy, vz));
+        const float vpr = rot_term(vx, vz, b.ty, vy, b.tz, b.tly, b.tlz);
+        const float vpz = rot_term(vz, vy, b.tx, vx, b.ty, b.tlx, b.tly);
+        const float vpt = rot_term(vy, vx, b.tz, vz, b.tx, b.tlz, b.tlx);
+        vx = rot_term(vx, vpz, b.sy, vpt, b.sz, b.sly, b.slz);
+        vy = rot_term(vy, vpr, b.sz, vpz, b.sx, b.slz, b.slx);
+        vz = rot_term(vz, vpt, b.sx, vpr, b.sy, b.slx, b.sly);
     }
 }
 
@@ -249,9 +264,7 @@ __device__ __forceinline__ void step_particle(const PushArgs& a, uint32_t& x, ui
     vx = fmaf(ex, a.hq, vx);
     vz = fmaf(ez, a.hq, vz);
     if (BFIELD) {
-        float tx, ty, tz, sx, sy, sz;
-        boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
-        rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
+        rotate<COORD>(vx, vy, vz, boris_vectors(a, x, z));
     }
     vx = fmaf(ex, a.hq, vx);
     vz = fmaf(ez, a.hq, vz);
@@ -706,9 +719,7 @@ __global__ void __launch_bounds__(256) k_push_init(const PushArgs a)
     float vx = a.vx[k], vy = a.vy[k], vz = a.vz[k];
     float ex, ez;
     gather_E<EMODE>(a, x, z, a.phase, ex, ez);
-    float tx, ty, tz, sx, sy, sz;
-    boris_vectors(a, x, z, tx, ty, tz, sx, sy, sz);
-    rotate<COORD>(vx, vy, vz, tx, ty, tz, sx, sy, sz);
+    rotate<COORD>(vx, vy, vz, boris_vectors(a, x, z));
     vx = fmaf(ex, a.hq, vx);
     vz = fmaf(ez, a.hq, vz);
     a.vx[k] = vx;

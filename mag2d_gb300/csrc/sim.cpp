@@ -891,12 +891,16 @@ PushArgs Sim::push_args(int s, bool init)
     a.hq = (float)(init ? -q / m * dt / 2.0 : q / m * dt / 2.0);
     const double tx = p.Br * rot, ty = p.Bt * rot, tz = p.Bz * rot;
     const double f = 2.0 / (1 + tx * tx + ty * ty + tz * tz);
-    a.tx = (float)tx;
-    a.ty = (float)ty;
-    a.tz = (float)tz;
-    a.sx = (float)(tx * f);
-    a.sy = (float)(ty * f);
-    a.sz = (float)(tz * f);
+    auto split = [](double v, float& hi, float& lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+    };
+    split(tx, a.tx, a.tlx);
+    split(ty, a.ty, a.tly);
+    split(tz, a.tz, a.tlz);
+    split(tx * f, a.sx, a.slx);
+    split(ty * f, a.sy, a.sly);
+    split(tz * f, a.sz, a.slz);
     a.btab = p.magnetic_field_const ? 0 : 1;
     a.has_b = (a.btab || p.Br != 0.0 || p.Bt != 0.0 || p.Bz != 0.0) ? 1 : 0;
     a.Br = d_Br.p;

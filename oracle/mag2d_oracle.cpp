@@ -352,7 +352,8 @@ struct Species {
     std::string name;
     double mass, charge, dt, density, temperature, E_max, v_max, lifetime, t;
     unsigned long niter = 0;
-    int64_t ncoll = 0;
+    int64_t ncoll = 0;  // candidates (null collisions included)
+    int64_t nreal = 0;  // collisions that selected an interaction
     std::vector<Particle> p;
     std::vector<int> freelist;  // BaseSpecies::empty (particles.hpp:100)
     Field rho;
@@ -622,6 +623,7 @@ struct orc_sim {
             if (tmp > gamma) break;
         }
         if (intid == list.size()) return;  // null collision
+        s.nreal++;
         Interaction* in = list[intid];
         const double mass = s.mass;
         tmp = 1.0 / (mass + m2);
@@ -1352,6 +1354,7 @@ int orc_rng(orc_sim* s, int kind, int n, double arg, double* out)
 }
 
 int64_t orc_collisions(orc_sim* s, int sp) { return s->sp[sp]->ncoll; }
+int64_t orc_real_collisions(orc_sim* s, int sp) { return s->sp[sp]->nreal; }
 
 void orc_u_smooth(int nx, int nz, const double* in, double* out)
 {

@@ -76,6 +76,8 @@ int orc_sigma_v(orc_sim* s, int sp, int tgt, int n, const double* v, double* out
 int orc_rng(orc_sim* s, int kind, int n, double arg, double* out);
 /* Collision counter: number of scatter() calls per species since creation */
 int64_t orc_collisions(orc_sim* s, int sp);
+/* collisions that selected an interaction (the candidates minus the null collisions) */
+int64_t orc_real_collisions(orc_sim* s, int sp);
 
 /* Fixed-point CIC deposit (Field2D.hpp:45-62 with quantised weights): a
  * particle at fixed-point grid position (xf, zf) -- cells times 2^20 -- in

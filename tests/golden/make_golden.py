@@ -19,7 +19,7 @@ present), and stores inputs and outputs as small .npz files:
 
 The CPU tests replay the same inputs through the oracle port (bit-exact) and
 through the product's host-side parser and geometry builder.
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [reference tree]   (or MAG2D_REFERENCE=...)
 """
 from __future__ import annotations
 
@@ -34,7 +34,10 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent))
 from mag2d_cases import AMU, KB, QE, Ref, full_config, write_config, write_field_file, write_species_conf  # noqa: E402
 
-REF_ROOT = Path("/root/reference")
+import os  # noqa: E402
+
+# the reference tree: MAG2D_REFERENCE or the first argument overrides the default location
+REF_ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MAG2D_REFERENCE", "/root/reference"))
 TMP = Path(tempfile.mkdtemp(prefix="golden_"))
 
 

@@ -15,6 +15,8 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parents[1]
 PORT_SO = ROOT / "oracle" / "build" / "libmag2d_oracle.so"
+# the same port built with the reference's -Ofast, for CPU-baseline timing only
+PORT_TIMING_SO = ROOT / "oracle" / "build" / "libmag2d_oracle_timing.so"
 REF_SO = ROOT / "oracle" / "_ref" / "libmag2d_ref.so"
 
 # Physical constants of the reference (src/param.cpp:8-10)
@@ -176,15 +178,17 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(_D)
 
 
-def load_port() -> ctypes.CDLL:
-    if not PORT_SO.exists():
-        raise RuntimeError(f"oracle port not built: {PORT_SO} (run __graft_entry__.build())")
-    L = ctypes.CDLL(str(PORT_SO))
+def load_port(timing: bool = False) -> ctypes.CDLL:
+    so = PORT_TIMING_SO if timing else PORT_SO
+    if not so.exists():
+        raise RuntimeError(f"oracle port not built: {so} (run __graft_entry__.build())")
+    L = ctypes.CDLL(str(so))
     L.orc_create.restype = ctypes.c_void_p
     L.orc_create.argtypes = [ctypes.POINTER(OrcConfig), ctypes.c_void_p, ctypes.c_void_p]
     L.orc_last_error.restype = ctypes.c_char_p
     L.orc_time_advance.restype = ctypes.c_double
     L.orc_collisions.restype = ctypes.c_int64
+    L.orc_real_collisions.restype = ctypes.c_int64
     L.orc_u_smooth.restype = None
     L.orc_u_smooth.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     L.orc_deposit_fixed.restype = ctypes.c_int64
@@ -224,8 +228,8 @@ class Port:
     """The oracle port (oracle/mag2d_oracle.cpp) driven like the reference's Pic."""
 
     def __init__(self, cfg: dict, species: list, interactions: list, mask: np.ndarray,
-                 voltage: np.ndarray, seed: int = 1, loaded_fields=None):
-        self.L = load_port()
+                 voltage: np.ndarray, seed: int = 1, loaded_fields=None, timing: bool = False):
+        self.L = load_port(timing)
         self.cfg = cfg
         self._c = orc_config(cfg)
         mask = np.ascontiguousarray(mask, dtype=np.int8)
@@ -337,7 +341,19 @@ class Port:
         return out
 
     def collisions(self, sp: int) -> int:
+        """Null-collision candidates of species sp (scatter() calls)."""
         return int(self.L.orc_collisions(self.h, sp))
+
+    def real_collisions(self, sp: int) -> int:
+        """Candidates that selected an interaction (not a null collision)."""
+        return int(self.L.orc_real_collisions(self.h, sp))
+
+    def set_bfield(self, nx: int, nz: int, dx: float, dz: float, x0: float, z0: float, Br, Bz):
+        """Fields::load_magnetic_field tables (src/fields.cpp:870-959) as arrays."""
+        br = np.ascontiguousarray(Br, dtype=np.float64)
+        bz = np.ascontiguousarray(Bz, dtype=np.float64)
+        self._check(self.L.orc_set_bfield(self.h, nx, nz, ctypes.c_double(dx), ctypes.c_double(dz),
+                                          ctypes.c_double(x0), ctypes.c_double(z0), _dp(br), _dp(bz)))
 
 
 def to_fixed(v: np.ndarray) -> np.ndarray:

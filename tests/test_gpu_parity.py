@@ -3,8 +3,9 @@
 Tolerances:
   * deposit        — bit-exact against the oracle's fixed-point CIC deposit
   * Poisson solve  — |u_gpu - u_oracle|_inf <= 1e-9 |u_oracle|_inf
-  * trajectories   — positions within 1e-5 of the domain size after 1000 steps
-                     with collisions off (FP32 state against the FP64 oracle)
+  * trajectories   — every position within 1e-5 of the domain size after 1000
+                     steps with collisions off (FP32 state against the FP64
+                     oracle); velocities within the bounds each test states
   * MCC            — collision counts within 3 sigma of the expected count and a
                      two-sample KS test on energies at p > 0.01
 """
@@ -186,7 +187,10 @@ def test_deposit_bit_exact(m, tmp_path):
 
 
 # ---------------------------------------------------------------------------
-def _trajectory_case(m, tmp_path, make, nsteps, n, species_index, **kw):
+def _trajectory_case(m, tmp_path, make, nsteps, n, species_index, track_r=None, **kw):
+    """GPU and oracle after nsteps from the same particles; with track_r = (xc, zc)
+    the oracle is stepped one step at a time and the largest distance of each
+    particle from (xc, zc) along its orbit is returned as well."""
     out = make(tmp_path, n=n, **kw)
     cfg, species, inter, cpath, spath, parts = out[:6]
     loaded = out[6] if len(out) > 6 else None
@@ -199,34 +203,73 @@ def _trajectory_case(m, tmp_path, make, nsteps, n, species_index, **kw):
     port = _port_for(m, cfg, species, inter, cpath, seed=3, loaded=loaded)
     port.set_particles(species_index, *parts)
     port.advance_init()
-    port.advance(nsteps)
+    rmax = None
+    if track_r is None:
+        port.advance(nsteps)
+    else:
+        rmax = np.zeros(n)
+        for _ in range(nsteps):
+            port.advance(1)
+            o = port.particles(species_index)
+            rmax = np.maximum(rmax, np.hypot(o[:, 0] - track_r[0], o[:, 2] - track_r[1]))
     o = port.particles(species_index)
     pic.close()
-    return g, o
+    return g, o, rmax
+
+
+def _trajectory_errors(g, o, lx, lz):
+    """Per matched particle: position error relative to the domain size, and
+    velocity error |dv| relative to the particle's own speed and to v_rms."""
+    common, sel, live = _match(g, o)
+    assert len(common) >= live.sum() - 2
+    ep = np.maximum(np.abs(g["x"][sel] - o[common, 0]) / lx, np.abs(g["z"][sel] - o[common, 2]) / lz)
+    vg = np.stack([g["vx"][sel], g["vy"][sel], g["vz"][sel]], axis=1)
+    vo = o[common][:, 3:6]
+    dv = np.linalg.norm(vg - vo, axis=1)
+    vmag = np.linalg.norm(vo, axis=1)
+    vrms = np.sqrt((vo ** 2).sum(axis=1).mean())
+    return common, ep, dv / vmag, dv / vrms
 
 
 def test_penning_trajectories_1000_steps(m, tmp_path):
+    """Self-consistent Penning trap (C0 grid), 2000 electrons, 1000 steps with
+    collisions off: every position within 1e-5 of the domain size of the
+    oracle's (measured max 1e-6).  Velocities: |dv|/|v| <= 5e-5 for every
+    electron (measured max 2.2e-5, median 1e-5).  The velocity bound is
+    that of FP32 state, not of the orbits: at omega_c dt = 1.76 rad per step
+    each component passes through about ten roundings at the scale of |v| per
+    step (Boris rotation, both half accelerations, the r map), a random walk
+    of ~3e-8 x sqrt(10 x 1000); the FP64 oracle itself carries a 6e-8
+    perturbation of its inputs to only 1e-7 over the same run."""
     from cases import penning_rz
 
-    g, o = _trajectory_case(m, tmp_path, penning_rz, 1000, 2000, 0)
-    common, sel, live = _match(g, o)
-    assert len(common) >= live.sum() - 2
-    ex = np.abs(g["x"][sel] - o[common, 0]) / 5e-3
-    ez = np.abs(g["z"][sel] - o[common, 2]) / 20e-3
-    assert np.percentile(np.maximum(ex, ez), 99) < 1e-5, (ex.max(), ez.max())
-    assert max(ex.max(), ez.max()) < 1e-4
+    g, o, _ = _trajectory_case(m, tmp_path, penning_rz, 1000, 2000, 0)
+    _, ep, dvv, _ = _trajectory_errors(g, o, 5e-3, 20e-3)
+    assert ep.max() <= 1e-5, ep.max()
+    assert dvv.max() <= 5e-5, (dvv.max(), np.median(dvv))
 
 
 def test_multipole_trajectories_1000_steps(m, tmp_path):
+    """22-pole RF trap on the 257 x 257 grid of the bench workload, 2000 ions,
+    1000 steps, collisions off: every position within 1e-5 of the domain size
+    (measured max 2.8e-6).  Velocities: every ion whose orbit stays inside
+    r < 0.7 r0 = 3.5 mm (the oracle's orbit) within |dv| <= 1e-5 v_rms
+    (measured max 4e-6); every ion within 1e-4 v_rms (measured max 4.6e-5).
+    The outer ions reach the RF wall, where the field grows as r^10 and turns
+    a position difference into a velocity difference about ten times larger:
+    the FP64 oracle itself carries a 6e-8 perturbation of its inputs to
+    4e-6 v_rms on those ions (5e-7 on the inner ones), and the GPU's FP32
+    rounding enters at every step."""
     from cases import multipole_xy
 
-    g, o = _trajectory_case(m, tmp_path, multipole_xy, 1000, 2000, 1, collisions=False, n_nodes=129)
-    common, sel, live = _match(g, o)
-    assert len(common) >= live.sum() - 2
-    ex = np.abs(g["x"][sel] - o[common, 0]) / 10e-3
-    ez = np.abs(g["z"][sel] - o[common, 2]) / 10e-3
-    assert np.percentile(np.maximum(ex, ez), 99) < 1e-5, (ex.max(), ez.max())
-    assert max(ex.max(), ez.max()) < 1e-4
+    g, o, rmax = _trajectory_case(m, tmp_path, multipole_xy, 1000, 2000, 1, track_r=(5e-3, 5e-3), collisions=False,
+                                  n_nodes=257)
+    common, ep, _, dvr = _trajectory_errors(g, o, 10e-3, 10e-3)
+    assert ep.max() <= 1e-5, ep.max()
+    inner = rmax[common] < 3.5e-3
+    assert inner.sum() > 300
+    assert dvr[inner].max() <= 1e-5, dvr[inner].max()
+    assert dvr.max() <= 1e-4, dvr.max()
 
 
 @pytest.mark.parametrize("direct", [-1, 1], ids=["multigrid", "inverse"])
@@ -263,16 +306,15 @@ def test_u_smooth_matches_oracle(m, tmp_path, direct):
 
 
 def test_u_smooth_trajectories_500_steps(m, tmp_path):
-    """A self-consistent Penning run with u_smooth = 1 against the oracle."""
+    """A self-consistent Penning run with u_smooth = 1 against the oracle, 500
+    steps: positions within 1e-5 of the domain size, velocities within the
+    FP32 bound of the Penning test."""
     from cases import penning_rz
 
-    g, o = _trajectory_case(m, tmp_path, penning_rz, 500, 2000, 0, u_smooth=1)
-    common, sel, live = _match(g, o)
-    assert len(common) >= live.sum() - 2
-    ex = np.abs(g["x"][sel] - o[common, 0]) / 5e-3
-    ez = np.abs(g["z"][sel] - o[common, 2]) / 20e-3
-    assert np.percentile(np.maximum(ex, ez), 99) < 1e-5, (ex.max(), ez.max())
-    assert max(ex.max(), ez.max()) < 1e-4
+    g, o, _ = _trajectory_case(m, tmp_path, penning_rz, 500, 2000, 0, u_smooth=1)
+    _, ep, dvv, _ = _trajectory_errors(g, o, 5e-3, 20e-3)
+    assert ep.max() <= 1e-5, ep.max()
+    assert dvv.max() <= 5e-5, dvv.max()
 
 
 # ---------------------------------------------------------------------------
