@@ -151,6 +151,21 @@ int mag_field_solve(mag_sim* sim, mag_solve_info* info);
  * direct solve has no iteration count). */
 int mag_solve_status(mag_sim* sim, mag_solve_info* info);
 
+/* Phase times of the multigrid Poisson solve (the time spent inside
+ * Fields::boundary_solve, src/fields.cpp:278-312, by part).  The first call
+ * switches the timing on for every later solve of the handle (thread 0 of
+ * block 0 reads the GPU's global timer after each grid-wide barrier; cost:
+ * one memset per solve) and returns zeros.  Later calls return the times of
+ * the most recent multigrid solve in ms (solves by the precomputed inverse
+ * are not timed):
+ *   [0] start (extrapolated start, right-hand side)  [1] FP64 residuals with
+ *   their max reductions  [2 + l] down part of level l (smoothing, residual,
+ *   restriction; l < 12)  [14] the coarse levels run by block 0, or the
+ *   coarsest solve  [15 + l] up part of level l (prolongation, smoothing; on
+ *   level 0 also the update of u)  [27] face field  [28] whole solve.
+ * Writes min(cap, 29) values; returns that number. */
+int mag_solve_phase_times(mag_sim* sim, double* ms_out, int cap);
+
 /* Live particles of a species as SoA doubles in SI units (the t_particle
  * fields x, z, vx, vy, vz of src/particles.hpp:26-33) plus a persistent id.
  * Any pointer may be NULL.  *n_out receives the number written (<= cap). */

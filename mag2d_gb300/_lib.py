@@ -94,6 +94,7 @@ def lib() -> ctypes.CDLL:
     L.mag_sync.argtypes = [P]
     L.mag_advance_timed.argtypes = [P, ctypes.c_uint64, D]
     L.mag_solve_status.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
+    L.mag_solve_phase_times.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
     L.mag_rho_fixed_ptr.argtypes = [P, ctypes.c_int]
     L.mag_rho_fixed_ptr.restype = ctypes.c_void_p
     L.mag_set_rho_fixed.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]

@@ -272,6 +272,15 @@ int mag_solve_status(mag_sim* sim, mag_solve_info* info)
     });
 }
 
+int mag_solve_phase_times(mag_sim* sim, double* ms_out, int cap)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!ms_out || cap <= 0) throw mag::Error(MAG_EINVAL, "null argument");
+        return sim->s->solve_phase_times(ms_out, cap);
+    });
+}
+
 int mag_get_particles(mag_sim* sim, int species, int64_t cap, double* x, double* z, double* vx, double* vy,
                       double* vz, uint32_t* id, int64_t* n_out)
 {

@@ -166,6 +166,7 @@ void Batch::pack(const Layout& L, Slot& slot)
         Sim& s = *sp;
         if (s.p.selfconsistent && (long long)s.nx * s.nz <= kSingleBlockNodes) {
             solves.emplace_back((long long)s.nx * s.nz, s.solve_args(false, s.rho_override ? 2 : 1, true));
+            solves.back().second.prof = nullptr;  // one block per instance: no phase timing
             s.rho_override = false;
         }
     }

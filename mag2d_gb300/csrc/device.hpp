@@ -27,6 +27,17 @@ constexpr int kMaxInteractions = 64;
 constexpr int kMaxLevels = 12;
 constexpr long long kSingleBlockNodes = 70000;  // grids up to this size run on one block
 constexpr long long kSingleBlockLevel = 4096;   // levels of a multi-block solve up to this size run on block 0
+// tile phases of a multi-block solve: halo rings around a tile's interior (the
+// four colour passes of a phase plus two) and shared bytes per region node
+// (FP32 correction, FP32 right-hand side / residual, one flag byte)
+constexpr int kTileHalo = 6;
+constexpr int kTileNodeBytes = 9;
+// phase times of one solve (mag_solve_phase_times): start and right-hand side,
+// FP64 residual with its reduction, the down part of each level, the coarse
+// part run by block 0 (or the coarsest solve), the up part of each level, the
+// face field, and the whole solve
+constexpr int kPhaseStart = 0, kPhaseResidual = 1, kPhaseDown = 2, kPhaseCoarse = 2 + 12, kPhaseUp = 3 + 12,
+              kPhaseFaces = 3 + 24, kPhaseTotal = 4 + 24, kSolvePhases = 5 + 24;
 constexpr long long kGreenMaxNodes = 20000;     // grids up to this size solve by the precomputed inverse
 constexpr int kFracBits = 20;      // fixed-point fraction of a cell in the positions
 constexpr int kDepositShift = 20;  // CIC weights quantised to 2^-20 per axis (= kFracBits)
@@ -339,6 +350,7 @@ struct MGLevelDev {
     float* t;               // residual scratch
     const float* coef;      // 9 planes of nx*nz (levels >= 1), plane k = (di+1)*3 + (dj+1)
     const float* inv_diag;  // levels >= 1
+    int ti, tj;             // multi-block solves: interior size of this level's tiles (0: not tiled)
 };
 
 struct SolveArgs {
@@ -367,6 +379,7 @@ struct SolveArgs {
     double k2;              // s/n coefficient of the fine stencil
     int nlev;
     int l_single;           // multi-block solves: first level run by block 0 alone (0: none)
+    int tiled;              // multi-block solves: levels above l_single run as tile phases (dynamic shared memory)
     const float* coarse_inv;  // dense inverse of the coarsest level, column-major (null: smooth it)
     MGLevelDev lev[kMaxLevels];
     int nu1, nu2, ncoarse;
@@ -379,6 +392,7 @@ struct SolveArgs {
     GridBarrier* bar;
     SolveStatus* status;
     int* err;
+    double* prof;           // phase times of the solve [ns] (kSolvePhases slots), or null
 };
 
 // Adjoint of one particle step (or of the leapfrog start) for every particle

@@ -66,11 +66,12 @@ int launch_collide_batch(const CollideArgs* d_args, int nitems, int max_tables, 
 // counting sort by cell with compaction; n_src = slots of the source arrays
 int launch_sort(const SortArgs& a, long long n_src, cudaStream_t s);
 // whole FP64-refined multigrid solve in one kernel; nblocks > 1 uses a
-// cooperative launch with a bounded grid barrier
-int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s);
-// blocks of 1024 threads a cooperative launch of the solve can have (1 when
-// the device cannot launch cooperatively)
-int solve_max_blocks(int sm_count);
+// cooperative launch with a bounded grid barrier, smem bytes of dynamic
+// shared memory per block for the tile phases (a.tiled)
+int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s, size_t smem = 0);
+// blocks of 1024 threads a cooperative launch of the solve can have with smem
+// bytes of dynamic shared memory (1 when the device cannot launch cooperatively)
+int solve_max_blocks(int sm_count, size_t smem = 0);
 // n independent single-block solves, arguments in device memory (one block of
 // 'threads' threads each; grids up to kSingleBlockNodes nodes)
 int launch_solve_batch(const SolveArgs* d_args, int n, int threads, cudaStream_t s);

@@ -184,4 +184,23 @@ bool dense_inverse(int nx, int nz, const std::vector<double>& A9, std::vector<fl
     return true;
 }
 
+void choose_tile(int nx, int nz, int nblocks, int halo, long long budget_nodes, int& ti, int& tj)
+{
+    long long best = -1, best_reg = 0;
+    ti = tj = 1;
+    for (int a = 1; a <= std::min(nx, 512); ++a)
+        for (int b = 1; b <= std::min(nz, 1024); ++b) {
+            const long long reg = (long long)(a + 2 * halo) * (b + 2 * halo);
+            if (reg > budget_nodes) break;
+            const long long tiles = (long long)((nx + a - 1) / a) * ((nz + b - 1) / b);
+            const long long cost = (tiles + nblocks - 1) / nblocks * reg;
+            if (best < 0 || cost < best || (cost == best && reg < best_reg)) {
+                best = cost;
+                best_reg = reg;
+                ti = a;
+                tj = b;
+            }
+        }
+}
+
 }  // namespace mag

@@ -39,4 +39,9 @@ void fine_stencil_table(int coord, int nx, double dx, double dz, std::vector<dou
 // (inv[col * n + row]).  Returns false when the operator is singular.
 bool dense_inverse(int nx, int nz, const std::vector<double>& A9, std::vector<float>& inv);
 
+// Tile of a level of a multi-block solve: the interior size ti x tj that
+// minimises (tiles per block, rounded up) x (region nodes), the region being
+// the tile with halo rings on each side, within budget_nodes region nodes.
+void choose_tile(int nx, int nz, int nblocks, int halo, long long budget_nodes, int& ti, int& tj);
+
 }  // namespace mag

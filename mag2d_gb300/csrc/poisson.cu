@@ -41,6 +41,22 @@ struct Team {
     unsigned nblocks;
     unsigned tid, nthreads;
     unsigned epoch = 0;  // barriers passed so far (the same in every thread)
+    double* prof = nullptr;  // phase times (thread 0 of block 0 records them), or null
+    unsigned long long t_mark = 0;
+    __device__ static unsigned long long now()
+    {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        return t;
+    }
+    // add the time since the last mark to phase slot `phase` (called after a barrier)
+    __device__ void mark(int phase)
+    {
+        if (prof == nullptr || blockIdx.x != 0 || threadIdx.x != 0) return;
+        const unsigned long long t = now();
+        prof[phase] += (double)(t - t_mark);
+        t_mark = t;
+    }
     __device__ Team(GridBarrier* b)
         : bar(b), nblocks(gridDim.x), tid(blockIdx.x * blockDim.x + threadIdx.x), nthreads(gridDim.x * blockDim.x)
     {
@@ -396,15 +412,18 @@ __device__ void vcycle_from(const SolveArgs& a, Team& t, int l0, bool& ok)
         if (!ok) return;
         restrict_level(a, t, l, a.lev[l].t);
         ok = t.sync();
+        t.mark(kPhaseDown + l);
     }
     if (!ok) return;
     coarse_solve(a, t, ok);
+    t.mark(kPhaseCoarse);
     for (int l = L - 2; l >= l0 && ok; --l) {
         prolong_level(a, t, l);
         ok = t.sync();
         if (!ok) return;
         if (l == 0) smooth_fine(a, t, a.nu2, true, 1.f, ok);
         else smooth_coarse(a, t, l, a.nu2, true, ok);
+        t.mark(kPhaseUp + l);
     }
 }
 
@@ -436,6 +455,7 @@ __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
         if (!ok) return;
         restrict_level(a, t, l, a.lev[l].t);
         ok = t.sync();
+        t.mark(kPhaseDown + l);
     }
     if (!ok) return;
     if (blockIdx.x == 0) {
@@ -445,12 +465,322 @@ __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
         __threadfence();
     }
     ok = t.sync();
+    t.mark(kPhaseCoarse);
     for (int l = ls - 1; l >= 0 && ok; --l) {
         prolong_level(a, t, l);
         ok = t.sync();
         if (!ok) return;
         if (l == 0) smooth_fine(a, t, a.nu2, true, 1.f, ok);
         else smooth_coarse(a, t, l, kCoarseSweepsGrid, true, ok);
+        t.mark(kPhaseUp + l);
+    }
+}
+
+// ---- tile phases of a multi-block solve -------------------------------------
+//
+// On the levels above l_single every block owns tiles of ti x tj nodes.  A
+// phase stages a tile and kTileHalo rings around it in shared memory, runs
+// all colour passes of the phase there and writes back only the tile: pass p
+// updates the nodes at most kTileHalo - 1 - p rings out, which are exactly
+// the nodes whose neighbours are still up to date in shared memory, so the
+// tile's values equal those of the same colour passes over the whole level.
+// Down phase of level l: pre-smoothing from e = 0, residual, restriction to
+// level l + 1 (one grid barrier instead of one per colour pass, residual and
+// restriction).  Up phase: prolongation of level l + 1's correction,
+// post-smoothing and, on the fine level, the FP64 update u += e.
+struct TileRegion {
+    int i0, j0, ni, nj;  // interior: rows i0 .. i0+ni-1, columns j0 .. j0+nj-1
+    int ri, rj;          // global indices of region node (0, 0)
+    int rh, rw;          // region rows and columns
+};
+
+__device__ __forceinline__ TileRegion tile_region(int t, int nx, int nz, int ti, int tj)
+{
+    const int ntj = (nz + tj - 1) / tj;
+    const int a = t / ntj, b = t - a * ntj;
+    TileRegion T;
+    T.i0 = a * ti;
+    T.j0 = b * tj;
+    T.ni = min(ti, nx - T.i0);
+    T.nj = min(tj, nz - T.j0);
+    T.ri = T.i0 - kTileHalo;
+    T.rj = T.j0 - kTileHalo;
+    T.rh = T.ni + 2 * kTileHalo;
+    T.rw = T.nj + 2 * kTileHalo;
+    return T;
+}
+
+// rings between region node (li, lj) and the tile interior (0 inside)
+__device__ __forceinline__ int tile_ring(const TileRegion& T, int li, int lj)
+{
+    const int di = max(max(kTileHalo - li, li - (T.ni + kTileHalo - 1)), 0);
+    const int dj = max(max(kTileHalo - lj, lj - (T.nj + kTileHalo - 1)), 0);
+    return max(di, dj);
+}
+
+struct TileShared {
+    float* e;    // correction
+    float* r;    // right-hand side, overwritten by the residual
+    uint8_t* f;  // 1: outside the grid, or a fixed node of the fine level
+};
+
+__device__ __forceinline__ TileShared tile_shared(const TileRegion& T)
+{
+    extern __shared__ __align__(16) unsigned char tile_smem[];
+    const int n = T.rh * T.rw;
+    TileShared S;
+    S.e = reinterpret_cast<float*>(tile_smem);
+    S.r = S.e + n;
+    S.f = reinterpret_cast<uint8_t*>(S.r + n);
+    return S;
+}
+
+// stage r (and e, or zeros) and the flags of the region
+__device__ void tile_load(const SolveArgs& a, int l, const TileRegion& T, const TileShared& S, bool load_e)
+{
+    const MGLevelDev& L = a.lev[l];
+    const int n = T.rh * T.rw;
+    const FastDiv dw((unsigned)T.rw);
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
+        const int gi = T.ri + li, gj = T.rj + lj;
+        const bool in = gi >= 0 && gi < L.nx && gj >= 0 && gj < L.nz;
+        const size_t k = in ? (size_t)gi * L.nz + gj : 0;
+        S.r[q] = in ? L.r[k] : 0.f;
+        S.e[q] = (in && load_e) ? L.e[k] : 0.f;
+        S.f[q] = (!in || (l == 0 && is_fixed(a.mask[k]))) ? 1 : 0;
+    }
+}
+
+// one colour pass over the region nodes at most `reach` rings out
+__device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const TileShared& S, int color, int reach)
+{
+    const MGLevelDev& L = a.lev[l];
+    if (l == 0) {  // red-black Gauss-Seidel on the 5-point operator (smooth_fine, omega = 1)
+        const float* __restrict__ st = a.st32;
+        const float k2 = (float)a.k2;
+        const int hw = (T.rw + 1) / 2;
+        const int n = T.rh * hw;
+        const FastDiv dh((unsigned)hw);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int li = (int)dh.div((unsigned)q);
+            const int lj = 2 * (q - li * hw) + ((color + T.ri + T.rj + li) & 1);
+            if (lj >= T.rw || tile_ring(T, li, lj) > reach) continue;
+            const int p = li * T.rw + lj;
+            if (S.f[p]) continue;
+            const int i = T.ri + li;
+            float acc = S.r[p];
+            if (i > 0) acc -= st[4 * i] * S.e[p - T.rw];
+            acc -= st[4 * i + 1] * S.e[p + T.rw];
+            acc -= k2 * S.e[p - 1];
+            acc -= k2 * S.e[p + 1];
+            S.e[p] = acc / st[4 * i + 2];
+        }
+    } else {  // 4-colour Gauss-Seidel on the 9-point Galerkin operator (smooth_coarse)
+        const int ci = color >> 1, cj = color & 1;
+        const int hh = (T.rh + 1) / 2, hw = (T.rw + 1) / 2;
+        const int n = hh * hw;
+        const FastDiv dh((unsigned)hw);
+        const size_t nn = (size_t)L.nx * L.nz;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const int a2 = (int)dh.div((unsigned)q);
+            const int li = 2 * a2 + ((ci + T.ri) & 1);
+            const int lj = 2 * (q - a2 * hw) + ((cj + T.rj) & 1);
+            if (li >= T.rh || lj >= T.rw || tile_ring(T, li, lj) > reach) continue;
+            const int p = li * T.rw + lj;
+            if (S.f[p]) continue;
+            const int i = T.ri + li, j = T.rj + lj;
+            const size_t k = (size_t)i * L.nz + j;
+            float off = 0.f;
+#pragma unroll
+            for (int di = -1; di <= 1; ++di) {
+                if (i + di < 0 || i + di >= L.nx) continue;
+#pragma unroll
+                for (int dj = -1; dj <= 1; ++dj) {
+                    if (j + dj < 0 || j + dj >= L.nz) continue;
+                    if (di == 0 && dj == 0) continue;
+                    off += __ldg(&L.coef[((di + 1) * 3 + (dj + 1)) * nn + k]) * S.e[p + di * T.rw + dj];
+                }
+            }
+            S.e[p] = (S.r[p] - off) * __ldg(&L.inv_diag[k]);
+        }
+    }
+}
+
+// residual t = r - A e in place of r, for the region nodes at most `reach` rings out
+__device__ void tile_residual(const SolveArgs& a, int l, const TileRegion& T, const TileShared& S, int reach)
+{
+    const MGLevelDev& L = a.lev[l];
+    const int n = T.rh * T.rw;
+    const FastDiv dw((unsigned)T.rw);
+    const float* __restrict__ st = a.st32;
+    const float k2 = (float)a.k2;
+    const size_t nn = (size_t)L.nx * L.nz;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
+        if (tile_ring(T, li, lj) > reach) continue;
+        if (S.f[q]) {
+            S.r[q] = 0.f;
+            continue;
+        }
+        const int i = T.ri + li, j = T.rj + lj;
+        float acc;
+        if (l == 0) {
+            acc = S.r[q] - st[4 * i + 2] * S.e[q];
+            if (i > 0) acc -= st[4 * i] * S.e[q - T.rw];
+            acc -= st[4 * i + 1] * S.e[q + T.rw];
+            acc -= k2 * S.e[q - 1];
+            acc -= k2 * S.e[q + 1];
+        } else {
+            const size_t k = (size_t)i * L.nz + j;
+            float ae = 0.f;
+#pragma unroll
+            for (int di = -1; di <= 1; ++di) {
+                if (i + di < 0 || i + di >= L.nx) continue;
+#pragma unroll
+                for (int dj = -1; dj <= 1; ++dj) {
+                    if (j + dj < 0 || j + dj >= L.nz) continue;
+                    ae += __ldg(&L.coef[((di + 1) * 3 + (dj + 1)) * nn + k]) * S.e[q + di * T.rw + dj];
+                }
+            }
+            acc = S.r[q] - ae;
+        }
+        S.r[q] = acc;
+    }
+}
+
+// down phase of level l: pre-smoothing, residual, restriction to level l + 1
+__device__ void tile_down(const SolveArgs& a, int l)
+{
+    const MGLevelDev& L = a.lev[l];
+    const MGLevelDev& C = a.lev[l + 1];
+    const int ntiles = ((L.nx + L.ti - 1) / L.ti) * ((L.nz + L.tj - 1) / L.tj);
+    const int sweeps = l == 0 ? a.nu1 : kCoarseSweepsGrid;
+    const int ncolors = l == 0 ? 2 : 4;
+    for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
+        const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
+        const TileShared S = tile_shared(T);
+        tile_load(a, l, T, S, false);
+        __syncthreads();
+        int pass = 0;
+        for (int s = 0; s < sweeps; ++s)
+            for (int c = 0; c < ncolors; ++c, ++pass) {
+                tile_pass(a, l, T, S, c, kTileHalo - 1 - pass);
+                __syncthreads();
+            }
+        // the tile's correction back to the level (read again by the up phase)
+        for (int q = threadIdx.x; q < T.ni * T.nj; q += blockDim.x) {
+            const int ii = q / T.nj, jj = q - ii * T.nj;
+            L.e[(size_t)(T.i0 + ii) * L.nz + T.j0 + jj] = S.e[(ii + kTileHalo) * T.rw + jj + kTileHalo];
+        }
+        tile_residual(a, l, T, S, kTileHalo - 1 - pass);
+        __syncthreads();
+        // coarse nodes (I, J) whose fine node (2I, 2J) lies in the tile (restrict_level)
+        const int I0 = (T.i0 + 1) / 2, I1 = (T.i0 + T.ni - 1) / 2;
+        const int J0 = (T.j0 + 1) / 2, J1 = (T.j0 + T.nj - 1) / 2;
+        const int cw = J1 - J0 + 1, nc = (I1 - I0 + 1) * cw;
+        for (int q = threadIdx.x; q < nc; q += blockDim.x) {
+            const int I = I0 + q / cw, J = J0 + q % cw;
+            float acc = 0.f;
+#pragma unroll
+            for (int di = -1; di <= 1; ++di) {
+                const int i = 2 * I + di;
+                if (i < 0 || i >= L.nx) continue;
+                const float wi = di == 0 ? 1.f : 0.5f;
+#pragma unroll
+                for (int dj = -1; dj <= 1; ++dj) {
+                    const int j = 2 * J + dj;
+                    if (j < 0 || j >= L.nz) continue;
+                    const float wj = dj == 0 ? 1.f : 0.5f;
+                    acc += wi * wj * S.r[(i - T.ri) * T.rw + (j - T.rj)];
+                }
+            }
+            const size_t K = (size_t)I * C.nz + J;
+            C.r[K] = acc;
+            C.e[K] = 0.f;
+        }
+        __syncthreads();
+    }
+}
+
+// up phase of level l: prolongation of level l + 1's correction, post-smoothing,
+// and on the fine level the FP64 update of u.  The phase reads the pre-smoothed
+// correction of its halo from L.e, which the down phase wrote, and writes its
+// post-smoothed tile to L.t, so that no block reads what another one writes
+// in the same phase; level l - 1 prolongs from L.t (level l_single's
+// correction, computed by block 0, stays in its e).
+__device__ void tile_up(const SolveArgs& a, int l)
+{
+    const MGLevelDev& L = a.lev[l];
+    const MGLevelDev& C = a.lev[l + 1];
+    const float* __restrict__ ce = l + 1 < a.l_single ? C.t : C.e;
+    const int ntiles = ((L.nx + L.ti - 1) / L.ti) * ((L.nz + L.tj - 1) / L.tj);
+    const int sweeps = l == 0 ? a.nu2 : kCoarseSweepsGrid;
+    const int ncolors = l == 0 ? 2 : 4;
+    for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
+        const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
+        const TileShared S = tile_shared(T);
+        tile_load(a, l, T, S, true);
+        __syncthreads();
+        // e += P e_coarse on every region node of the grid (prolong_level)
+        const int n = T.rh * T.rw;
+        const FastDiv dw((unsigned)T.rw);
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            if (S.f[q]) continue;
+            const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
+            const int i = T.ri + li, j = T.rj + lj;
+            const int I0 = i >> 1, J0 = j >> 1;
+            const bool oi = i & 1, oj = j & 1;
+            const size_t b = (size_t)I0 * C.nz + J0;
+            float v;
+            if (!oi && !oj) v = ce[b];
+            else if (oi && !oj) v = 0.5f * (ce[b] + ce[b + C.nz]);
+            else if (!oi && oj) v = 0.5f * (ce[b] + ce[b + 1]);
+            else v = 0.25f * (ce[b] + ce[b + C.nz] + ce[b + 1] + ce[b + C.nz + 1]);
+            S.e[q] += v;
+        }
+        __syncthreads();
+        int pass = 0;
+        for (int s = 0; s < sweeps; ++s)
+            for (int c = ncolors - 1; c >= 0; --c, ++pass) {
+                tile_pass(a, l, T, S, c, kTileHalo - 1 - pass);
+                __syncthreads();
+            }
+        for (int q = threadIdx.x; q < T.ni * T.nj; q += blockDim.x) {
+            const int ii = q / T.nj, jj = q - ii * T.nj;
+            const int p = (ii + kTileHalo) * T.rw + jj + kTileHalo;
+            const size_t k = (size_t)(T.i0 + ii) * L.nz + T.j0 + jj;
+            if (l > 0) L.t[k] = S.e[p];
+            else if (!S.f[p]) a.u[k] += (double)S.e[p];
+        }
+        __syncthreads();
+    }
+}
+
+// One V-cycle of a multi-block solve with tile phases on the levels above
+// l_single and block 0 alone below; ends with u += e (done by the fine level's
+// up phase).
+__device__ void vcycle_tiled(const SolveArgs& a, Team& t, bool& ok)
+{
+    const int ls = a.l_single;
+    for (int l = 0; l < ls && ok; ++l) {
+        tile_down(a, l);
+        ok = t.sync();
+        t.mark(kPhaseDown + l);
+    }
+    if (!ok) return;
+    if (blockIdx.x == 0) {
+        Team tb = Team::block(a.bar);
+        bool okb = true;
+        vcycle_from(a, tb, ls, okb);
+        __threadfence();
+    }
+    ok = t.sync();
+    t.mark(kPhaseCoarse);
+    for (int l = ls - 1; l >= 0 && ok; --l) {
+        tile_up(a, l);
+        ok = t.sync();
+        t.mark(kPhaseUp + l);
     }
 }
 
@@ -459,6 +789,9 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
     const int nx = a.nx, nz = a.nz;
     const unsigned nn = (unsigned)(nx * nz);
     bool ok = true;
+    t.prof = a.prof;
+    const unsigned long long t_start = Team::now();
+    t.t_mark = t_start;
     // 0. start of a step's solve: the linear extrapolation of the last two solutions
     if (a.u_prev) {
         const bool valid = *((volatile const int*)a.u_prev_valid) != 0;
@@ -493,6 +826,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
             for (int s = 0; s < a.nsp; ++s) ((unsigned long long*)a.rho_fixed[s])[k] = 0ull;
     }
     ok = t.sync();
+    t.mark(kPhaseStart);
     // 2. FP64 residual refinement around the FP32 multigrid
     int it = 0;
     double res = 0.0, ref0 = 0.0;
@@ -544,6 +878,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
                 a.red[3 - slot] = 0.0;
             }
         }
+        t.mark(kPhaseResidual);
         // relative to max|u|; a cold start from u = 0 (a homogeneous solve)
         // measures against its own initial residual instead
         if (it == 0) ref0 = lres;
@@ -554,6 +889,12 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
             break;
         }
         if (it >= a.max_outer) break;
+        if (a.tiled && t.nblocks > 1) {
+            // the barrier of the reduction above already ordered F.r; the fine
+            // level's up phase adds the correction to u
+            vcycle_tiled(a, t, ok);
+            continue;
+        }
         ok = t.sync();
         if (!ok) break;
         vcycle(a, t, ok);
@@ -561,9 +902,12 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
         for (unsigned k = t.tid; k < nn; k += t.nthreads)
             if (!is_fixed(a.mask[k])) a.u[k] += (double)F.e[k];
         ok = t.sync();
+        t.mark(kPhaseUp);
     }
     // 3. face electric field E = -grad u for the particle kernel
     if (ok && a.Exf != nullptr) faces_pass(a.u, nx, nz, a.idx, a.idz, a.Exf, a.Ezf, t.tid, t.nthreads);
+    t.mark(kPhaseFaces);
+    if (a.prof && blockIdx.x == 0 && threadIdx.x == 0) a.prof[kPhaseTotal] += (double)(Team::now() - t_start);
     if (t.tid == 0) {
         a.status->iterations = it;
         a.status->residual = res;
@@ -836,23 +1180,38 @@ __global__ void k_faces(const double* __restrict__ u, int nx, int nz, double idx
 
 }  // namespace
 
-int solve_max_blocks(int sm_count)
+// allow smem bytes of dynamic shared memory for k_solve (false when refused)
+bool solve_allow_smem(size_t smem)
+{
+    static size_t allowed = 0;
+    if (smem <= allowed) return true;
+    if (cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    allowed = smem;
+    return true;
+}
+
+int solve_max_blocks(int sm_count, size_t smem)
 {
     int per_sm = 0, coop = 0, dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 1;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve, 1024, 0) != cudaSuccess || per_sm < 1)
+    if (smem && !solve_allow_smem(smem)) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve, 1024, smem) != cudaSuccess || per_sm < 1)
         return 1;
     return per_sm * sm_count;
 }
 
-int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s)
+int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s, size_t smem)
 {
     if (nblocks <= 1) {
         k_solve<<<1, 1024, 0, s>>>(a);
     } else {
+        if (smem) solve_allow_smem(smem);
         void* args[] = {(void*)&a};
-        cudaLaunchCooperativeKernel((const void*)k_solve, dim3(nblocks), dim3(1024), args, 0, s);
+        cudaLaunchCooperativeKernel((const void*)k_solve, dim3(nblocks), dim3(1024), args, smem, s);
     }
     return 1;
 }

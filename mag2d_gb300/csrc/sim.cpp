@@ -538,21 +538,51 @@ void Sim::run_solve(SolveArgs a)
     // cooperative launch; their coarse levels below that size run on block 0
     int nblocks = 1;
     a.l_single = 0;
+    a.tiled = 0;
     if ((long long)nx * nz > kSingleBlockNodes) {
-        if (solve_blocks == 0) solve_blocks = std::min(solve_max_blocks(sm_count), sm_count);
+        int ls = lv.nlev;
+        for (int l = 0; l < lv.nlev; ++l)
+            if ((long long)lv.nx[l] * lv.nz[l] <= kSingleBlockLevel) {
+                ls = l;
+                break;
+            }
+        if (solve_blocks == 0) {
+            // tile phases on the levels above ls: one tile region per block in
+            // shared memory (up to 200 KB), when the pre- and post-smoothing
+            // passes fit the halo and the cooperative launch keeps one block per SM
+            const long long budget = (200LL << 10) / kTileNodeBytes;
+            const int base_blocks = std::min(solve_max_blocks(sm_count), sm_count);
+            const bool fits = ls > 0 && ls < lv.nlev && 2 * std::max(a.nu1, a.nu2) <= kTileHalo - 2;
+            lv.ti.assign(lv.nlev, 0);
+            lv.tj.assign(lv.nlev, 0);
+            lv.tile_smem = 0;
+            if (fits && base_blocks > 1) {
+                long long region = 0;
+                for (int l = 0; l < ls; ++l) {
+                    choose_tile(lv.nx[l], lv.nz[l], base_blocks, kTileHalo, budget, lv.ti[l], lv.tj[l]);
+                    region = std::max(region, (long long)(lv.ti[l] + 2 * kTileHalo) * (lv.tj[l] + 2 * kTileHalo));
+                }
+                const size_t smem = (size_t)region * kTileNodeBytes;
+                if (std::min(solve_max_blocks(sm_count, smem), sm_count) >= base_blocks) lv.tile_smem = smem;
+            }
+            solve_blocks = base_blocks;
+        }
         nblocks = std::max(1, solve_blocks);
         if (nblocks > 1) {
-            a.l_single = lv.nlev;
-            for (int l = 0; l < lv.nlev; ++l)
-                if ((long long)lv.nx[l] * lv.nz[l] <= kSingleBlockLevel) {
-                    a.l_single = l;
-                    break;
+            a.l_single = ls;
+            if (lv.tile_smem) {
+                a.tiled = 1;
+                for (int l = 0; l < ls; ++l) {
+                    a.lev[l].ti = lv.ti[l];
+                    a.lev[l].tj = lv.tj[l];
                 }
+            }
             MAG_CK(cudaMemsetAsync(d_bar.p, 0, sizeof(GridBarrier), stream));
             MAG_CK(cudaMemsetAsync(red.p, 0, 4 * sizeof(double), stream));
         }
     }
-    launches += launch_solve(a, nblocks, stream);
+    if (a.prof) MAG_CK(cudaMemsetAsync(a.prof, 0, kSolvePhases * sizeof(double), stream));
+    launches += launch_solve(a, nblocks, stream, a.tiled ? lv.tile_smem : 0);
     MAG_CK(cudaGetLastError());
 }
 
@@ -620,7 +650,25 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
     a.bar = d_bar.p;
     a.status = d_status.p;
     a.err = d_err.p;
+    a.prof = prof_on ? d_prof.p : nullptr;
     return a;
+}
+
+// Phase timing of the multigrid solve: on from the first call; the times of
+// the most recent multigrid solve since then, in ms
+int Sim::solve_phase_times(double* out, int cap)
+{
+    if (!prof_on) {
+        d_prof.alloc(kSolvePhases);
+        d_prof.zero(stream);
+        prof_on = true;
+    }
+    std::vector<double> ns(kSolvePhases, 0.0);
+    MAG_CK(cudaStreamSynchronize(stream));
+    MAG_CK(cudaMemcpy(ns.data(), d_prof.p, kSolvePhases * sizeof(double), cudaMemcpyDeviceToHost));
+    const int n = std::min(cap, kSolvePhases);
+    for (int k = 0; k < n; ++k) out[k] = ns[k] * 1e-6;
+    return n;
 }
 
 // Speclist (pic.cpp:27-80) and lifetime_init (particles.cpp:142-206)

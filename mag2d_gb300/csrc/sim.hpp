@@ -127,6 +127,9 @@ struct SolverLevels {
     DevArray<double> rscale;     // right-hand-side scaling of rho per row
     DevArray<float> st32;
     double k2 = 1.0;
+    // multi-block solves: tile phases of the levels above the single-block ones
+    std::vector<int> ti, tj;     // tile interiors per level (empty: not yet chosen)
+    size_t tile_smem = 0;        // dynamic shared memory of the launch (0: tile phases off)
 };
 
 void build_species(const std::vector<SpeciesParams>& species_prm, std::vector<InteractionParams>& inters,
@@ -246,6 +249,7 @@ public:
     int diag(int s, double& sum_v2, unsigned long long& n, Counters& c);
     uint64_t niter(int s);
     int solver_levels() const { return lv.nlev; }
+    int solve_phase_times(double* out, int cap);
 
 private:
     friend class Batch;
@@ -278,6 +282,8 @@ private:
     DevArray<double> d_tables;
     SolverLevels lv;
     bool solver_ready = false;
+    DevArray<double> d_prof;  // phase times of the last multigrid solve [ns] once timing is on
+    bool prof_on = false;
 
     void setup_fields();
     void setup_species();

@@ -303,6 +303,15 @@ class Pic:
         return {"iterations": info.iterations, "residual": info.residual, "status": info.status,
                 "levels": info.levels}
 
+    def solve_phase_times(self) -> dict:
+        """Phase times [ms] of the most recent multigrid solve (mag_solve_phase_times);
+        the first call switches the timing on and returns zeros."""
+        out = np.zeros(29)
+        n = check(lib().mag_solve_phase_times(self.h, _dp(out), len(out)))
+        out = out[:n]
+        return {"start": out[0], "residual": out[1], "down": list(out[2:14]), "coarse": out[14],
+                "up": list(out[15:27]), "faces": out[27], "total": out[28]}
+
     def adjoint(self, nsteps: int, voltage_keys=(), *, checkpoint: int = 100, grad_b: bool = True,
                 w_energy: float = 1.0, w_lost: float = 1.0):
         """mag_adjoint_run: runs advance_init and nsteps steps, returns (info, gradient).

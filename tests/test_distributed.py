@@ -158,3 +158,73 @@ def test_particle_decomposition_equals_single_run(built, tmp_path):
         assert np.array_equal(g["vz"][sel], vz), rank
         assert np.array_equal(pic.field.u, u), rank
     pic.close()
+
+
+def _nccl_worker(port, q, tmp):
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import torch
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    os.environ.setdefault("NCCL_NVLS_ENABLE", "0")
+    torch.cuda.set_device(0)
+    dist.init_process_group("nccl", rank=0, world_size=1)
+    try:
+        import mag2d_gb300 as m
+        from cases import penning_rz
+        from mag2d_gb300.distributed import ParticleDecomposition
+
+        cfg, species, inter, cpath, spath, parts = penning_rz(Path(tmp), n=6000)
+        pic = m.Pic(cpath, spath, seed=1)
+        pic.speclist[0].set_particles(*parts)
+        dec = ParticleDecomposition(pic)
+        assert dec.device_reduce
+        dec.advance_init()
+        dec.advance(20)
+        g = pic.speclist[0].particles()
+        q.put(("ok", g["x"], g["z"], g["vz"], g["id"], pic.field.u, pic.speclist[0].rho_fixed()))
+        pic.close()
+    except Exception as e:  # reported to the parent
+        q.put(("error", repr(e)))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+@pytest.mark.timeout(300)
+def test_particle_decomposition_nccl_in_place(built, tmp_path):
+    """The NCCL branch of the particle decomposition: the deposit all-reduce
+    runs in place on the device array of mag_rho_fixed_ptr (a torch view
+    through __cuda_array_interface__).  One rank on the one GPU: the run
+    equals the plain run of the same electrons bit for bit."""
+    import multiprocessing as mp
+
+    import mag2d_gb300 as m
+    from cases import penning_rz
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    (tmp_path / "r0").mkdir()
+    p = ctx.Process(target=_nccl_worker, args=(_free_port(), q, str(tmp_path / "r0")))
+    p.start()
+    res = q.get(timeout=240)
+    p.join(timeout=60)
+    assert res[0] == "ok", res
+    assert p.exitcode == 0
+    _, x, z, vz, ids, u, rho = res
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=6000)
+    pic = m.Pic(cpath, spath, seed=1)
+    pic.speclist[0].set_particles(*parts)
+    pic.advance_init()
+    pic.advance(20)
+    g = pic.speclist[0].particles()
+    assert np.array_equal(g["id"], ids)
+    assert np.array_equal(g["x"], x) and np.array_equal(g["z"], z) and np.array_equal(g["vz"], vz)
+    assert np.array_equal(pic.field.u, u)
+    assert np.array_equal(pic.speclist[0].rho_fixed(), rho)
+    pic.close()
