@@ -29,9 +29,11 @@ constexpr long long kSingleBlockNodes = 70000;  // grids up to this size run on 
 constexpr long long kSingleBlockLevel = 4096;   // levels of a multi-block solve up to this size run on block 0
 // tile phases of a multi-block solve: halo rings around a tile's interior (the
 // four colour passes of a phase plus two) and shared bytes per region node
-// (FP32 correction, FP32 right-hand side / residual, one flag byte)
+// (FP32 correction, FP32 right-hand side / residual, one flag byte; on the
+// Galerkin levels also the 9 operator planes and the inverse diagonal)
 constexpr int kTileHalo = 6;
 constexpr int kTileNodeBytes = 9;
+constexpr int kTileNodeBytesGalerkin = 49;
 // phase times of one solve (mag_solve_phase_times): start and right-hand side,
 // FP64 residual with its reduction, the down part of each level, the coarse
 // part run by block 0 (or the coarsest solve), the up part of each level, the
@@ -380,6 +382,7 @@ struct SolveArgs {
     int nlev;
     int l_single;           // multi-block solves: first level run by block 0 alone (0: none)
     int tiled;              // multi-block solves: levels above l_single run as tile phases (dynamic shared memory)
+    int coarse_staged;      // tiled solves: block 0 runs the levels from l_single down in shared memory
     const float* coarse_inv;  // dense inverse of the coarsest level, column-major (null: smooth it)
     MGLevelDev lev[kMaxLevels];
     int nu1, nu2, ncoarse;
@@ -394,6 +397,9 @@ struct SolveArgs {
     int* err;
     double* prof;           // phase times of the solve [ns] (kSolvePhases slots), or null
 };
+
+// bytes of the argument copy in front of block 0's staged coarse levels (16-byte aligned)
+constexpr size_t kStagedArgsBytes = (sizeof(SolveArgs) + 15) & ~(size_t)15;
 
 // Adjoint of one particle step (or of the leapfrog start) for every particle
 // of a species: the state before the step, the removal marker after it, and

@@ -19,6 +19,7 @@
 
 #include "device.hpp"
 #include "kernels.hpp"
+#include "multigrid_host.hpp"
 
 namespace mag {
 
@@ -27,6 +28,8 @@ namespace {
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kEps0d = 8.854187817e-12;
 constexpr long long kBarrierSpinLimit = 20000000;  // ~seconds of __nanosleep(64) polling
+constexpr int kDenseCoarseMaxDev = (int)kDenseCoarseMax;
+constexpr int kCoarseChunks = 4;
 
 // The threads that share a piece of the solve: the whole grid (synchronised
 // by a bounded grid barrier) or one block (synchronised by __syncthreads).
@@ -250,7 +253,7 @@ __device__ __forceinline__ float coarse_apply(const float* __restrict__ coef, in
             if (j + dj < 0 || j + dj >= nz) continue;
             if (skip_center && di == 0 && dj == 0) continue;
             const int p = (di + 1) * 3 + (dj + 1);
-            acc += __ldg(&coef[p * n + k]) * e[k + (ptrdiff_t)di * nz + dj];
+            acc += coef[p * n + k] * e[k + (ptrdiff_t)di * nz + dj];  // coef may sit in shared memory
         }
     }
     return acc;
@@ -280,7 +283,7 @@ __device__ void smooth_coarse(const SolveArgs& a, Team& t, int l, int sweeps, bo
                 if (i >= nx || j >= nz) continue;
                 const size_t k = (size_t)i * nz + j;
                 const float off = coarse_apply(coef, nx, nz, i, j, k, ein, true);
-                eout[k] = (r[k] - off) * __ldg(&idg[k]);
+                eout[k] = (r[k] - off) * idg[k];
             }
             ok = t.sync();
         }
@@ -390,6 +393,29 @@ __device__ void coarse_solve(const SolveArgs& a, Team& t, bool& ok)
         return;
     }
     const unsigned n = (unsigned)(L.nx * L.nz);
+    if (t.nblocks == 1 && n <= (unsigned)kDenseCoarseMaxDev) {
+        // e = G r with the columns split into kCoarseChunks ranges: thread (k, row)
+        // sums its range (independent, coalesced loads), then the ranges are
+        // added in a fixed order, so the result does not depend on the thread count
+        __shared__ float part[kCoarseChunks][kDenseCoarseMaxDev];
+        for (unsigned q = t.tid; q < kCoarseChunks * n; q += t.nthreads) {
+            const unsigned k = q / n, row = q - k * n;
+            const unsigned c0 = k * n / kCoarseChunks, c1 = (k + 1) * n / kCoarseChunks;
+            float acc = 0.f;
+#pragma unroll 8
+            for (unsigned c = c0; c < c1; ++c) acc += a.coarse_inv[(size_t)c * n + row] * L.r[c];
+            part[k][row] = acc;
+        }
+        __syncthreads();
+        for (unsigned row = t.tid; row < n; row += t.nthreads) {
+            float acc = part[0][row];
+#pragma unroll
+            for (int k = 1; k < kCoarseChunks; ++k) acc += part[k][row];
+            L.e[row] = acc;
+        }
+        ok = t.sync();
+        return;
+    }
     for (unsigned row = t.tid; row < n; row += t.nthreads) {
         float acc = 0.f;
         for (unsigned c = 0; c < n; ++c) acc += a.coarse_inv[(size_t)c * n + row] * L.r[c];
@@ -521,26 +547,32 @@ __device__ __forceinline__ int tile_ring(const TileRegion& T, int li, int lj)
 struct TileShared {
     float* e;    // correction
     float* r;    // right-hand side, overwritten by the residual
+    float* cf;   // Galerkin levels: the 9 operator planes of the region (plane p of node q at p * n + q)
+    float* dg;   // Galerkin levels: inverse diagonal
     uint8_t* f;  // 1: outside the grid, or a fixed node of the fine level
 };
 
-__device__ __forceinline__ TileShared tile_shared(const TileRegion& T)
+__device__ __forceinline__ TileShared tile_shared(const TileRegion& T, int l)
 {
     extern __shared__ __align__(16) unsigned char tile_smem[];
     const int n = T.rh * T.rw;
     TileShared S;
     S.e = reinterpret_cast<float*>(tile_smem);
     S.r = S.e + n;
-    S.f = reinterpret_cast<uint8_t*>(S.r + n);
+    S.cf = S.r + n;
+    S.dg = S.cf + 9 * n;
+    S.f = reinterpret_cast<uint8_t*>(l > 0 ? S.dg + n : S.cf);
     return S;
 }
 
-// stage r (and e, or zeros) and the flags of the region
+// stage r (and e, or zeros), the flags and, on a Galerkin level, the operator
+// of the region: every load of the phase is issued here at once
 __device__ void tile_load(const SolveArgs& a, int l, const TileRegion& T, const TileShared& S, bool load_e)
 {
     const MGLevelDev& L = a.lev[l];
     const int n = T.rh * T.rw;
     const FastDiv dw((unsigned)T.rw);
+    const size_t nn = (size_t)L.nx * L.nz;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
         const int gi = T.ri + li, gj = T.rj + lj;
@@ -549,6 +581,11 @@ __device__ void tile_load(const SolveArgs& a, int l, const TileRegion& T, const 
         S.r[q] = in ? L.r[k] : 0.f;
         S.e[q] = (in && load_e) ? L.e[k] : 0.f;
         S.f[q] = (!in || (l == 0 && is_fixed(a.mask[k]))) ? 1 : 0;
+        if (l > 0) {
+#pragma unroll
+            for (int p = 0; p < 9; ++p) S.cf[p * n + q] = in ? __ldg(&L.coef[p * nn + k]) : 0.f;
+            S.dg[q] = in ? __ldg(&L.inv_diag[k]) : 0.f;
+        }
     }
 }
 
@@ -574,14 +611,14 @@ __device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const 
             acc -= st[4 * i + 1] * S.e[p + T.rw];
             acc -= k2 * S.e[p - 1];
             acc -= k2 * S.e[p + 1];
-            S.e[p] = acc / st[4 * i + 2];
+            S.e[p] = acc * st[4 * i + 3];
         }
     } else {  // 4-colour Gauss-Seidel on the 9-point Galerkin operator (smooth_coarse)
         const int ci = color >> 1, cj = color & 1;
         const int hh = (T.rh + 1) / 2, hw = (T.rw + 1) / 2;
         const int n = hh * hw;
+        const int nr = T.rh * T.rw;
         const FastDiv dh((unsigned)hw);
-        const size_t nn = (size_t)L.nx * L.nz;
         for (int q = threadIdx.x; q < n; q += blockDim.x) {
             const int a2 = (int)dh.div((unsigned)q);
             const int li = 2 * a2 + ((ci + T.ri) & 1);
@@ -590,7 +627,6 @@ __device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const 
             const int p = li * T.rw + lj;
             if (S.f[p]) continue;
             const int i = T.ri + li, j = T.rj + lj;
-            const size_t k = (size_t)i * L.nz + j;
             float off = 0.f;
 #pragma unroll
             for (int di = -1; di <= 1; ++di) {
@@ -599,10 +635,10 @@ __device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const 
                 for (int dj = -1; dj <= 1; ++dj) {
                     if (j + dj < 0 || j + dj >= L.nz) continue;
                     if (di == 0 && dj == 0) continue;
-                    off += __ldg(&L.coef[((di + 1) * 3 + (dj + 1)) * nn + k]) * S.e[p + di * T.rw + dj];
+                    off += S.cf[((di + 1) * 3 + (dj + 1)) * nr + p] * S.e[p + di * T.rw + dj];
                 }
             }
-            S.e[p] = (S.r[p] - off) * __ldg(&L.inv_diag[k]);
+            S.e[p] = (S.r[p] - off) * S.dg[p];
         }
     }
 }
@@ -615,7 +651,6 @@ __device__ void tile_residual(const SolveArgs& a, int l, const TileRegion& T, co
     const FastDiv dw((unsigned)T.rw);
     const float* __restrict__ st = a.st32;
     const float k2 = (float)a.k2;
-    const size_t nn = (size_t)L.nx * L.nz;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
         if (tile_ring(T, li, lj) > reach) continue;
@@ -632,7 +667,6 @@ __device__ void tile_residual(const SolveArgs& a, int l, const TileRegion& T, co
             acc -= k2 * S.e[q - 1];
             acc -= k2 * S.e[q + 1];
         } else {
-            const size_t k = (size_t)i * L.nz + j;
             float ae = 0.f;
 #pragma unroll
             for (int di = -1; di <= 1; ++di) {
@@ -640,7 +674,7 @@ __device__ void tile_residual(const SolveArgs& a, int l, const TileRegion& T, co
 #pragma unroll
                 for (int dj = -1; dj <= 1; ++dj) {
                     if (j + dj < 0 || j + dj >= L.nz) continue;
-                    ae += __ldg(&L.coef[((di + 1) * 3 + (dj + 1)) * nn + k]) * S.e[q + di * T.rw + dj];
+                    ae += S.cf[((di + 1) * 3 + (dj + 1)) * n + q] * S.e[q + di * T.rw + dj];
                 }
             }
             acc = S.r[q] - ae;
@@ -659,7 +693,7 @@ __device__ void tile_down(const SolveArgs& a, int l)
     const int ncolors = l == 0 ? 2 : 4;
     for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
-        const TileShared S = tile_shared(T);
+        const TileShared S = tile_shared(T, l);
         tile_load(a, l, T, S, false);
         __syncthreads();
         int pass = 0;
@@ -719,7 +753,7 @@ __device__ void tile_up(const SolveArgs& a, int l)
     const int ncolors = l == 0 ? 2 : 4;
     for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
-        const TileShared S = tile_shared(T);
+        const TileShared S = tile_shared(T, l);
         tile_load(a, l, T, S, true);
         __syncthreads();
         // e += P e_coarse on every region node of the grid (prolong_level)
@@ -757,6 +791,63 @@ __device__ void tile_up(const SolveArgs& a, int l)
     }
 }
 
+// Block 0's part of a multi-block V-cycle: the levels from l_single down.
+// With a.coarse_staged those levels (Galerkin planes, inverse diagonal,
+// correction, right-hand side, scratch) are staged in the block's dynamic
+// shared memory, which the tile phases do not use meanwhile, and the V-cycle
+// runs on a copy of the arguments that points there: its ~40 colour passes
+// then wait on shared memory instead of L2.  Level l_single's correction is
+// copied back for the up phase of the level above.
+__device__ void coarse_part(const SolveArgs& a, bool& okb)
+{
+    Team tb = Team::block(a.bar);
+    const int ls = a.l_single;
+    if (!a.coarse_staged) {
+        vcycle_from(a, tb, ls, okb);
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char tile_smem[];
+    static_assert(sizeof(SolveArgs) % 8 == 0, "word copy");
+    SolveArgs* sa = reinterpret_cast<SolveArgs*>(tile_smem);
+    {
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&a);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(tile_smem);
+        for (int w = threadIdx.x; w < (int)(sizeof(SolveArgs) / 8); w += blockDim.x) dst[w] = src[w];
+    }
+    __syncthreads();
+    float* base = reinterpret_cast<float*>(tile_smem + kStagedArgsBytes);
+    size_t off = 0;
+    for (int l = ls; l < a.nlev; ++l) {
+        const MGLevelDev& G = a.lev[l];
+        const int n = G.nx * G.nz;
+        float* e = base + off;
+        float* r = e + n;
+        float* t = r + n;
+        float* idg = t + n;
+        float* coef = idg + n;
+        off += 13 * (size_t)n;
+        if (threadIdx.x == 0) {
+            sa->lev[l].e = e;
+            sa->lev[l].r = r;
+            sa->lev[l].t = t;
+            sa->lev[l].inv_diag = idg;
+            sa->lev[l].coef = coef;
+        }
+        for (int k = threadIdx.x; k < 9 * n; k += blockDim.x) coef[k] = G.coef[k];
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            idg[k] = G.inv_diag[k];
+            r[k] = l == ls ? G.r[k] : 0.f;
+            e[k] = 0.f;
+        }
+    }
+    __syncthreads();
+    vcycle_from(*sa, tb, ls, okb);
+    __syncthreads();
+    const MGLevelDev& G = a.lev[ls];
+    const float* e = sa->lev[ls].e;
+    for (int k = threadIdx.x; k < G.nx * G.nz; k += blockDim.x) G.e[k] = e[k];
+}
+
 // One V-cycle of a multi-block solve with tile phases on the levels above
 // l_single and block 0 alone below; ends with u += e (done by the fine level's
 // up phase).
@@ -770,9 +861,8 @@ __device__ void vcycle_tiled(const SolveArgs& a, Team& t, bool& ok)
     }
     if (!ok) return;
     if (blockIdx.x == 0) {
-        Team tb = Team::block(a.bar);
         bool okb = true;
-        vcycle_from(a, tb, ls, okb);
+        coarse_part(a, okb);
         __threadfence();
     }
     ok = t.sync();

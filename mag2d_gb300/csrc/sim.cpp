@@ -539,6 +539,7 @@ void Sim::run_solve(SolveArgs a)
     int nblocks = 1;
     a.l_single = 0;
     a.tiled = 0;
+    a.coarse_staged = 0;
     if ((long long)nx * nz > kSingleBlockNodes) {
         int ls = lv.nlev;
         for (int l = 0; l < lv.nlev; ++l)
@@ -550,20 +551,28 @@ void Sim::run_solve(SolveArgs a)
             // tile phases on the levels above ls: one tile region per block in
             // shared memory (up to 200 KB), when the pre- and post-smoothing
             // passes fit the halo and the cooperative launch keeps one block per SM
-            const long long budget = (200LL << 10) / kTileNodeBytes;
+            const long long smem_max = 200LL << 10;
             const int base_blocks = std::min(solve_max_blocks(sm_count), sm_count);
             const bool fits = ls > 0 && ls < lv.nlev && 2 * std::max(a.nu1, a.nu2) <= kTileHalo - 2;
             lv.ti.assign(lv.nlev, 0);
             lv.tj.assign(lv.nlev, 0);
             lv.tile_smem = 0;
             if (fits && base_blocks > 1) {
-                long long region = 0;
+                size_t smem = 0;
                 for (int l = 0; l < ls; ++l) {
-                    choose_tile(lv.nx[l], lv.nz[l], base_blocks, kTileHalo, budget, lv.ti[l], lv.tj[l]);
-                    region = std::max(region, (long long)(lv.ti[l] + 2 * kTileHalo) * (lv.tj[l] + 2 * kTileHalo));
+                    const int bytes = l == 0 ? kTileNodeBytes : kTileNodeBytesGalerkin;
+                    choose_tile(lv.nx[l], lv.nz[l], base_blocks, kTileHalo, smem_max / bytes, lv.ti[l], lv.tj[l]);
+                    smem = std::max(smem, (size_t)(lv.ti[l] + 2 * kTileHalo) * (lv.tj[l] + 2 * kTileHalo) * bytes);
                 }
-                const size_t smem = (size_t)region * kTileNodeBytes;
-                if (std::min(solve_max_blocks(sm_count, smem), sm_count) >= base_blocks) lv.tile_smem = smem;
+                // block 0's levels in shared memory: the arguments and 13 floats per node
+                size_t stage = kStagedArgsBytes;
+                for (int l = ls; l < lv.nlev; ++l) stage += 13 * sizeof(float) * (size_t)lv.nx[l] * lv.nz[l];
+                const bool staged = stage <= (size_t)smem_max;
+                if (staged) smem = std::max(smem, stage);
+                if (std::min(solve_max_blocks(sm_count, smem), sm_count) >= base_blocks) {
+                    lv.tile_smem = smem;
+                    lv.coarse_staged = staged;
+                }
             }
             solve_blocks = base_blocks;
         }
@@ -572,6 +581,7 @@ void Sim::run_solve(SolveArgs a)
             a.l_single = ls;
             if (lv.tile_smem) {
                 a.tiled = 1;
+                a.coarse_staged = lv.coarse_staged ? 1 : 0;
                 for (int l = 0; l < ls; ++l) {
                     a.lev[l].ti = lv.ti[l];
                     a.lev[l].tj = lv.tj[l];

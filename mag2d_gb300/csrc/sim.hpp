@@ -130,6 +130,7 @@ struct SolverLevels {
     // multi-block solves: tile phases of the levels above the single-block ones
     std::vector<int> ti, tj;     // tile interiors per level (empty: not yet chosen)
     size_t tile_smem = 0;        // dynamic shared memory of the launch (0: tile phases off)
+    bool coarse_staged = false;  // block 0's levels fit the dynamic shared memory
 };
 
 void build_species(const std::vector<SpeciesParams>& species_prm, std::vector<InteractionParams>& inters,
