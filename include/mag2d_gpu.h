@@ -54,8 +54,8 @@ typedef struct {
     double poisson_tol;    /* Jacobi-scaled residual / max|u| at which the solve stops (0 = 1e-12) */
     int poisson_max_iter;  /* outer refinement iterations before MAG_ENOTCONV (0 = 200) */
     int64_t capacity_hint; /* particle slots to reserve per species (0 = grow as needed) */
-    int push_vec;          /* consecutive slots per thread of the particle kernel: 1, 2 or 4 (0 = 2);
-                              results do not depend on it */
+    int push_vec;          /* consecutive slots per thread of the particle kernel: 1, 2 or 4 (0 = 4 for
+                              species of at least 4e6 slots, else 2); results do not depend on it */
     int direct_solve;      /* self-consistent Poisson solves by the precomputed inverse of the operator
                               (built at the first solve): 0 = for grids up to 20000 nodes, 1 = also
                               larger ones up to the one-block size, -1 = always multigrid */

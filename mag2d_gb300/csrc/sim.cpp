@@ -62,7 +62,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     poisson_tol = opts.poisson_tol > 0 ? opts.poisson_tol : 1e-12;
     poisson_max_iter = opts.poisson_max_iter > 0 ? opts.poisson_max_iter : 200;
     sort_interval = opts.sort_interval == 0 ? 20 : opts.sort_interval;
-    push_vec = opts.push_vec == 1 || opts.push_vec == 2 || opts.push_vec == 4 ? opts.push_vec : 2;
+    push_vec = opts.push_vec == 1 || opts.push_vec == 2 || opts.push_vec == 4 ? opts.push_vec : 0;
     direct_mode = opts.direct_solve;
     max_fused = opts.max_fused_steps <= 0 ? kMaxFusedSteps : std::min(opts.max_fused_steps, kMaxFusedSteps);
     if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sm_count < 1)
@@ -1132,7 +1132,7 @@ void Sim::step(double* ms)
             S.niter++;
             continue;
         }
-        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, false, push_vec, sm_count, stream);
+        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, false, push_vec_for(S.n_slots), sm_count, stream);
         mark(2);
         if (coll_mode((int)s) == 2) {
             CollideArgs ca = collide_args((int)s);
@@ -1252,7 +1252,7 @@ void Sim::advance_init(bool deposit)
     for (size_t s = 0; s < sp.size(); ++s) {
         if (sp[s].n_slots == 0 || multicoll) continue;  // ADVANCE_MULTICOLL has no leapfrog start
         PushArgs pa = push_args((int)s, true);
-        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, true, push_vec, sm_count, stream);
+        launches += launch_push(pa, p.coord == CYLINDRICAL ? 1 : 0, true, push_vec_for(sp[s].n_slots), sm_count, stream);
     }
     if (p.use_source) source_refresh(p.src_fact);  // the driver's refresh after advance_init (src/test.cpp:56-59)
     MAG_CK(cudaGetLastError());

@@ -74,7 +74,7 @@ struct SimOptions {
     double poisson_tol = 1e-12;
     int poisson_max_iter = 200;
     int64_t capacity_hint = 0;
-    int push_vec = 0;       // slots per thread of the particle kernel: 1, 2 or 4 (0: 2)
+    int push_vec = 0;       // slots per thread of the particle kernel: 1, 2 or 4 (0: by particle count)
     int direct_solve = 0;   // Poisson by the precomputed inverse: 0 automatic (small grids), 1 forced, -1 never
     int max_fused_steps = 0;  // steps per fused particle launch where particles are independent (0: 64, 1: none)
     cudaStream_t stream = nullptr;  // work on this stream instead of one of its own (not destroyed)
@@ -175,7 +175,11 @@ public:
     bool rho_override = false;
     SolveStatus last_solve{};
     int sort_interval = 20;
-    int push_vec = 2;
+    int push_vec = 0;  // 1, 2 or 4 slots per thread of the particle kernel, 0: by particle count
+    // slots per thread: 4 once a species has millions of slots (fewer chunk
+    // flushes of the deposit tile and more loads in flight per thread,
+    // measured faster on 1e8 electrons), else 2 (more threads for small runs)
+    int push_vec_for(int64_t n) const { return push_vec ? push_vec : (n >= 4000000 ? 4 : 2); }
     int sm_count = 1;
     bool multicoll = false;  // mover ADVANCE_MULTICOLL
     int solve_blocks = 0;  // blocks of a cooperative solve (0: not yet chosen)
