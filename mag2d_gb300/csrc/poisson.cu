@@ -29,7 +29,7 @@ constexpr double kPi = 3.14159265358979323846;
 constexpr double kEps0d = 8.854187817e-12;
 constexpr long long kBarrierSpinLimit = 20000000;  // ~seconds of __nanosleep(64) polling
 constexpr int kDenseCoarseMaxDev = (int)kDenseCoarseMax;
-constexpr int kCoarseChunks = 4;
+constexpr int kCoarseChunks = 6;
 
 // The threads that share a piece of the solve: the whole grid (synchronised
 // by a bounded grid barrier) or one block (synchronised by __syncthreads).
@@ -398,12 +398,14 @@ __device__ void coarse_solve(const SolveArgs& a, Team& t, bool& ok)
         // sums its range (independent, coalesced loads), then the ranges are
         // added in a fixed order, so the result does not depend on the thread count
         __shared__ float part[kCoarseChunks][kDenseCoarseMaxDev];
+        constexpr int kSpan = (kDenseCoarseMaxDev + kCoarseChunks - 1) / kCoarseChunks;
         for (unsigned q = t.tid; q < kCoarseChunks * n; q += t.nthreads) {
             const unsigned k = q / n, row = q - k * n;
             const unsigned c0 = k * n / kCoarseChunks, c1 = (k + 1) * n / kCoarseChunks;
             float acc = 0.f;
-#pragma unroll 8
-            for (unsigned c = c0; c < c1; ++c) acc += a.coarse_inv[(size_t)c * n + row] * L.r[c];
+#pragma unroll
+            for (int c = 0; c < kSpan; ++c)  // every load of the range in flight at once
+                if (c0 + c < c1) acc += a.coarse_inv[(size_t)(c0 + c) * n + row] * L.r[c0 + c];
             part[k][row] = acc;
         }
         __syncthreads();
@@ -791,6 +793,18 @@ __device__ void tile_up(const SolveArgs& a, int l)
     }
 }
 
+// Block copy of n floats from global to shared memory, 16-byte vectors where
+// both sides allow (level arrays start 16-byte aligned on both sides).
+__device__ __forceinline__ void stage_copy(float* dst, const float* __restrict__ src, int n)
+{
+    const int n4 = n >> 2;
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll 4
+    for (int k = threadIdx.x; k < n4; k += blockDim.x) d4[k] = __ldg(&s4[k]);
+    for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+}
+
 // Block 0's part of a multi-block V-cycle: the levels from l_single down.
 // With a.coarse_staged those levels (Galerkin planes, inverse diagonal,
 // correction, right-hand side, scratch) are staged in the block's dynamic
@@ -820,12 +834,13 @@ __device__ void coarse_part(const SolveArgs& a, bool& okb)
     for (int l = ls; l < a.nlev; ++l) {
         const MGLevelDev& G = a.lev[l];
         const int n = G.nx * G.nz;
+        const int n4 = (n + 3) & ~3;  // every array of the level starts 16-byte aligned
         float* e = base + off;
-        float* r = e + n;
-        float* t = r + n;
-        float* idg = t + n;
-        float* coef = idg + n;
-        off += 13 * (size_t)n;
+        float* r = e + n4;
+        float* t = r + n4;
+        float* idg = t + n4;
+        float* coef = idg + n4;
+        off += 4 * (size_t)n4 + (((size_t)9 * n + 3) & ~(size_t)3);
         if (threadIdx.x == 0) {
             sa->lev[l].e = e;
             sa->lev[l].r = r;
@@ -833,12 +848,10 @@ __device__ void coarse_part(const SolveArgs& a, bool& okb)
             sa->lev[l].inv_diag = idg;
             sa->lev[l].coef = coef;
         }
-        for (int k = threadIdx.x; k < 9 * n; k += blockDim.x) coef[k] = G.coef[k];
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            idg[k] = G.inv_diag[k];
-            r[k] = l == ls ? G.r[k] : 0.f;
-            e[k] = 0.f;
-        }
+        stage_copy(coef, G.coef, 9 * n);
+        stage_copy(idg, G.inv_diag, n);
+        if (l == ls) stage_copy(r, G.r, n);
+        for (int k = threadIdx.x; k < n; k += blockDim.x) e[k] = 0.f;
     }
     __syncthreads();
     vcycle_from(*sa, tb, ls, okb);
@@ -929,13 +942,18 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
     for (; ok; ++it) {
         // residual in FP64; its Jacobi-scaled max norm and max|u| only steer
         // the stopping test and are taken in FP32
-        float lres32 = 0.f, lumax32 = 0.f;
-#pragma unroll 1
+        // max|u| from the high words of the doubles (sign cleared): integer
+        // compares, no FP64 conversion; 20 mantissa bits are plenty for the
+        // stopping test, and the truncation only makes the test stricter
+        float lres32 = 0.f;
+        unsigned lumax_hi = 0u;
+        const bool zero_e = !(a.tiled && t.nblocks > 1);  // the tile phases start from e = 0 in shared memory
+#pragma unroll 2
         for (unsigned k = t.tid; k < nn; k += t.nthreads) {
             const int i = (int)dnz.div(k);
             const double uk = uin[k];
-            lumax32 = fmaxf(lumax32, fabsf((float)uk));
-            F.e[k] = 0.f;
+            lumax_hi = max(lumax_hi, (unsigned)__double2hiint(uk) & 0x7FFFFFFFu);
+            if (zero_e) F.e[k] = 0.f;
             if (is_fixed(mask[k])) {
                 F.r[k] = 0.f;
                 continue;
@@ -950,7 +968,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
             F.r[k] = rf;
             lres32 = fmaxf(lres32, fabsf(rf * st32[4 * i + 3]));
         }
-        double lres = lres32, lumax = lumax32;
+        double lres = lres32, lumax = __hiloint2double((int)lumax_hi, 0);
         lres = block_max(lres);
         lumax = block_max(lumax);
         if (t.nblocks > 1) {

@@ -566,7 +566,10 @@ void Sim::run_solve(SolveArgs a)
                 }
                 // block 0's levels in shared memory: the arguments and 13 floats per node
                 size_t stage = kStagedArgsBytes;
-                for (int l = ls; l < lv.nlev; ++l) stage += 13 * sizeof(float) * (size_t)lv.nx[l] * lv.nz[l];
+                for (int l = ls; l < lv.nlev; ++l) {
+                    const size_t n = (size_t)lv.nx[l] * lv.nz[l];
+                    stage += sizeof(float) * (4 * ((n + 3) & ~(size_t)3) + ((9 * n + 3) & ~(size_t)3));
+                }
                 const bool staged = stage <= (size_t)smem_max;
                 if (staged) smem = std::max(smem, stage);
                 if (std::min(solve_max_blocks(sm_count, smem), sm_count) >= base_blocks) {
