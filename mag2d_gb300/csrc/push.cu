@@ -191,6 +191,18 @@ __device__ __forceinline__ int to_fixed_disp(float c)
     return __float2int_rn(v);
 }
 
+// The four CIC corner weights of fractions U, V (2^-20 cell units, at most
+// 2^20): products of two 21-bit numbers, each one 32 x 32 -> 64 multiply.
+__device__ __forceinline__ void cic_weights(uint32_t U, uint32_t V, unsigned long long (&w)[4])
+{
+    const uint32_t one = 1u << kDepositShift;
+    const uint32_t oU = one - U, oV = one - V;
+    w[0] = (unsigned long long)oU * oV;
+    w[1] = (unsigned long long)U * oV;
+    w[2] = (unsigned long long)oU * V;
+    w[3] = (unsigned long long)U * V;
+}
+
 // One particle of the step, in registers.  Returns alive (false: removed at
 // the boundary or in a closed cell) and cand (the collision test fired).
 // CIC deposit of one particle into the fixed-point grid (Field2D::accumulate):
@@ -200,12 +212,13 @@ struct GlobalDeposit {
     int nz;
     __device__ __forceinline__ void add(int ic, int jc, unsigned long long U, unsigned long long V) const
     {
-        const unsigned long long one = 1ull << kDepositShift;
+        unsigned long long w[4];
+        cic_weights((uint32_t)U, (uint32_t)V, w);
         unsigned long long* r0 = rho + (size_t)ic * nz + jc;
-        atomicAdd(r0, (one - U) * (one - V));
-        atomicAdd(r0 + nz, U * (one - V));
-        atomicAdd(r0 + 1, (one - U) * V);
-        atomicAdd(r0 + nz + 1, U * V);
+        atomicAdd(r0, w[0]);
+        atomicAdd(r0 + nz, w[1]);
+        atomicAdd(r0 + 1, w[2]);
+        atomicAdd(r0 + nz + 1, w[3]);
     }
 };
 
@@ -231,8 +244,8 @@ struct TileDeposit {
             g.add(ic, jc, U, V);
             return;
         }
-        const unsigned long long one = 1ull << kDepositShift;
-        const unsigned long long w[4] = {(one - U) * (one - V), U * (one - V), (one - U) * V, U * V};
+        unsigned long long w[4];
+        cic_weights((uint32_t)U, (uint32_t)V, w);
         const int cp = (threadIdx.x & (kTileCopies - 1)) * kTileStride;
         const int t[4] = {cp + r * kTileCols + c, cp + (r + 1) * kTileCols + c, cp + r * kTileCols + c + 1,
                           cp + (r + 1) * kTileCols + c + 1};
