@@ -45,28 +45,33 @@ void fine_operator(int coord, int nx, int nz, double dx, double dz, const std::v
         }
 }
 
-void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int& nxc,
+void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int mode, int& nxc,
               int& nzc, std::vector<double>& Ac)
 {
-    nxc = (nxf - 1) / 2 + 1;
-    nzc = (nzf - 1) / 2 + 1;
+    // coarse node (J0, J1) sits on fine node (sx J0, sz J1); the interpolation
+    // reaches rx (rz) fine nodes either side in a coarsened direction, none in
+    // a kept one
+    const int sx = mode == kCoarsenZ ? 1 : 2, sz = mode == kCoarsenX ? 1 : 2;
+    const int rx = sx - 1, rz = sz - 1;
+    nxc = sx == 2 ? (nxf - 1) / 2 + 1 : nxf;
+    nzc = sz == 2 ? (nzf - 1) / 2 + 1 : nzf;
     const size_t nf = (size_t)nxf * nzf, nc = (size_t)nxc * nzc;
     Ac.assign(9 * nc, 0.0);
     auto pw = [](int a) { return a == 0 ? 1.0 : 0.5; };
     for (int J0 = 0; J0 < nxc; ++J0)
         for (int J1 = 0; J1 < nzc; ++J1) {
-            double v[3][3] = {{0}};
-            for (int a = -1; a <= 1; ++a)
-                for (int b = -1; b <= 1; ++b) {
-                    const int i = 2 * J0 + a, j = 2 * J1 + b;
+            double v[3][3] = {{0}};  // P e_J on the fine nodes around (sx J0, sz J1)
+            for (int a = -rx; a <= rx; ++a)
+                for (int b = -rz; b <= rz; ++b) {
+                    const int i = sx * J0 + a, j = sz * J1 + b;
                     if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
                     if (fixed_f[(size_t)i * nzf + j]) continue;
                     v[a + 1][b + 1] = pw(a) * pw(b);
                 }
-            double w[5][5] = {{0}};
-            for (int a = -2; a <= 2; ++a)
-                for (int b = -2; b <= 2; ++b) {
-                    const int i = 2 * J0 + a, j = 2 * J1 + b;
+            double w[5][5] = {{0}};  // A P e_J on the fine nodes within reach + 1
+            for (int a = -rx - 1; a <= rx + 1; ++a)
+                for (int b = -rz - 1; b <= rz + 1; ++b) {
+                    const int i = sx * J0 + a, j = sz * J1 + b;
                     if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
                     const size_t f = (size_t)i * nzf + j;
                     double acc = 0.0;
@@ -84,13 +89,13 @@ void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector
                 for (int I1 = J1 - 1; I1 <= J1 + 1; ++I1) {
                     if (I0 < 0 || I0 >= nxc || I1 < 0 || I1 >= nzc) continue;
                     double acc = 0.0;
-                    for (int a = -1; a <= 1; ++a)
-                        for (int b = -1; b <= 1; ++b) {
-                            const int i = 2 * I0 + a, j = 2 * I1 + b;
+                    for (int a = -rx; a <= rx; ++a)
+                        for (int b = -rz; b <= rz; ++b) {
+                            const int i = sx * I0 + a, j = sz * I1 + b;
                             if (i < 0 || i >= nxf || j < 0 || j >= nzf) continue;
                             if (fixed_f[(size_t)i * nzf + j]) continue;
-                            const int wa = i - 2 * J0, wb = j - 2 * J1;
-                            if (wa < -2 || wa > 2 || wb < -2 || wb > 2) continue;
+                            const int wa = i - sx * J0, wb = j - sz * J1;
+                            if (wa < -rx - 1 || wa > rx + 1 || wb < -rz - 1 || wb > rz + 1) continue;
                             acc += pw(a) * pw(b) * w[wa + 2][wb + 2];
                         }
                     Ac[(size_t)plane(J0 - I0, J1 - I1) * nc + (size_t)I0 * nzc + I1] = acc;
@@ -103,14 +108,26 @@ void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector
         }
 }
 
-void multigrid_levels(int nx, int nz, int max_levels, std::vector<int>& lnx, std::vector<int>& lnz)
+void multigrid_levels(int nx, int nz, double couple_ratio, int max_levels, std::vector<int>& lnx, std::vector<int>& lnz,
+                      std::vector<int>& lmode)
 {
     lnx.assign(1, nx);
     lnz.assign(1, nz);
-    while ((int)lnx.size() < max_levels && (lnx.back() - 1) % 2 == 0 && (lnz.back() - 1) % 2 == 0 && lnx.back() >= 5 &&
-           lnz.back() >= 5 && (long long)lnx.back() * lnz.back() > kDenseCoarseMax) {
-        lnx.push_back((lnx.back() - 1) / 2 + 1);
-        lnz.push_back((lnz.back() - 1) / 2 + 1);
+    lmode.assign(1, kCoarsenFull);
+    double ratio = couple_ratio;  // x couplings / z couplings of the current level
+    while ((int)lnx.size() < max_levels && (long long)lnx.back() * lnz.back() > kDenseCoarseMax) {
+        const int x = lnx.back(), z = lnz.back();
+        const bool cx = (x - 1) % 2 == 0 && x >= 5, cz = (z - 1) % 2 == 0 && z >= 5;
+        int mode;
+        if (ratio >= kSemiCoarsenRatio && cx) mode = kCoarsenX;       // strong x couplings: halve x only
+        else if (ratio <= 1.0 / kSemiCoarsenRatio && cz) mode = kCoarsenZ;
+        else if (cx && cz) mode = kCoarsenFull;
+        else break;
+        lnx.push_back(mode == kCoarsenZ ? x : (x - 1) / 2 + 1);
+        lnz.push_back(mode == kCoarsenX ? z : (z - 1) / 2 + 1);
+        lmode.push_back(mode);
+        if (mode == kCoarsenX) ratio /= 4.0;  // the x spacing doubles
+        if (mode == kCoarsenZ) ratio *= 4.0;
     }
 }
 

@@ -16,17 +16,30 @@ inline int plane(int di, int dj) { return (di + 1) * 3 + (dj + 1); }
 void fine_operator(int coord, int nx, int nz, double dx, double dz, const std::vector<int8_t>& mask,
                    std::vector<double>& A);
 
-// Galerkin coarse operator Ac = P^T Af P with bilinear P (rows of fixed fine
-// nodes are zero).  Coarse rows left without a diagonal become identity.
-void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int& nxc,
+// How a level is coarsened to the next: both directions, or only x (r), or
+// only z.  A level whose x couplings are at least kSemiCoarsenRatio times its
+// z couplings (the cylindrical operator on cells with dz = 2 dx has 4) is
+// halved in x only, which makes the next level's couplings alike; point
+// Gauss-Seidel with full coarsening converges slowly on such levels.
+constexpr int kCoarsenFull = 0, kCoarsenX = 1, kCoarsenZ = 2;
+constexpr double kSemiCoarsenRatio = 2.5;
+
+// Galerkin coarse operator Ac = P^T Af P with P bilinear in the coarsened
+// directions (mode: kCoarsen*; rows of fixed fine nodes are zero).  Coarse
+// rows left without a diagonal become identity.
+void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int mode, int& nxc,
               int& nzc, std::vector<double>& Ac);
 
 // Coarsest levels up to this many nodes are solved exactly with a dense inverse.
 constexpr long long kDenseCoarseMax = 200;
 
-// Level sizes: halve while both sizes are odd and >= 5 (at most max_levels
+// Level sizes: halve while the sizes are odd and >= 5 (at most max_levels
 // levels), and stop at the first level of at most kDenseCoarseMax nodes.
-void multigrid_levels(int nx, int nz, int max_levels, std::vector<int>& lnx, std::vector<int>& lnz);
+// couple_ratio = x couplings / z couplings of the fine operator ((dz/dx)^2 for
+// the cylindrical one, 1 for the reference's Cartesian one); lmode[l] says how
+// level l - 1 was coarsened to level l (lmode[0] unused).
+void multigrid_levels(int nx, int nz, double couple_ratio, int max_levels, std::vector<int>& lnx, std::vector<int>& lnz,
+                      std::vector<int>& lmode);
 
 // Per-row coefficients (w, e, c, 1/c) of the fine 5-point stencil, FP64,
 // 4 * nx values, and the common s/n coefficient k2 (src/fields.cpp:149-238);

@@ -124,8 +124,9 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
             }
         }
     // multigrid hierarchy (host, FP64) and the scratch layout
-    std::vector<int> lnx, lnz;
-    multigrid_levels(nx, nz, kMaxLevels, lnx, lnz);
+    // full coarsening only, so that the scratch layout of every accepted grid fits the static array
+    std::vector<int> lnx, lnz, lmode;
+    multigrid_levels(nx, nz, 1.0, kMaxLevels, lnx, lnz, lmode);
     const int nlev = (int)lnx.size();
     std::vector<std::vector<float>> coef(nlev), idiag(nlev);
     std::vector<float> cinv;
@@ -136,7 +137,7 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
         for (size_t k = 0; k < nn; ++k) fixed_f[k] = mask[k] == 0 || mask[k] == 1;
         for (int l = 1; l < nlev; ++l) {
             int cx, cz;
-            galerkin(lnx[l - 1], lnz[l - 1], A, fixed_f, cx, cz, Ac);
+            galerkin(lnx[l - 1], lnz[l - 1], A, fixed_f, kCoarsenFull, cx, cz, Ac);
             const size_t n = (size_t)cx * cz;
             coef[l].assign(Ac.begin(), Ac.end());
             idiag[l].resize(n);

@@ -326,6 +326,52 @@ __device__ void residual_level(const SolveArgs& a, Team& t, int l, float* __rest
     }
 }
 
+// Interpolation between level l and l + 1 (coarsening mode m): coarse node
+// (I, J) sits on fine node (sx I, sz J) with sx = 2 where x is coarsened
+// (1 where it is kept), likewise sz; the reach is 1 in a coarsened direction
+// (weights 1, 1/2), 0 in a kept one.
+__device__ __forceinline__ int coarsen_sx(int m) { return m == 2 ? 1 : 2; }
+__device__ __forceinline__ int coarsen_sz(int m) { return m == 1 ? 1 : 2; }
+
+// coarse residual of node (I, J): P^T t around fine (sx I, sz J); get(i, j)
+// returns the fine residual (0 at fixed fine nodes)
+template <class Get>
+__device__ __forceinline__ float restrict_node(int I, int J, int m, int nxf, int nzf, const Get& get)
+{
+    const int sx = coarsen_sx(m), sz = coarsen_sz(m);
+    const int rx = sx - 1, rz = sz - 1;
+    float acc = 0.f;
+#pragma unroll
+    for (int di = -1; di <= 1; ++di) {
+        if (di < -rx || di > rx) continue;
+        const int i = sx * I + di;
+        if (i < 0 || i >= nxf) continue;
+        const float wi = di == 0 ? 1.f : 0.5f;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+            if (dj < -rz || dj > rz) continue;
+            const int j = sz * J + dj;
+            if (j < 0 || j >= nzf) continue;
+            const float wj = dj == 0 ? 1.f : 0.5f;
+            acc += wi * wj * get(i, j);
+        }
+    }
+    return acc;
+}
+
+// fine value (i, j) of P e_coarse
+__device__ __forceinline__ float prolong_node(int i, int j, int m, const float* __restrict__ ec, int ncz)
+{
+    const int sx = coarsen_sx(m), sz = coarsen_sz(m);
+    const int I0 = sx == 2 ? i >> 1 : i, J0 = sz == 2 ? j >> 1 : j;
+    const bool oi = sx == 2 && (i & 1), oj = sz == 2 && (j & 1);
+    const size_t b = (size_t)I0 * ncz + J0;
+    if (!oi && !oj) return ec[b];
+    if (oi && !oj) return 0.5f * (ec[b] + ec[b + ncz]);
+    if (!oi && oj) return 0.5f * (ec[b] + ec[b + 1]);
+    return 0.25f * (ec[b] + ec[b + ncz] + ec[b + 1] + ec[b + ncz + 1]);
+}
+
 // r_{l+1} = P^T t_l (weights 1, 1/2, 1/4; fixed fine nodes carry no residual); e_{l+1} = 0
 __device__ void restrict_level(const SolveArgs& a, Team& t, int l, const float* __restrict__ tl)
 {
@@ -335,24 +381,12 @@ __device__ void restrict_level(const SolveArgs& a, Team& t, int l, const float* 
     float* __restrict__ ce = C.e;
     const unsigned n = (unsigned)(C.nx * C.nz);
     const FastDiv dz((unsigned)C.nz);
+    const int fnz = F.nz;
+    auto get = [&](int i, int j) { return tl[(size_t)i * fnz + j]; };
 #pragma unroll 2
     for (unsigned q = t.tid; q < n; q += t.nthreads) {
         const int I = (int)dz.div(q), J = (int)(q - (unsigned)I * C.nz);
-        float acc = 0.f;
-#pragma unroll
-        for (int di = -1; di <= 1; ++di) {
-            const int i = 2 * I + di;
-            if (i < 0 || i >= F.nx) continue;
-            const float wi = di == 0 ? 1.f : 0.5f;
-#pragma unroll
-            for (int dj = -1; dj <= 1; ++dj) {
-                const int j = 2 * J + dj;
-                if (j < 0 || j >= F.nz) continue;
-                const float wj = dj == 0 ? 1.f : 0.5f;
-                acc += wi * wj * tl[(size_t)i * F.nz + j];
-            }
-        }
-        cr[q] = acc;
+        cr[q] = restrict_node(I, J, F.cmode, F.nx, F.nz, get);
         ce[q] = 0.f;
     }
 }
@@ -370,15 +404,7 @@ __device__ void prolong_level(const SolveArgs& a, Team& t, int l)
     for (unsigned q = t.tid; q < n; q += t.nthreads) {
         if (l == 0 && is_fixed(a.mask[q])) continue;
         const int i = (int)dz.div(q), j = (int)(q - (unsigned)i * F.nz);
-        const int I0 = i >> 1, J0 = j >> 1;
-        const bool oi = i & 1, oj = j & 1;
-        const size_t b = (size_t)I0 * C.nz + J0;
-        float v;
-        if (!oi && !oj) v = ec[b];
-        else if (oi && !oj) v = 0.5f * (ec[b] + ec[b + C.nz]);
-        else if (!oi && oj) v = 0.5f * (ec[b] + ec[b + 1]);
-        else v = 0.25f * (ec[b] + ec[b + C.nz] + ec[b + 1] + ec[b + C.nz + 1]);
-        fe[q] += v;
+        fe[q] += prolong_node(i, j, F.cmode, ec, C.nz);
     }
 }
 
@@ -711,28 +737,16 @@ __device__ void tile_down(const SolveArgs& a, int l)
         }
         tile_residual(a, l, T, S, kTileHalo - 1 - pass);
         __syncthreads();
-        // coarse nodes (I, J) whose fine node (2I, 2J) lies in the tile (restrict_level)
-        const int I0 = (T.i0 + 1) / 2, I1 = (T.i0 + T.ni - 1) / 2;
-        const int J0 = (T.j0 + 1) / 2, J1 = (T.j0 + T.nj - 1) / 2;
+        // coarse nodes (I, J) whose fine node (sx I, sz J) lies in the tile (restrict_level)
+        const int sx = coarsen_sx(L.cmode), sz = coarsen_sz(L.cmode);
+        const int I0 = (T.i0 + sx - 1) / sx, I1 = (T.i0 + T.ni - 1) / sx;
+        const int J0 = (T.j0 + sz - 1) / sz, J1 = (T.j0 + T.nj - 1) / sz;
         const int cw = J1 - J0 + 1, nc = (I1 - I0 + 1) * cw;
+        auto get = [&](int i, int j) { return S.r[(i - T.ri) * T.rw + (j - T.rj)]; };
         for (int q = threadIdx.x; q < nc; q += blockDim.x) {
             const int I = I0 + q / cw, J = J0 + q % cw;
-            float acc = 0.f;
-#pragma unroll
-            for (int di = -1; di <= 1; ++di) {
-                const int i = 2 * I + di;
-                if (i < 0 || i >= L.nx) continue;
-                const float wi = di == 0 ? 1.f : 0.5f;
-#pragma unroll
-                for (int dj = -1; dj <= 1; ++dj) {
-                    const int j = 2 * J + dj;
-                    if (j < 0 || j >= L.nz) continue;
-                    const float wj = dj == 0 ? 1.f : 0.5f;
-                    acc += wi * wj * S.r[(i - T.ri) * T.rw + (j - T.rj)];
-                }
-            }
             const size_t K = (size_t)I * C.nz + J;
-            C.r[K] = acc;
+            C.r[K] = restrict_node(I, J, L.cmode, L.nx, L.nz, get);
             C.e[K] = 0.f;
         }
         __syncthreads();
@@ -764,16 +778,7 @@ __device__ void tile_up(const SolveArgs& a, int l)
         for (int q = threadIdx.x; q < n; q += blockDim.x) {
             if (S.f[q]) continue;
             const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
-            const int i = T.ri + li, j = T.rj + lj;
-            const int I0 = i >> 1, J0 = j >> 1;
-            const bool oi = i & 1, oj = j & 1;
-            const size_t b = (size_t)I0 * C.nz + J0;
-            float v;
-            if (!oi && !oj) v = ce[b];
-            else if (oi && !oj) v = 0.5f * (ce[b] + ce[b + C.nz]);
-            else if (!oi && oj) v = 0.5f * (ce[b] + ce[b + 1]);
-            else v = 0.25f * (ce[b] + ce[b + C.nz] + ce[b + 1] + ce[b + C.nz + 1]);
-            S.e[q] += v;
+            S.e[q] += prolong_node(T.ri + li, T.rj + lj, L.cmode, ce, C.nz);
         }
         __syncthreads();
         int pass = 0;

@@ -296,11 +296,14 @@ void Sim::setup_solver()
     if (solver_ready) return;
     validate_operator();
     const int coord = p.coord == CYLINDRICAL ? 1 : 0;
-    std::vector<int> lnx, lnz;
-    multigrid_levels(nx, nz, kMaxLevels, lnx, lnz);
+    std::vector<int> lnx, lnz, lmode;
+    // couplings of the fine operator: r ones ~ 1/dx^2, z ones 1/dz^2 (cylindrical); unit in Cartesian runs
+    multigrid_levels(nx, nz, coord == 1 ? (dz * dz) / (dx * dx) : 1.0, kMaxLevels, lnx, lnz, lmode);
     lv.nlev = (int)lnx.size();
     lv.nx = lnx;
     lv.nz = lnz;
+    lv.cmode.assign(lv.nlev, kCoarsenFull);
+    for (int l = 0; l + 1 < lv.nlev; ++l) lv.cmode[l] = lmode[l + 1];
     lv.e.resize(lv.nlev);
     lv.r.resize(lv.nlev);
     lv.t.resize(lv.nlev);
@@ -318,7 +321,7 @@ void Sim::setup_solver()
         lv.e[l].zero(stream);
         if (l == 0) continue;
         int cx, cz;
-        galerkin(lnx[l - 1], lnz[l - 1], A, fixed_f, cx, cz, Ac);
+        galerkin(lnx[l - 1], lnz[l - 1], A, fixed_f, lmode[l], cx, cz, Ac);
         std::vector<float> cf(Ac.begin(), Ac.end()), idg(n);
         for (size_t k = 0; k < n; ++k) idg[k] = (float)(1.0 / Ac[4 * n + k]);
         lv.coef[l].upload(cf.data(), cf.size(), stream);
@@ -640,6 +643,7 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
         a.lev[l].t = lv.t[l].p;
         a.lev[l].coef = lv.coef[l].p;
         a.lev[l].inv_diag = lv.inv_diag[l].p;
+        a.lev[l].cmode = lv.cmode[l];
     }
     a.nu1 = 2;
     a.nu2 = 2;

@@ -121,6 +121,7 @@ struct SourceState {
 struct SolverLevels {
     int nlev = 0;
     std::vector<int> nx, nz;
+    std::vector<int> cmode;      // how level l is coarsened to level l + 1 (kCoarsen*)
     std::vector<DevArray<float>> e, r, t, coef, inv_diag;
     DevArray<float> coarse_inv;  // dense inverse of the coarsest level (column-major) or empty
     DevArray<double> st64;       // fine stencil rows (w, e, c)
