@@ -60,7 +60,7 @@ BYTES_PER_NODE_STEP = 24
 # dram__bytes_write.sum of one launch, divided by the particles):
 #   profiles/k_push_fused_multipole_xy_1e6.md   (50 fused steps per launch)
 #   profiles/k_push_penning_large_rz_2e7.md     (one step per launch)
-DRAM_BYTES_PER_PARTICLE = {"multipole": 24.8, "large": 41.6}
+DRAM_BYTES_PER_PARTICLE = {"multipole": 24.8, "large": 41.7}
 # ncu warp instructions per 32 particle-steps of k_push_fused<0,2,0>
 # (smsp__inst_executed per launch / (1e6 x 50 / 32), profiles/k_push_fused_multipole_xy_1e6.md)
 FUSED_WARP_INSTR_PER_32 = 177
@@ -506,8 +506,8 @@ def measure_single(args, wk: str, rank: int = 0, world: int = 1, local: int = 0,
                                         "large": "profiles/k_push_penning_large_rz_2e7.md"}.get(wk),
                      "kernel": ("k_push_fused<0,2,0> (50 steps per launch: gather + Boris + collision test + "
                                 "background scatter + boundary)" if wk == "multipole" else
-                                "k_push<1,1,1,2> (cylindrical gather + Boris + r map + boundary + collision test + "
-                                "deposit)"),
+                                "k_push<1,1,1,VEC> (cylindrical gather + Boris + r map + boundary + collision test + "
+                                "deposit; 4 slots per thread for 1e8 electrons, 2 for 1e5)"),
                      "alg_bytes_per_launch": alg_bytes, "bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
                      "kernel_ms": push_ms, "peak_source": peak_src},
         "kernel_ms_per_step": {"sort": kern[0] / L, "solve": kern[1] / L, "particles": kern[2] / L,
