@@ -47,6 +47,7 @@ constexpr uint32_t kFracMask = (1u << kFracBits) - 1u;
 constexpr uint32_t kDead = 0xFFFFFFFFu;
 constexpr int kMaxCellsPerAxis = 4095;
 constexpr int64_t kSlotAlign = 64;  // particle arrays hold a multiple of this many slots (vector access)
+constexpr int64_t kScrambledSortMin = 4000000;  // slots from which scrambled input takes the three-pass sort
 
 // CollType of the species_conf INTERACTION blocks (src/parser.hpp:15)
 enum CollType { ELASTIC = 0, LANGEVIN = 1, CX = 2, COULOMB = 3, SUPERELASTIC = 4 };
@@ -174,7 +175,8 @@ struct SortArgs {
     uint32_t* oid;
     int64_t n;
     int nx, nz;
-    long long ncells;        // (nx-1)*(nz-1)
+    int si, sj, nzk;         // sort key of cell (i, j): (i >> si) * nzk + (j >> sj)
+    long long ncells;        // number of keys: ((nx-2 >> si) + 1) * nzk
     uint32_t* count;         // ncells, zero on entry and on exit
     uint32_t* offset;        // ncells + 1
     uint32_t* blocksum;      // ceil(ncells/1024)

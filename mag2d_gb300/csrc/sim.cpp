@@ -835,6 +835,7 @@ void Sim::add_loaded(int s, int64_t n, int kind, double cx, double cz, double ra
     MAG_CK(cudaGetLastError());
     S.n_slots += n;
     S.next_id += (uint32_t)n;
+    S.scrambled = true;
     upload_slots(s);
     init_ttd(s, o, n);
     sort_due = true;
@@ -1047,6 +1048,11 @@ CollideArgs Sim::collide_args(int s)
 }
 
 // Counting sort by cell into the double buffers, then swap (compacts removed particles).
+// Counting sort of one species by cell.  Slots that a loader or
+// set_particles filled in no cell order are sorted in three passes of
+// decreasing key size (blocks of 64 x 128 cells, blocks of 4 x 8 cells, cells),
+// so that each pass meets only a few hundred keys per chunk of slots and its
+// stores leave in runs; slots sorted a few steps ago take the single pass by cell.
 void Sim::sort_species(int s)
 {
     SpeciesState& S = sp[s];
@@ -1059,34 +1065,47 @@ void Sim::sort_species(int s)
         S.bvz.alloc(S.cap);
         S.bid.alloc(S.cap);
     }
-    SortArgs a{};
-    a.x = S.x.p;
-    a.z = S.z.p;
-    a.vx = S.vx.p;
-    a.vy = S.vy.p;
-    a.vz = S.vz.p;
-    a.id = S.id.p;
-    a.ox = S.bx.p;
-    a.oz = S.bz.p;
-    a.ovx = S.bvx.p;
-    a.ovy = S.bvy.p;
-    a.ovz = S.bvz.p;
-    a.oid = S.bid.p;
-    a.n = S.n_slots;
-    a.nx = nx;
-    a.nz = nz;
-    a.ncells = (long long)(nx - 1) * (nz - 1);
-    a.count = sort_count.p;
-    a.offset = sort_offset.p;
-    a.blocksum = sort_blocksum.p;
-    a.cnt = S.cnt.p;
-    launches += launch_sort(a, S.n_slots, stream);
-    std::swap(S.x, S.bx);
-    std::swap(S.z, S.bz);
-    std::swap(S.vx, S.bvx);
-    std::swap(S.vy, S.bvy);
-    std::swap(S.vz, S.bvz);
-    std::swap(S.id, S.bid);
+    struct KeyLevel {
+        int si, sj;
+    };
+    static const KeyLevel kScrambled[3] = {{6, 7}, {2, 3}, {0, 0}};
+    static const KeyLevel kCells[1] = {{0, 0}};
+    const bool three = S.scrambled && S.n_slots >= kScrambledSortMin;
+    const KeyLevel* lv = three ? kScrambled : kCells;
+    for (int pass = 0; pass < (three ? 3 : 1); ++pass) {
+        SortArgs a{};
+        a.x = S.x.p;
+        a.z = S.z.p;
+        a.vx = S.vx.p;
+        a.vy = S.vy.p;
+        a.vz = S.vz.p;
+        a.id = S.id.p;
+        a.ox = S.bx.p;
+        a.oz = S.bz.p;
+        a.ovx = S.bvx.p;
+        a.ovy = S.bvy.p;
+        a.ovz = S.bvz.p;
+        a.oid = S.bid.p;
+        a.n = S.n_slots;
+        a.nx = nx;
+        a.nz = nz;
+        a.si = lv[pass].si;
+        a.sj = lv[pass].sj;
+        a.nzk = ((nz - 2) >> a.sj) + 1;
+        a.ncells = (long long)(((nx - 2) >> a.si) + 1) * a.nzk;
+        a.count = sort_count.p;
+        a.offset = sort_offset.p;
+        a.blocksum = sort_blocksum.p;
+        a.cnt = S.cnt.p;
+        launches += launch_sort(a, S.n_slots, stream);
+        std::swap(S.x, S.bx);
+        std::swap(S.z, S.bz);
+        std::swap(S.vx, S.bvx);
+        std::swap(S.vy, S.bvy);
+        std::swap(S.vz, S.bvz);
+        std::swap(S.id, S.bid);
+    }
+    S.scrambled = false;
 }
 
 // One Pic::advance (src/pic.cpp:330-358).  Species advance in order, each
@@ -1404,9 +1423,36 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     launches += launch_set_particles(cols, n, g, S.x.p, S.z.p, S.vx.p, S.vy.p, S.vz.p, S.id.p, stream);
     S.n_slots = n;
     S.next_id = (uint32_t)n;
+    S.scrambled = cell_order_broken(x, z, n);
     upload_slots(s);
     init_ttd(s, 0, n);
     sort_due = true;
+}
+
+// Whether host particles come in no cell order: eight windows of 512
+// consecutive particles spread over the arrays, scrambled when more than a
+// quarter of the neighbour pairs step back in cell index.  (Particles read back
+// from a sorted species step back only where one crossed a cell edge since.)
+bool Sim::cell_order_broken(const double* x, const double* z, int64_t n) const
+{
+    if (n < 2) return false;
+    auto index = [](double f, int last) {  // floor(f) clamped to [0, last]; non-finite -> 0
+        return f >= 0.0 ? (int64_t)std::min(std::floor(f), (double)last) : (int64_t)0;
+    };
+    auto cell = [&](int64_t k) { return index((x[k] - x0) / dx, nx - 2) * (nz - 1) + index((z[k] - z0) / dz, nz - 2); };
+    const int64_t w = std::min<int64_t>(512, n);
+    int64_t pairs = 0, back = 0;
+    for (int k = 0; k < 8; ++k) {
+        const int64_t first = (n - w) * k / 8;
+        int64_t prev = cell(first);
+        for (int64_t q = first + 1; q < first + w; ++q) {
+            const int64_t c = cell(q);
+            back += c < prev;
+            ++pairs;
+            prev = c;
+        }
+    }
+    return 4 * back > pairs;
 }
 
 // Pic::print_trace (src/pic.cpp:446-451): TrackedParticle::print of every

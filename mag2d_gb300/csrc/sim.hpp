@@ -99,6 +99,7 @@ struct SpeciesState {
     DevArray<MccSpecies> mcc;
     int64_t cap = 0, n_slots = 0;
     uint32_t next_id = 0;
+    bool scrambled = false;            // slots filled in no cell order since the last sort (loaders, set_particles)
     DevArray<unsigned long long> rho;  // fixed-point charge grid
     DevArray<Counters> cnt;
     uint64_t niter = 0;                // steps advanced (Species::advance niter++, particles.hpp:347)
@@ -309,6 +310,7 @@ private:
     void fused_block(int nsteps, double* ms = nullptr);
     float rf_factor(uint64_t niter, double dt) const;
     void sort_species(int s);
+    bool cell_order_broken(const double* x, const double* z, int64_t n) const;
     void refresh_rf_pairs();
     void upload_slots(int s);
     void init_ttd(int s, int64_t first, int64_t n);

@@ -372,18 +372,52 @@ def test_sort_does_not_change_results(m, tmp_path):
     from cases import penning_rz
 
     cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=5000)
-    out = []
+    out, descents = [], []
     for si in (1, -1):
         pic = m.Pic(cpath, spath, seed=5, sort_interval=si)
         pic.speclist[0].set_particles(*parts)
         pic.advance_init()
         pic.advance(200)
         g = pic.speclist[0].particles()
+        # slot order: cell index (r-major) of each live particle
+        nz = pic.shape[1]
+        cell = np.floor((g["x"] - pic.x_min) / pic.dx).astype(np.int64) * (nz - 1) + \
+            np.floor((g["z"] - pic.z_min) / pic.dz).astype(np.int64)
+        descents.append(np.mean(np.diff(cell) < 0))
         order = np.argsort(g["id"])
         out.append({k: v[order] for k, v in g.items()})
         pic.close()
     for k in ("id", "x", "z", "vx", "vy", "vz"):
         assert np.array_equal(out[0][k], out[1][k]), k
+    # sorted one step ago: only particles that crossed a cell edge since are out of order
+    assert descents[0] < 0.2 and descents[1] > 0.3, descents
+
+
+def test_scrambled_sort_three_passes(m, tmp_path):
+    """5e6 particles loaded in random order take the three-pass sort (blocks of
+    cells, smaller blocks, cells): the particles after 3 steps are bit-identical
+    to a run that never sorts, and they sit in cell order."""
+    from cases import penning_rz
+
+    cfg, species, inter, cpath, spath, parts = penning_rz(tmp_path, n=5_000_000, nr=257, nz=513)
+    out, descents = [], []
+    for si in (1, -1):
+        pic = m.Pic(cpath, spath, seed=8, sort_interval=si)
+        pic.speclist[0].set_particles(*parts)
+        pic.advance_init()
+        pic.advance(3)
+        g = pic.speclist[0].particles()
+        nz = pic.shape[1]
+        cell = np.floor((g["x"] - pic.x_min) / pic.dx).astype(np.int64) * (nz - 1) + \
+            np.floor((g["z"] - pic.z_min) / pic.dz).astype(np.int64)
+        descents.append(np.mean(np.diff(cell) < 0))
+        order = np.argsort(g["id"])
+        out.append({k: v[order] for k, v in g.items()})
+        pic.close()
+    assert len(out[0]["id"]) > 4_000_000
+    for k in ("id", "x", "z", "vx", "vy", "vz"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+    assert descents[0] < 0.2 and descents[1] > 0.3, descents
 
 
 def test_inverse_solve_partial_rows_cover_the_particles(m, tmp_path):
