@@ -582,10 +582,8 @@ def measure_batched(args, local: int = 0) -> dict:
     b.close()
     stride = max(1, n_inst // args.plain_sample)
     sample = list(range(0, n_inst, stride))
-    plain = []
-    for i in sample:
-        c = inst[i]
-        pic = m.Pic(c[3], c[4], c[5], seed=c[6], device=local, poisson_tol=1e-9)
+    def plain_step_ms(c, **kw):
+        pic = m.Pic(c[3], c[4], c[5], seed=c[6], device=local, poisson_tol=1e-9, **kw)
         pic.advance_init()
         pic.advance(3)
         s_ = torch.cuda.ExternalStream(pic.stream, device=local)
@@ -595,9 +593,17 @@ def measure_batched(args, local: int = 0) -> dict:
         pic.advance(args.plain_steps)
         a1.record(s_)
         torch.cuda.synchronize()
-        plain.append(a0.elapsed_time(a1) / args.plain_steps)
+        res = pic.solve_status()["residual"]
         pic.close()
-    plain_ms = float(np.mean(plain)) * n_inst  # the sweep one instance after another
+        return a0.elapsed_time(a1) / args.plain_steps, res
+
+    # plain: each instance alone with the default solver (the precomputed
+    # inverse on grids up to 2e4 nodes, else FP32 multigrid + FP64 refinement);
+    # plain FP64: each instance alone with every multigrid level in FP64
+    plain = [plain_step_ms(inst[i]) for i in sample]
+    plain64 = [plain_step_ms(inst[i], direct_solve=-1, multigrid_fp64=1) for i in sample]
+    plain_ms = float(np.mean([p_[0] for p_ in plain])) * n_inst  # the sweep one instance after another
+    plain64_ms = float(np.mean([p_[0] for p_ in plain64])) * n_inst
     batch_step_ms = batch_ms / args.steps
     return {"metric": METRIC, "value": psteps / (batch_ms * 1e-3), "unit": UNIT, "ms_per_step": batch_step_ms,
             "steps": args.steps,
@@ -607,9 +613,14 @@ def measure_batched(args, local: int = 0) -> dict:
             "clocks": clk.summary(), "gpu_launches": int(launches),
             "batched_vs_plain": {"batched_ms_per_step": batch_step_ms, "plain_ms_per_step": plain_ms,
                                  "speedup": plain_ms / batch_step_ms,
+                                 "plain_fp64_multigrid_ms_per_step": plain64_ms,
+                                 "speedup_vs_fp64_multigrid": plain64_ms / batch_step_ms,
                                  "plain_sample": f"{len(sample)} of {n_inst} instances (every {stride}th), "
                                                  f"{args.plain_steps} steps each, summed over the sweep",
-                                 "max_final_poisson_residual": max_res},
+                                 "tolerance": "every solve stops at Jacobi-scaled residual <= 1e-9 of max|u|",
+                                 "max_final_poisson_residual": {
+                                     "batched": max_res, "plain": max(p_[1] for p_ in plain),
+                                     "plain_fp64_multigrid": max(p_[1] for p_ in plain64)}},
             "tuning": tuning, "setup_s": setup_s}
 
 

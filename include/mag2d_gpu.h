@@ -63,6 +63,9 @@ typedef struct {
                               field, collision targets without particles), up to this many steps run
                               as one particle launch, with results identical to single steps
                               (0 = 64, 1 = never) */
+    int multigrid_fp64;    /* 1: multigrid Poisson solves with every level in FP64 (no FP32 V-cycle), for
+                              grids up to 70000 nodes; slower, kept to time the FP32 multigrid with FP64
+                              refinement against (0 = FP32 multigrid + FP64 refinement) */
 } mag_opts;
 
 typedef struct {

@@ -18,7 +18,8 @@ class MagOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("seed", ctypes.c_uint64), ("sort_interval", ctypes.c_int),
                 ("poisson_tol", ctypes.c_double), ("poisson_max_iter", ctypes.c_int),
                 ("capacity_hint", ctypes.c_int64), ("push_vec", ctypes.c_int),
-                ("direct_solve", ctypes.c_int), ("max_fused_steps", ctypes.c_int)]
+                ("direct_solve", ctypes.c_int), ("max_fused_steps", ctypes.c_int),
+                ("multigrid_fp64", ctypes.c_int)]
 
 
 class MagSpeciesInfo(ctypes.Structure):

@@ -103,6 +103,7 @@ int mag_create(const char* config_path, const char* species_conf_path, const cha
             o.push_vec = opts->push_vec;
             o.direct_solve = opts->direct_solve;
             o.max_fused_steps = opts->max_fused_steps;
+            o.multigrid_fp64 = opts->multigrid_fp64;
         }
         auto h = std::make_unique<mag_sim>();
         h->s = std::unique_ptr<mag::Sim, SimRelease>(new mag::Sim(config_path, species_conf_path, o), SimRelease{true});

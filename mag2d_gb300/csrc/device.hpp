@@ -401,6 +401,19 @@ struct SolveArgs {
     double* prof;           // phase times of the solve [ns] (kSolvePhases slots), or null
 };
 
+// FP64 multigrid levels (the all-FP64 solver option): the same hierarchy and
+// Galerkin operators as the FP32 levels, every array in FP64
+struct MG64Level {
+    int nx, nz, cmode;
+    double *e, *r, *t;
+    const double* coef;      // 9 planes (levels >= 1)
+    const double* inv_diag;  // levels >= 1
+};
+struct MG64Args {
+    MG64Level lev[kMaxLevels];
+    const double* coarse_inv;  // dense inverse of the coarsest level, column-major (null: smooth it)
+};
+
 // bytes of the argument copy in front of block 0's staged coarse levels (16-byte aligned)
 constexpr size_t kStagedArgsBytes = (sizeof(SolveArgs) + 15) & ~(size_t)15;
 

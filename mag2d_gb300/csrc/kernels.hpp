@@ -75,6 +75,8 @@ int solve_max_blocks(int sm_count, size_t smem = 0);
 // n independent single-block solves, arguments in device memory (one block of
 // 'threads' threads each; grids up to kSingleBlockNodes nodes)
 int launch_solve_batch(const SolveArgs* d_args, int n, int threads, cudaStream_t s);
+// the all-FP64 multigrid solve of one grid of at most kSingleBlockNodes nodes (one block)
+int launch_solve64(const SolveArgs& a, const MG64Args& g, cudaStream_t s);
 int launch_faces(const double* u, int nx, int nz, double dx, double dz, float* Exf, float* Ezf, cudaStream_t s);
 // Fields::u_smooth(): u = the smoothing of t, a copy of u (nx*nz each)
 int launch_u_smooth(const double* t, double* u, int nx, int nz, cudaStream_t s);

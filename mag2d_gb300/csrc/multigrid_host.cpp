@@ -161,6 +161,14 @@ void fine_stencil_table(int coord, int nx, double dx, double dz, std::vector<dou
 
 bool dense_inverse(int nx, int nz, const std::vector<double>& A9, std::vector<float>& inv)
 {
+    std::vector<double> inv64;
+    if (!dense_inverse64(nx, nz, A9, inv64)) return false;
+    inv.assign(inv64.begin(), inv64.end());
+    return true;
+}
+
+bool dense_inverse64(int nx, int nz, const std::vector<double>& A9, std::vector<double>& inv)
+{
     const int n = nx * nz;
     std::vector<double> M((size_t)n * 2 * n, 0.0);  // [A | I], row-major, row length 2n
     const size_t w = 2 * (size_t)n;
@@ -195,9 +203,9 @@ bool dense_inverse(int nx, int nz, const std::vector<double>& A9, std::vector<fl
             for (size_t q = (size_t)c; q < w; ++q) M[r * w + q] -= f * M[c * w + q];
         }
     }
-    inv.assign((size_t)n * n, 0.f);
+    inv.assign((size_t)n * n, 0.0);
     for (int r = 0; r < n; ++r)
-        for (int c = 0; c < n; ++c) inv[(size_t)c * n + r] = (float)M[r * w + n + c];
+        for (int c = 0; c < n; ++c) inv[(size_t)c * n + r] = M[r * w + n + c];
     return true;
 }
 

@@ -51,6 +51,8 @@ void fine_stencil_table(int coord, int nx, double dx, double dz, std::vector<dou
 // Gauss-Jordan with partial pivoting, stored in FP32 column-major
 // (inv[col * n + row]).  Returns false when the operator is singular.
 bool dense_inverse(int nx, int nz, const std::vector<double>& A9, std::vector<float>& inv);
+// the same inverse kept in FP64
+bool dense_inverse64(int nx, int nz, const std::vector<double>& A9, std::vector<double>& inv);
 
 // Tile of a level of a multi-block solve: the interior size ti x tj that
 // minimises (tiles per block, rounded up) x (region nodes), the region being

@@ -16,6 +16,7 @@
 // serves grids up to a few 1e4 nodes; larger grids run the same code on many
 // blocks under a cooperative launch with a bounded grid barrier.
 #include <cooperative_groups.h>
+#include <utility>
 
 #include "device.hpp"
 #include "kernels.hpp"
@@ -334,25 +335,25 @@ __device__ __forceinline__ int coarsen_sx(int m) { return m == 2 ? 1 : 2; }
 __device__ __forceinline__ int coarsen_sz(int m) { return m == 1 ? 1 : 2; }
 
 // coarse residual of node (I, J): P^T t around fine (sx I, sz J); get(i, j)
-// returns the fine residual (0 at fixed fine nodes)
-template <class Get>
-__device__ __forceinline__ float restrict_node(int I, int J, int m, int nxf, int nzf, const Get& get)
+// returns the fine residual (0 at fixed fine nodes) as float or double
+template <class Get, class T = decltype(std::declval<Get>()(0, 0))>
+__device__ __forceinline__ T restrict_node(int I, int J, int m, int nxf, int nzf, const Get& get)
 {
     const int sx = coarsen_sx(m), sz = coarsen_sz(m);
     const int rx = sx - 1, rz = sz - 1;
-    float acc = 0.f;
+    T acc = T(0);
 #pragma unroll
     for (int di = -1; di <= 1; ++di) {
         if (di < -rx || di > rx) continue;
         const int i = sx * I + di;
         if (i < 0 || i >= nxf) continue;
-        const float wi = di == 0 ? 1.f : 0.5f;
+        const T wi = di == 0 ? T(1) : T(0.5);
 #pragma unroll
         for (int dj = -1; dj <= 1; ++dj) {
             if (dj < -rz || dj > rz) continue;
             const int j = sz * J + dj;
             if (j < 0 || j >= nzf) continue;
-            const float wj = dj == 0 ? 1.f : 0.5f;
+            const T wj = dj == 0 ? T(1) : T(0.5);
             acc += wi * wj * get(i, j);
         }
     }
@@ -360,16 +361,17 @@ __device__ __forceinline__ float restrict_node(int I, int J, int m, int nxf, int
 }
 
 // fine value (i, j) of P e_coarse
-__device__ __forceinline__ float prolong_node(int i, int j, int m, const float* __restrict__ ec, int ncz)
+template <class T>
+__device__ __forceinline__ T prolong_node(int i, int j, int m, const T* __restrict__ ec, int ncz)
 {
     const int sx = coarsen_sx(m), sz = coarsen_sz(m);
     const int I0 = sx == 2 ? i >> 1 : i, J0 = sz == 2 ? j >> 1 : j;
     const bool oi = sx == 2 && (i & 1), oj = sz == 2 && (j & 1);
     const size_t b = (size_t)I0 * ncz + J0;
     if (!oi && !oj) return ec[b];
-    if (oi && !oj) return 0.5f * (ec[b] + ec[b + ncz]);
-    if (!oi && oj) return 0.5f * (ec[b] + ec[b + 1]);
-    return 0.25f * (ec[b] + ec[b + ncz] + ec[b + 1] + ec[b + ncz + 1]);
+    if (oi && !oj) return T(0.5) * (ec[b] + ec[b + ncz]);
+    if (!oi && oj) return T(0.5) * (ec[b] + ec[b + 1]);
+    return T(0.25) * (ec[b] + ec[b + ncz] + ec[b + 1] + ec[b + ncz + 1]);
 }
 
 // r_{l+1} = P^T t_l (weights 1, 1/2, 1/4; fixed fine nodes carry no residual); e_{l+1} = 0
@@ -892,14 +894,11 @@ __device__ void vcycle_tiled(const SolveArgs& a, Team& t, bool& ok)
     }
 }
 
-__device__ void solve_body(const SolveArgs& a, Team& t)
+// Steps 0 and 1 of a solve, shared by the FP32 and the FP64 multigrid
+__device__ void solve_prologue(const SolveArgs& a, Team& t, bool& ok)
 {
     const int nx = a.nx, nz = a.nz;
     const unsigned nn = (unsigned)(nx * nz);
-    bool ok = true;
-    t.prof = a.prof;
-    const unsigned long long t_start = Team::now();
-    t.t_mark = t_start;
     // 0. start of a step's solve: the linear extrapolation of the last two solutions
     if (a.u_prev) {
         const bool valid = *((volatile const int*)a.u_prev_valid) != 0;
@@ -934,6 +933,30 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
             for (int s = 0; s < a.nsp; ++s) ((unsigned long long*)a.rho_fixed[s])[k] = 0ull;
     }
     ok = t.sync();
+}
+
+// the solve's status words (thread 0 of the team)
+__device__ void solve_report(const SolveArgs& a, const Team& t, int it, double res, bool conv, bool ok)
+{
+    if (t.tid != 0) return;
+    a.status->iterations = it;
+    a.status->residual = res;
+    a.status->converged = conv ? 1 : 0;
+    a.status->aborted = ok ? 0 : 1;
+    if (!ok) atomicCAS(a.err, 0, -5);
+    else if (!conv) atomicCAS(a.err, 0, -4);
+}
+
+__device__ void solve_body(const SolveArgs& a, Team& t)
+{
+    const int nx = a.nx, nz = a.nz;
+    const unsigned nn = (unsigned)(nx * nz);
+    bool ok = true;
+    t.prof = a.prof;
+    const unsigned long long t_start = Team::now();
+    t.t_mark = t_start;
+    solve_prologue(a, t, ok);
+    const FastDiv dnz((unsigned)nz);
     t.mark(kPhaseStart);
     // 2. FP64 residual refinement around the FP32 multigrid
     int it = 0;
@@ -1021,14 +1044,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
     if (ok && a.Exf != nullptr) faces_pass(a.u, nx, nz, a.idx, a.idz, a.Exf, a.Ezf, t.tid, t.nthreads);
     t.mark(kPhaseFaces);
     if (a.prof && blockIdx.x == 0 && threadIdx.x == 0) a.prof[kPhaseTotal] += (double)(Team::now() - t_start);
-    if (t.tid == 0) {
-        a.status->iterations = it;
-        a.status->residual = res;
-        a.status->converged = conv ? 1 : 0;
-        a.status->aborted = ok ? 0 : 1;
-        if (!ok) atomicCAS(a.err, 0, -5);
-        else if (!conv) atomicCAS(a.err, 0, -4);
-    }
+    solve_report(a, t, it, res, conv, ok);
 }
 
 __global__ void __launch_bounds__(1024) k_solve(const __grid_constant__ SolveArgs a)
@@ -1049,6 +1065,218 @@ __global__ void __launch_bounds__(1024) k_solve_batch(const SolveArgs* __restric
     __syncthreads();
     Team t = Team::block(nullptr);
     solve_body(*reinterpret_cast<const SolveArgs*>(raw), t);
+}
+
+// ---- FP64 multigrid (the all-FP64 solver option) ---------------------------
+//
+// The same V-cycle as the single-block FP32 path (red-black Gauss-Seidel on
+// the fine level, 4-colour Gauss-Seidel on the Galerkin levels, bilinear
+// transfers, dense coarsest inverse) with every level in FP64, iterated on the
+// FP64 residual to the same stopping rule.  It is what the FP32 multigrid with
+// FP64 refinement replaces, kept as a solver option so that the two can be
+// timed against each other at the same tolerance.  One block per solve: grids
+// up to kSingleBlockNodes nodes.
+
+__device__ void smooth_fine64(const SolveArgs& a, const MG64Args& g, Team& t, int sweeps, bool reverse, double omega)
+{
+    const MG64Level& L = g.lev[0];
+    const int nx = L.nx, nz = L.nz, hz = (nz + 1) / 2;
+    double* __restrict__ e = L.e;
+    const double* __restrict__ r = L.r;
+    const double k2 = a.k2;
+    const unsigned n = (unsigned)(nx * hz);
+    const FastDiv dh((unsigned)hz);
+    for (int s = 0; s < sweeps; ++s)
+        for (int cc = 0; cc < 2; ++cc) {
+            const int color = reverse ? 1 - cc : cc;
+            for (unsigned q = t.tid; q < n; q += t.nthreads) {
+                const int i = (int)dh.div(q);
+                const int j = 2 * (int)(q - (unsigned)i * hz) + ((i + color) & 1);
+                if (j >= nz) continue;
+                const size_t k = (size_t)i * nz + j;
+                if (is_fixed(a.mask[k])) continue;
+                const double* st = a.st64 + 4 * i;
+                double acc = r[k] - st[1] * e[k + nz] - k2 * (e[k - 1] + e[k + 1]);
+                if (i > 0) acc -= st[0] * e[k - nz];
+                const double enew = acc * st[3];
+                e[k] = omega == 1.0 ? enew : e[k] + omega * (enew - e[k]);
+            }
+            __syncthreads();
+        }
+}
+
+__device__ __forceinline__ double coarse_apply64(const double* __restrict__ coef, int nx, int nz, int i, int j, size_t k,
+                                                 const double* __restrict__ e, bool skip_center)
+{
+    const size_t n = (size_t)nx * nz;
+    double acc = 0.0;
+#pragma unroll
+    for (int di = -1; di <= 1; ++di) {
+        if (i + di < 0 || i + di >= nx) continue;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+            if (j + dj < 0 || j + dj >= nz) continue;
+            if (skip_center && di == 0 && dj == 0) continue;
+            acc += coef[((di + 1) * 3 + (dj + 1)) * n + k] * e[k + (ptrdiff_t)di * nz + dj];
+        }
+    }
+    return acc;
+}
+
+__device__ void smooth_coarse64(const MG64Level& L, Team& t, int sweeps, bool reverse)
+{
+    const int nx = L.nx, nz = L.nz, hx = (nx + 1) / 2, hz = (nz + 1) / 2;
+    const unsigned n = (unsigned)(hx * hz);
+    const FastDiv dh((unsigned)hz);
+    for (int s = 0; s < sweeps; ++s)
+        for (int cc = 0; cc < 4; ++cc) {
+            const int color = reverse ? 3 - cc : cc;
+            const int ci = color >> 1, cj = color & 1;
+            for (unsigned q = t.tid; q < n; q += t.nthreads) {
+                const unsigned qi = dh.div(q);
+                const int i = 2 * (int)qi + ci, j = 2 * (int)(q - qi * hz) + cj;
+                if (i >= nx || j >= nz) continue;
+                const size_t k = (size_t)i * nz + j;
+                L.e[k] = (L.r[k] - coarse_apply64(L.coef, nx, nz, i, j, k, L.e, true)) * L.inv_diag[k];
+            }
+            __syncthreads();
+        }
+}
+
+// t = r - A e on level l (fine level: free nodes only)
+__device__ void residual64(const SolveArgs& a, const MG64Args& g, Team& t, int l)
+{
+    const MG64Level& L = g.lev[l];
+    const int nx = L.nx, nz = L.nz;
+    const unsigned n = (unsigned)(nx * nz);
+    const FastDiv dz((unsigned)nz);
+    for (unsigned q = t.tid; q < n; q += t.nthreads) {
+        const int i = (int)dz.div(q);
+        if (l == 0) {
+            if (is_fixed(a.mask[q])) {
+                L.t[q] = 0.0;
+                continue;
+            }
+            const double* st = a.st64 + 4 * i;
+            double acc = L.r[q] - st[2] * L.e[q] - st[1] * L.e[q + nz] - a.k2 * (L.e[q - 1] + L.e[q + 1]);
+            if (i > 0) acc -= st[0] * L.e[q - nz];
+            L.t[q] = acc;
+        } else {
+            L.t[q] = L.r[q] - coarse_apply64(L.coef, nx, nz, i, (int)(q - (unsigned)i * nz), q, L.e, false);
+        }
+    }
+    __syncthreads();
+}
+
+__device__ void restrict64(const MG64Args& g, Team& t, int l)
+{
+    const MG64Level& F = g.lev[l];
+    const MG64Level& C = g.lev[l + 1];
+    const unsigned n = (unsigned)(C.nx * C.nz);
+    const FastDiv dz((unsigned)C.nz);
+    auto get = [&](int i, int j) { return F.t[(size_t)i * F.nz + j]; };
+    for (unsigned q = t.tid; q < n; q += t.nthreads) {
+        const int I = (int)dz.div(q), J = (int)(q - (unsigned)I * C.nz);
+        C.r[q] = restrict_node(I, J, F.cmode, F.nx, F.nz, get);
+        C.e[q] = 0.0;
+    }
+    __syncthreads();
+}
+
+__device__ void prolong64(const SolveArgs& a, const MG64Args& g, Team& t, int l)
+{
+    const MG64Level& F = g.lev[l];
+    const MG64Level& C = g.lev[l + 1];
+    const unsigned n = (unsigned)(F.nx * F.nz);
+    const FastDiv dz((unsigned)F.nz);
+    for (unsigned q = t.tid; q < n; q += t.nthreads) {
+        if (l == 0 && is_fixed(a.mask[q])) continue;
+        const int i = (int)dz.div(q), j = (int)(q - (unsigned)i * F.nz);
+        F.e[q] += prolong_node(i, j, F.cmode, (const double*)C.e, C.nz);
+    }
+    __syncthreads();
+}
+
+__device__ void vcycle64(const SolveArgs& a, const MG64Args& g, Team& t)
+{
+    const int L = a.nlev;
+    if (L == 1) {
+        smooth_fine64(a, g, t, a.ncoarse, false, (double)a.omega);
+        return;
+    }
+    for (int l = 0; l < L - 1; ++l) {
+        if (l == 0) smooth_fine64(a, g, t, a.nu1, false, 1.0);
+        else smooth_coarse64(g.lev[l], t, a.nu1, false);
+        residual64(a, g, t, l);
+        restrict64(g, t, l);
+    }
+    const MG64Level& Lc = g.lev[L - 1];
+    if (g.coarse_inv) {
+        const unsigned n = (unsigned)(Lc.nx * Lc.nz);
+        for (unsigned row = t.tid; row < n; row += t.nthreads) {
+            double acc = 0.0;
+            for (unsigned c = 0; c < n; ++c) acc += g.coarse_inv[(size_t)c * n + row] * Lc.r[c];
+            Lc.e[row] = acc;
+        }
+        __syncthreads();
+    } else {
+        smooth_coarse64(Lc, t, a.ncoarse, false);
+    }
+    for (int l = L - 2; l >= 0; --l) {
+        prolong64(a, g, t, l);
+        if (l == 0) smooth_fine64(a, g, t, a.nu2, true, 1.0);
+        else smooth_coarse64(g.lev[l], t, a.nu2, true);
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_solve64(const __grid_constant__ SolveArgs a, const __grid_constant__ MG64Args g)
+{
+    Team t = Team::block(nullptr);
+    bool ok = true;
+    solve_prologue(a, t, ok);
+    const int nz = a.nz;
+    const unsigned nn = (unsigned)(a.nx * nz);
+    const FastDiv dnz((unsigned)nz);
+    const MG64Level& F = g.lev[0];
+    int it = 0;
+    double res = 0.0, ref0 = 0.0;
+    bool conv = false;
+    for (;; ++it) {
+        // r = b - A u in FP64 and its Jacobi-scaled max norm against max|u|
+        double lres = 0.0, lumax = 0.0;
+        for (unsigned k = t.tid; k < nn; k += t.nthreads) {
+            const int i = (int)dnz.div(k);
+            const double uk = a.u[k];
+            lumax = fmax(lumax, fabs(uk));
+            F.e[k] = 0.0;
+            if (is_fixed(a.mask[k])) {
+                F.r[k] = 0.0;
+                continue;
+            }
+            const Stencil5 st = fine_stencil(a, i);
+            double acc = st.c * uk + st.e * a.u[k + nz] + st.s * a.u[k - 1] + st.n * a.u[k + 1];
+            if (i > 0) acc += st.w * a.u[k - nz];
+            const double rk = a.b[k] - acc;
+            F.r[k] = rk;
+            lres = fmax(lres, fabs(rk * st.inv_c));
+        }
+        lres = block_max(lres);
+        lumax = block_max(lumax);
+        if (it == 0) ref0 = lres;
+        const double uref = lumax > 0.0 ? lumax : ref0;
+        res = uref > 0.0 ? lres / uref : lres;
+        if (res <= a.tol || lres == 0.0) {
+            conv = true;
+            break;
+        }
+        if (it >= a.max_outer) break;
+        vcycle64(a, g, t);
+        for (unsigned k = t.tid; k < nn; k += t.nthreads)
+            if (!is_fixed(a.mask[k])) a.u[k] += F.e[k];
+        __syncthreads();
+    }
+    if (a.Exf != nullptr) faces_pass(a.u, a.nx, a.nz, a.idx, a.idz, a.Exf, a.Ezf, t.tid, t.nthreads);
+    solve_report(a, t, it, res, conv, ok);
 }
 
 // ---- direct solve with the precomputed inverse ----------------------------
@@ -1326,6 +1554,12 @@ int launch_solve(const SolveArgs& a, int nblocks, cudaStream_t s, size_t smem)
         void* args[] = {(void*)&a};
         cudaLaunchCooperativeKernel((const void*)k_solve, dim3(nblocks), dim3(1024), args, smem, s);
     }
+    return 1;
+}
+
+int launch_solve64(const SolveArgs& a, const MG64Args& g, cudaStream_t s)
+{
+    k_solve64<<<1, 1024, 0, s>>>(a, g);
     return 1;
 }
 

@@ -64,6 +64,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     sort_interval = opts.sort_interval == 0 ? 20 : opts.sort_interval;
     push_vec = opts.push_vec == 1 || opts.push_vec == 2 || opts.push_vec == 4 ? opts.push_vec : 0;
     direct_mode = opts.direct_solve;
+    mg_fp64 = opts.multigrid_fp64 != 0;
     max_fused = opts.max_fused_steps <= 0 ? kMaxFusedSteps : std::min(opts.max_fused_steps, kMaxFusedSteps);
     if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sm_count < 1)
         sm_count = 1;
@@ -309,6 +310,12 @@ void Sim::setup_solver()
     lv.t.resize(lv.nlev);
     lv.coef.resize(lv.nlev);
     lv.inv_diag.resize(lv.nlev);
+    if (mg_fp64) {
+        if ((long long)nx * nz > kSingleBlockNodes)
+            throw Error(-1, "multigrid_fp64: the FP64 multigrid runs on one block, grids up to " +
+                                        std::to_string(kSingleBlockNodes) + " nodes");
+        for (auto* v : {&lv.e64, &lv.r64, &lv.t64, &lv.coef64, &lv.inv_diag64}) v->resize(lv.nlev);
+    }
     std::vector<double> A, Ac;
     fine_operator(coord, nx, nz, dx, dz, mask, A);
     std::vector<char> fixed_f(mask.size());
@@ -319,6 +326,12 @@ void Sim::setup_solver()
         lv.r[l].alloc(n);
         lv.t[l].alloc(n);
         lv.e[l].zero(stream);
+        if (mg_fp64) {
+            lv.e64[l].alloc(n);
+            lv.r64[l].alloc(n);
+            lv.t64[l].alloc(n);
+            lv.e64[l].zero(stream);
+        }
         if (l == 0) continue;
         int cx, cz;
         galerkin(lnx[l - 1], lnz[l - 1], A, fixed_f, lmode[l], cx, cz, Ac);
@@ -326,6 +339,12 @@ void Sim::setup_solver()
         for (size_t k = 0; k < n; ++k) idg[k] = (float)(1.0 / Ac[4 * n + k]);
         lv.coef[l].upload(cf.data(), cf.size(), stream);
         lv.inv_diag[l].upload(idg.data(), idg.size(), stream);
+        if (mg_fp64) {
+            std::vector<double> idg64(n);
+            for (size_t k = 0; k < n; ++k) idg64[k] = 1.0 / Ac[4 * n + k];
+            lv.coef64[l].upload(Ac.data(), Ac.size(), stream);
+            lv.inv_diag64[l].upload(idg64.data(), idg64.size(), stream);
+        }
         MAG_CK(cudaStreamSynchronize(stream));
         A.swap(Ac);
         fixed_f.assign(n, 0);
@@ -355,6 +374,9 @@ void Sim::setup_solver()
             cache[key] = inv;
         }
         if (!inv.empty()) lv.coarse_inv.upload(inv.data(), inv.size(), stream);
+        std::vector<double> inv64;
+        if (mg_fp64 && dense_inverse64(lnx.back(), lnz.back(), A, inv64))
+            lv.coarse_inv64.upload(inv64.data(), inv64.size(), stream);
     }
     std::vector<double> st;
     fine_stencil_table(coord, nx, dx, dz, st, lv.k2);
@@ -525,6 +547,23 @@ void Sim::smooth_u()
 void Sim::run_solve(SolveArgs a)
 {
     u_partial = false;  // every path below writes u (a partial direct solve sets it again)
+    if (mg_fp64) {
+        MG64Args g{};
+        for (int l = 0; l < lv.nlev; ++l) {
+            g.lev[l].nx = lv.nx[l];
+            g.lev[l].nz = lv.nz[l];
+            g.lev[l].cmode = lv.cmode[l];
+            g.lev[l].e = lv.e64[l].p;
+            g.lev[l].r = lv.r64[l].p;
+            g.lev[l].t = lv.t64[l].p;
+            g.lev[l].coef = l > 0 ? lv.coef64[l].p : nullptr;
+            g.lev[l].inv_diag = l > 0 ? lv.inv_diag64[l].p : nullptr;
+        }
+        g.coarse_inv = lv.coarse_inv64.p;
+        launches += launch_solve64(a, g, stream);
+        MAG_CK(cudaGetLastError());
+        return;
+    }
     if (a.rho_src != 3 && direct_mode >= 0 && p.selfconsistent && !a.rf_solve) {
         if (!green_tried) build_green();
         if (green_ready()) {

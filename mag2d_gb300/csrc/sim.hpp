@@ -77,6 +77,7 @@ struct SimOptions {
     int push_vec = 0;       // slots per thread of the particle kernel: 1, 2 or 4 (0: by particle count)
     int direct_solve = 0;   // Poisson by the precomputed inverse: 0 automatic (small grids), 1 forced, -1 never
     int max_fused_steps = 0;  // steps per fused particle launch where particles are independent (0: 64, 1: none)
+    int multigrid_fp64 = 0;   // 1: every multigrid level in FP64 (one-block grids only)
     cudaStream_t stream = nullptr;  // work on this stream instead of one of its own (not destroyed)
 };
 
@@ -133,6 +134,9 @@ struct SolverLevels {
     std::vector<int> ti, tj;     // tile interiors per level (empty: not yet chosen)
     size_t tile_smem = 0;        // dynamic shared memory of the launch (0: tile phases off)
     bool coarse_staged = false;  // block 0's levels fit the dynamic shared memory
+    // the all-FP64 multigrid (SimOptions::multigrid_fp64): the same levels in FP64
+    std::vector<DevArray<double>> e64, r64, t64, coef64, inv_diag64;
+    DevArray<double> coarse_inv64;
 };
 
 void build_species(const std::vector<SpeciesParams>& species_prm, std::vector<InteractionParams>& inters,
@@ -186,6 +190,7 @@ public:
     bool multicoll = false;  // mover ADVANCE_MULTICOLL
     int solve_blocks = 0;  // blocks of a cooperative solve (0: not yet chosen)
     int direct_mode = 0;   // SimOptions::direct_solve
+    bool mg_fp64 = false;  // SimOptions::multigrid_fp64
     int max_fused = kMaxFusedSteps;  // SimOptions::max_fused_steps
     DevArray<double> stage64;  // host particle arrays on their way to the SoA state
     // the inverse of the Poisson operator for direct solves (built at the first self-consistent solve)

@@ -206,10 +206,11 @@ class Pic:
 
     def __init__(self, config, species_conf, initscript=None, *, seed: int = 1, device: int = 0,
                  poisson_tol: float = 0.0, poisson_max_iter: int = 0, capacity_hint: int = 0,
-                 sort_interval: int = 0, push_vec: int = 0, direct_solve: int = 0, max_fused_steps: int = 0):
+                 sort_interval: int = 0, push_vec: int = 0, direct_solve: int = 0, max_fused_steps: int = 0,
+                 multigrid_fp64: int = 0):
         opts = MagOpts(device=device, seed=seed, sort_interval=sort_interval, poisson_tol=poisson_tol,
                        poisson_max_iter=poisson_max_iter, capacity_hint=capacity_hint, push_vec=push_vec,
-                       direct_solve=direct_solve, max_fused_steps=max_fused_steps)
+                       direct_solve=direct_solve, max_fused_steps=max_fused_steps, multigrid_fp64=multigrid_fp64)
         h = ctypes.c_void_p()
         ini = str(initscript).encode() if initscript else None
         check(lib().mag_create(str(config).encode(), str(species_conf).encode(), ini, ctypes.byref(opts),

@@ -54,18 +54,21 @@ def _match(g, o):
     dict(coord="CARTESIAN", geometry="PROBE", x_max=2e-2, z_max=2e-2, x_sampl=65, z_sampl=65, probe_radius=1e-3),
     dict(coord="CARTESIAN", geometry="EMPTY", x_max=2e-2, z_max=2e-2, x_sampl=50, z_sampl=50, extern_field=300.0),
 ], ids=["penning_endcap", "penning_simple", "penning", "rf22pt", "probe", "empty_sor"])
-@pytest.mark.parametrize("direct", [-1, 1], ids=["multigrid", "inverse"])
+@pytest.mark.parametrize("direct", [-1, 1, "fp64"], ids=["multigrid", "inverse", "multigrid_fp64"])
 def test_poisson_matches_direct_solve(m, tmp_path, geom, direct):
-    """Both solvers of a small grid: the multigrid solve and the product with
-    the precomputed inverse of the operator (whose columns are multigrid
-    solves of unit right-hand sides)."""
+    """The three solvers of a small grid: the FP32 multigrid with FP64
+    refinement, the product with the precomputed inverse of the operator
+    (whose columns are multigrid solves of unit right-hand sides) and the
+    all-FP64 multigrid."""
     from mag2d_cases import QE, write_config, write_species_conf
 
     cfg = dict(selfconsistent=1, rf=0, do_plot=0, macroparticle_factor=100.0, **geom)
     species = [dict(name="E", type="ELECTRON", mass=9.11e-31, charge=-QE, dt=1e-11, temperature=1e4, density=1e13)]
     cpath = write_config(cfg, tmp_path / "c.txt")
     spath = write_species_conf(species, [], tmp_path / "s.txt")
-    pic = m.Pic(cpath, spath, seed=1, direct_solve=direct)
+    fp64 = direct == "fp64"
+    direct = -1 if fp64 else direct
+    pic = m.Pic(cpath, spath, seed=1, direct_solve=direct, multigrid_fp64=int(fp64))
     port = _port_for(m, cfg, species, [], cpath)
     rng = np.random.default_rng(5)
     nx, nz = pic.shape
