@@ -387,6 +387,8 @@ struct SolveArgs {
     int tiled;              // multi-block solves: levels above l_single run as tile phases (dynamic shared memory)
     int coarse_staged;      // tiled solves: block 0 runs the levels from l_single down in shared memory
     const float* coarse_inv;  // dense inverse of the coarsest level, column-major (null: smooth it)
+    const float* coarse_inv_rows;  // multi-block solves: the same inverse row-major, applied by every block
+    int coarse_grid;          // 1: the coarsest level is l_single and all blocks solve it with coarse_inv_rows
     MGLevelDev lev[kMaxLevels];
     int nu1, nu2, ncoarse;
     float omega;            // SOR factor for the one-level smoother

@@ -109,13 +109,13 @@ void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector
 }
 
 void multigrid_levels(int nx, int nz, double couple_ratio, int max_levels, std::vector<int>& lnx, std::vector<int>& lnz,
-                      std::vector<int>& lmode)
+                      std::vector<int>& lmode, long long coarse_max)
 {
     lnx.assign(1, nx);
     lnz.assign(1, nz);
     lmode.assign(1, kCoarsenFull);
     double ratio = couple_ratio;  // x couplings / z couplings of the current level
-    while ((int)lnx.size() < max_levels && (long long)lnx.back() * lnz.back() > kDenseCoarseMax) {
+    while ((int)lnx.size() < max_levels && (long long)lnx.back() * lnz.back() > coarse_max) {
         const int x = lnx.back(), z = lnz.back();
         const bool cx = (x - 1) % 2 == 0 && x >= 5, cz = (z - 1) % 2 == 0 && z >= 5;
         int mode;

@@ -30,16 +30,19 @@ constexpr double kSemiCoarsenRatio = 2.5;
 void galerkin(int nxf, int nzf, const std::vector<double>& Af, const std::vector<char>& fixed_f, int mode, int& nxc,
               int& nzc, std::vector<double>& Ac);
 
-// Coarsest levels up to this many nodes are solved exactly with a dense inverse.
+// Coarsest levels up to this many nodes are solved exactly with a dense inverse
+// (one block applies it); multi-block solves stop coarsening at this larger
+// size and apply the inverse with every block, one warp per row.
 constexpr long long kDenseCoarseMax = 200;
+constexpr long long kDenseCoarseGridMax = 1280;
 
 // Level sizes: halve while the sizes are odd and >= 5 (at most max_levels
-// levels), and stop at the first level of at most kDenseCoarseMax nodes.
+// levels), and stop at the first level of at most coarse_max nodes.
 // couple_ratio = x couplings / z couplings of the fine operator ((dz/dx)^2 for
 // the cylindrical one, 1 for the reference's Cartesian one); lmode[l] says how
 // level l - 1 was coarsened to level l (lmode[0] unused).
 void multigrid_levels(int nx, int nz, double couple_ratio, int max_levels, std::vector<int>& lnx, std::vector<int>& lnz,
-                      std::vector<int>& lmode);
+                      std::vector<int>& lmode, long long coarse_max = kDenseCoarseMax);
 
 // Per-row coefficients (w, e, c, 1/c) of the fine 5-point stencil, FP64,
 // 4 * nx values, and the common s/n coefficient k2 (src/fields.cpp:149-238);

@@ -454,6 +454,28 @@ __device__ void coarse_solve(const SolveArgs& a, Team& t, bool& ok)
     ok = t.sync();
 }
 
+// Coarsest level of a multi-block solve (a.coarse_grid): e = A^-1 r with the
+// row-major dense inverse, one warp per row over all blocks; each lane sums a
+// fixed set of columns and the warp adds them in a fixed tree, so the result
+// does not depend on the launch shape.
+__device__ void coarse_solve_grid(const SolveArgs& a, Team& t, bool& ok)
+{
+    const MGLevelDev& L = a.lev[a.nlev - 1];
+    const unsigned n = (unsigned)(L.nx * L.nz);
+    const unsigned lane = threadIdx.x & 31u, nwarps = t.nthreads >> 5;
+    const float* __restrict__ r = L.r;
+    for (unsigned row = t.tid >> 5; row < n; row += nwarps) {
+        const float* __restrict__ g = a.coarse_inv_rows + (size_t)row * n;
+        float acc = 0.f;
+#pragma unroll 8
+        for (unsigned c = lane; c < n; c += 32) acc += __ldg(&g[c]) * r[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) L.e[row] = acc;
+    }
+    ok = t.sync();
+}
+
 // The part of a V-cycle from level l0 down to the coarsest level and back up
 // to l0, pre- and post-smoothing on l0 included.
 __device__ void vcycle_from(const SolveArgs& a, Team& t, int l0, bool& ok)
@@ -514,13 +536,17 @@ __device__ void vcycle(const SolveArgs& a, Team& t, bool& ok)
         t.mark(kPhaseDown + l);
     }
     if (!ok) return;
-    if (blockIdx.x == 0) {
-        Team tb = Team::block(a.bar);
-        bool okb = true;
-        vcycle_from(a, tb, ls, okb);
-        __threadfence();
+    if (a.coarse_grid) {
+        coarse_solve_grid(a, t, ok);
+    } else {
+        if (blockIdx.x == 0) {
+            Team tb = Team::block(a.bar);
+            bool okb = true;
+            vcycle_from(a, tb, ls, okb);
+            __threadfence();
+        }
+        ok = t.sync();
     }
-    ok = t.sync();
     t.mark(kPhaseCoarse);
     for (int l = ls - 1; l >= 0 && ok; --l) {
         prolong_level(a, t, l);
@@ -880,12 +906,16 @@ __device__ void vcycle_tiled(const SolveArgs& a, Team& t, bool& ok)
         t.mark(kPhaseDown + l);
     }
     if (!ok) return;
-    if (blockIdx.x == 0) {
-        bool okb = true;
-        coarse_part(a, okb);
-        __threadfence();
+    if (a.coarse_grid) {
+        coarse_solve_grid(a, t, ok);
+    } else {
+        if (blockIdx.x == 0) {
+            bool okb = true;
+            coarse_part(a, okb);
+            __threadfence();
+        }
+        ok = t.sync();
     }
-    ok = t.sync();
     t.mark(kPhaseCoarse);
     for (int l = ls - 1; l >= 0 && ok; --l) {
         tile_up(a, l);

@@ -299,7 +299,10 @@ void Sim::setup_solver()
     const int coord = p.coord == CYLINDRICAL ? 1 : 0;
     std::vector<int> lnx, lnz, lmode;
     // couplings of the fine operator: r ones ~ 1/dx^2, z ones 1/dz^2 (cylindrical); unit in Cartesian runs
-    multigrid_levels(nx, nz, coord == 1 ? (dz * dz) / (dx * dx) : 1.0, kMaxLevels, lnx, lnz, lmode);
+    // grids solved by all blocks stop at a larger coarsest level, which every block helps to solve
+    const bool multi_block = (long long)nx * nz > kSingleBlockNodes;
+    multigrid_levels(nx, nz, coord == 1 ? (dz * dz) / (dx * dx) : 1.0, kMaxLevels, lnx, lnz, lmode,
+                     multi_block ? kDenseCoarseGridMax : kDenseCoarseMax);
     lv.nlev = (int)lnx.size();
     lv.nx = lnx;
     lv.nz = lnz;
@@ -353,7 +356,8 @@ void Sim::setup_solver()
     // inverse depends only on the operator, so instances that share grid and
     // geometry (batched sweeps) compute it once per process
     lv.coarse_inv.release();
-    if (lv.nlev > 1 && (long long)lnx.back() * lnz.back() <= kDenseCoarseMax) {
+    lv.coarse_inv_rows.release();
+    if (lv.nlev > 1 && (long long)lnx.back() * lnz.back() <= (multi_block ? kDenseCoarseGridMax : kDenseCoarseMax)) {
         static std::mutex mu;
         static std::map<std::string, std::vector<float>> cache;
         std::string key((const char*)A.data(), A.size() * sizeof(double));
@@ -374,6 +378,14 @@ void Sim::setup_solver()
             cache[key] = inv;
         }
         if (!inv.empty()) lv.coarse_inv.upload(inv.data(), inv.size(), stream);
+        if (!inv.empty() && multi_block) {
+            const size_t n = (size_t)lnx.back() * lnz.back();
+            std::vector<float> rows(n * n);
+            for (size_t r = 0; r < n; ++r)
+                for (size_t c = 0; c < n; ++c) rows[r * n + c] = inv[c * n + r];
+            lv.coarse_inv_rows.upload(rows.data(), rows.size(), stream);
+            MAG_CK(cudaStreamSynchronize(stream));
+        }
         std::vector<double> inv64;
         if (mg_fp64 && dense_inverse64(lnx.back(), lnz.back(), A, inv64))
             lv.coarse_inv64.upload(inv64.data(), inv64.size(), stream);
@@ -624,6 +636,7 @@ void Sim::run_solve(SolveArgs a)
         nblocks = std::max(1, solve_blocks);
         if (nblocks > 1) {
             a.l_single = ls;
+            a.coarse_grid = ls == lv.nlev - 1 && lv.coarse_inv_rows.p ? 1 : 0;
             if (lv.tile_smem) {
                 a.tiled = 1;
                 a.coarse_staged = lv.coarse_staged ? 1 : 0;
@@ -673,6 +686,8 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
     a.st32 = lv.st32.p;
     a.k2 = lv.k2;
     a.coarse_inv = lv.coarse_inv.p;
+    a.coarse_inv_rows = lv.coarse_inv_rows.p;
+    a.coarse_grid = 0;
     a.nlev = lv.nlev;
     for (int l = 0; l < lv.nlev; ++l) {
         a.lev[l].nx = lv.nx[l];

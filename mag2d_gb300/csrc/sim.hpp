@@ -126,6 +126,7 @@ struct SolverLevels {
     std::vector<int> cmode;      // how level l is coarsened to level l + 1 (kCoarsen*)
     std::vector<DevArray<float>> e, r, t, coef, inv_diag;
     DevArray<float> coarse_inv;  // dense inverse of the coarsest level (column-major) or empty
+    DevArray<float> coarse_inv_rows;  // multi-block grids: the same inverse row-major
     DevArray<double> st64;       // fine stencil rows (w, e, c)
     DevArray<double> rscale;     // right-hand-side scaling of rho per row
     DevArray<float> st32;
