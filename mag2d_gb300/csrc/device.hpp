@@ -396,7 +396,7 @@ struct SolveArgs {
     int max_outer;
     float* Exf;             // faces of -grad u (may be null)
     float* Ezf;
-    double* red;            // reduction scratch (4 doubles)
+    double* red;            // reduction scratch (8 doubles: FP64 residual passes, then updated residuals)
     GridBarrier* bar;
     SolveStatus* status;
     int* err;

@@ -158,7 +158,7 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
         off = align256(off + bytes);
         return o;
     };
-    const size_t o_mask = take(nn), o_volt = take(nn * 8), o_b = take(nn * 8), o_red = take(4 * 8),
+    const size_t o_mask = take(nn), o_volt = take(nn * 8), o_b = take(nn * 8), o_red = take(8 * 8),
                  o_status = take(sizeof(SolveStatus)), o_bar = take(sizeof(GridBarrier)), o_err = take(sizeof(int));
     std::vector<size_t> o_e(nlev), o_r(nlev), o_t(nlev), o_c(nlev), o_d(nlev);
     for (int l = 0; l < nlev; ++l) {
@@ -204,7 +204,7 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
     if (!cinv.empty())
         ck(cudaMemcpyAsync(base + o_cinv, cinv.data(), cinv.size() * 4, cudaMemcpyHostToDevice, s), "inverse copy");
     // state left by the previous call that must start at zero
-    ck(cudaMemsetAsync(base + o_red, 0, 4 * 8, s), "clear");
+    ck(cudaMemsetAsync(base + o_red, 0, 8 * 8, s), "clear");
     ck(cudaMemsetAsync(base + o_status, 0, sizeof(SolveStatus), s), "clear");
     ck(cudaMemsetAsync(base + o_bar, 0, sizeof(GridBarrier), s), "clear");
     ck(cudaMemsetAsync(base + o_err, 0, sizeof(int), s), "clear");

@@ -787,7 +787,15 @@ __device__ void tile_down(const SolveArgs& a, int l)
 // post-smoothed tile to L.t, so that no block reads what another one writes
 // in the same phase; level l - 1 prolongs from L.t (level l_single's
 // correction, computed by block 0, stays in its e).
-__device__ void tile_up(const SolveArgs& a, int l)
+//
+// res_slot >= 0 (fine level): the phase also writes the next residual
+// r - A e of its tile interior into L.r, in FP32 from the FP32 correction, and
+// adds the block's max |r / c| and max |u| into a.red[res_slot], [res_slot + 1].
+// The residual that r approximates changes by exactly -A e in the iteration,
+// so the difference to the FP64 residual b - A u grows only by the rounding of
+// each update, about 2^-24 of that iteration's residual: a few 1e-13 of max|u|
+// after the whole solve.
+__device__ void tile_up(const SolveArgs& a, int l, int res_slot)
 {
     const MGLevelDev& L = a.lev[l];
     const MGLevelDev& C = a.lev[l + 1];
@@ -815,12 +823,38 @@ __device__ void tile_up(const SolveArgs& a, int l)
                 tile_pass(a, l, T, S, c, kTileHalo - 1 - pass);
                 __syncthreads();
             }
+        float lres = 0.f;
+        unsigned lumax_hi = 0u;
         for (int q = threadIdx.x; q < T.ni * T.nj; q += blockDim.x) {
             const int ii = q / T.nj, jj = q - ii * T.nj;
             const int p = (ii + kTileHalo) * T.rw + jj + kTileHalo;
             const size_t k = (size_t)(T.i0 + ii) * L.nz + T.j0 + jj;
-            if (l > 0) L.t[k] = S.e[p];
-            else if (!S.f[p]) a.u[k] += (double)S.e[p];
+            if (l > 0) {
+                L.t[k] = S.e[p];
+            } else if (!S.f[p]) {
+                const double un = a.u[k] + (double)S.e[p];
+                a.u[k] = un;
+                if (res_slot >= 0) {
+                    // every neighbour of an interior node holds its final value after the last pass
+                    const int i = T.i0 + ii;
+                    const float* st = a.st32 + 4 * i;
+                    const float k2 = (float)a.k2;
+                    float acc = S.r[p] - st[2] * S.e[p] - st[1] * S.e[p + T.rw] - k2 * (S.e[p - 1] + S.e[p + 1]);
+                    if (i > 0) acc -= st[0] * S.e[p - T.rw];
+                    L.r[k] = acc;
+                    lres = fmaxf(lres, fabsf(acc * st[3]));
+                    lumax_hi = max(lumax_hi, (unsigned)__double2hiint(un) & 0x7FFFFFFFu);
+                }
+            } else if (res_slot >= 0) {
+                lumax_hi = max(lumax_hi, (unsigned)__double2hiint(a.u[k]) & 0x7FFFFFFFu);
+            }
+        }
+        if (res_slot >= 0) {
+            const double br = block_max((double)lres), bu = block_max(__hiloint2double((int)lumax_hi, 0));
+            if (threadIdx.x == 0) {
+                atomic_max_nonneg(&a.red[res_slot], br);
+                atomic_max_nonneg(&a.red[res_slot + 1], bu);
+            }
         }
         __syncthreads();
     }
@@ -896,8 +930,8 @@ __device__ void coarse_part(const SolveArgs& a, bool& okb)
 
 // One V-cycle of a multi-block solve with tile phases on the levels above
 // l_single and block 0 alone below; ends with u += e (done by the fine level's
-// up phase).
-__device__ void vcycle_tiled(const SolveArgs& a, Team& t, bool& ok)
+// up phase, which also leaves the next residual in the fine r when res_slot >= 0).
+__device__ void vcycle_tiled(const SolveArgs& a, Team& t, bool& ok, int res_slot)
 {
     const int ls = a.l_single;
     for (int l = 0; l < ls && ok; ++l) {
@@ -918,7 +952,7 @@ __device__ void vcycle_tiled(const SolveArgs& a, Team& t, bool& ok)
     }
     t.mark(kPhaseCoarse);
     for (int l = ls - 1; l >= 0 && ok; --l) {
-        tile_up(a, l);
+        tile_up(a, l, l == 0 ? res_slot : -1);
         ok = t.sync();
         t.mark(kPhaseUp + l);
     }
@@ -997,52 +1031,71 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
     const double* __restrict__ bb = a.b;
     const int8_t* __restrict__ mask = a.mask;
     const float* __restrict__ st32 = a.st32;
+    // A multi-block tiled solve takes the residual of each V-cycle from the
+    // cycle's fine up phase (tile_up) and computes it in FP64 only at the start
+    // and to confirm convergence; the other paths compute it in FP64 every time.
+    const bool tiled = a.tiled && t.nblocks > 1;
+    int cycles = 0, n64 = 0;
+    bool updated = false;  // this pass's residual was left by the last fine up phase
     for (; ok; ++it) {
-        // residual in FP64; its Jacobi-scaled max norm and max|u| only steer
-        // the stopping test and are taken in FP32
-        // max|u| from the high words of the doubles (sign cleared): integer
-        // compares, no FP64 conversion; 20 mantissa bits are plenty for the
-        // stopping test, and the truncation only makes the test stricter
-        float lres32 = 0.f;
-        unsigned lumax_hi = 0u;
-        const bool zero_e = !(a.tiled && t.nblocks > 1);  // the tile phases start from e = 0 in shared memory
-#pragma unroll 2
-        for (unsigned k = t.tid; k < nn; k += t.nthreads) {
-            const int i = (int)dnz.div(k);
-            const double uk = uin[k];
-            lumax_hi = max(lumax_hi, (unsigned)__double2hiint(uk) & 0x7FFFFFFFu);
-            if (zero_e) F.e[k] = 0.f;
-            if (is_fixed(mask[k])) {
-                F.r[k] = 0.f;
-                continue;
-            }
-            const Stencil5 st = fine_stencil(a, i);
-            double acc = st.c * uk;
-            if (i > 0) acc += st.w * uin[k - nz];
-            acc += st.e * uin[k + nz];
-            acc += st.s * uin[k - 1];
-            acc += st.n * uin[k + 1];
-            const float rf = (float)(bb[k] - acc);
-            F.r[k] = rf;
-            lres32 = fmaxf(lres32, fabsf(rf * st32[4 * i + 3]));
-        }
-        double lres = lres32, lumax = __hiloint2double((int)lumax_hi, 0);
-        lres = block_max(lres);
-        lumax = block_max(lumax);
-        if (t.nblocks > 1) {
-            const int slot = (it & 1) * 2;
-            if (threadIdx.x == 0) {
-                atomic_max_nonneg(&a.red[slot], lres);
-                atomic_max_nonneg(&a.red[slot + 1], lumax);
-            }
-            ok = t.sync();
-            if (!ok) break;
+        double lres, lumax;
+        if (updated) {
+            const int slot = 4 + ((cycles - 1) & 1) * 2;
             lres = *((volatile double*)&a.red[slot]);
             lumax = *((volatile double*)&a.red[slot + 1]);
-            if (t.tid == 0) {
-                a.red[2 - slot] = 0.0;
-                a.red[3 - slot] = 0.0;
+            if (t.tid == 0) {  // clear the next cycle's slots (last read right after the cycle before this one)
+                a.red[10 - slot] = 0.0;
+                a.red[11 - slot] = 0.0;
             }
+        } else {
+            // residual in FP64; its Jacobi-scaled max norm and max|u| only steer
+            // the stopping test and are taken in FP32
+            // max|u| from the high words of the doubles (sign cleared): integer
+            // compares, no FP64 conversion; 20 mantissa bits are plenty for the
+            // stopping test, and the truncation only makes the test stricter
+            float lres32 = 0.f;
+            unsigned lumax_hi = 0u;
+            const bool zero_e = !tiled;  // the tile phases start from e = 0 in shared memory
+#pragma unroll 2
+            for (unsigned k = t.tid; k < nn; k += t.nthreads) {
+                const int i = (int)dnz.div(k);
+                const double uk = uin[k];
+                lumax_hi = max(lumax_hi, (unsigned)__double2hiint(uk) & 0x7FFFFFFFu);
+                if (zero_e) F.e[k] = 0.f;
+                if (is_fixed(mask[k])) {
+                    F.r[k] = 0.f;
+                    continue;
+                }
+                const Stencil5 st = fine_stencil(a, i);
+                double acc = st.c * uk;
+                if (i > 0) acc += st.w * uin[k - nz];
+                acc += st.e * uin[k + nz];
+                acc += st.s * uin[k - 1];
+                acc += st.n * uin[k + 1];
+                const float rf = (float)(bb[k] - acc);
+                F.r[k] = rf;
+                lres32 = fmaxf(lres32, fabsf(rf * st32[4 * i + 3]));
+            }
+            lres = lres32;
+            lumax = __hiloint2double((int)lumax_hi, 0);
+            lres = block_max(lres);
+            lumax = block_max(lumax);
+            if (t.nblocks > 1) {
+                const int slot = (n64 & 1) * 2;
+                if (threadIdx.x == 0) {
+                    atomic_max_nonneg(&a.red[slot], lres);
+                    atomic_max_nonneg(&a.red[slot + 1], lumax);
+                }
+                ok = t.sync();
+                if (!ok) break;
+                lres = *((volatile double*)&a.red[slot]);
+                lumax = *((volatile double*)&a.red[slot + 1]);
+                if (t.tid == 0) {
+                    a.red[2 - slot] = 0.0;
+                    a.red[3 - slot] = 0.0;
+                }
+            }
+            ++n64;
         }
         t.mark(kPhaseResidual);
         // relative to max|u|; a cold start from u = 0 (a homogeneous solve)
@@ -1051,14 +1104,21 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
         const double uref = lumax > 0.0 ? lumax : ref0;
         res = uref > 0.0 ? lres / uref : lres;
         if (res <= a.tol || lres == 0.0) {
-            conv = true;
-            break;
+            if (!updated) {
+                conv = true;
+                break;
+            }
+            updated = false;  // confirm with the FP64 residual
+            continue;
         }
-        if (it >= a.max_outer) break;
-        if (a.tiled && t.nblocks > 1) {
-            // the barrier of the reduction above already ordered F.r; the fine
-            // level's up phase adds the correction to u
-            vcycle_tiled(a, t, ok);
+        if (cycles >= a.max_outer) break;
+        if (tiled) {
+            // the barrier of the reduction above (or of the last up phase)
+            // already ordered F.r; the fine level's up phase adds the
+            // correction to u and leaves the next residual
+            vcycle_tiled(a, t, ok, 4 + (cycles & 1) * 2);
+            ++cycles;
+            updated = true;
             continue;
         }
         ok = t.sync();
@@ -1068,13 +1128,14 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
         for (unsigned k = t.tid; k < nn; k += t.nthreads)
             if (!is_fixed(a.mask[k])) a.u[k] += (double)F.e[k];
         ok = t.sync();
+        ++cycles;
         t.mark(kPhaseUp);
     }
     // 3. face electric field E = -grad u for the particle kernel
     if (ok && a.Exf != nullptr) faces_pass(a.u, nx, nz, a.idx, a.idz, a.Exf, a.Ezf, t.tid, t.nthreads);
     t.mark(kPhaseFaces);
     if (a.prof && blockIdx.x == 0 && threadIdx.x == 0) a.prof[kPhaseTotal] += (double)(Team::now() - t_start);
-    solve_report(a, t, it, res, conv, ok);
+    solve_report(a, t, cycles, res, conv, ok);
 }
 
 __global__ void __launch_bounds__(1024) k_solve(const __grid_constant__ SolveArgs a)

@@ -108,7 +108,7 @@ Sim::Sim(const std::string& config, const std::string& species_conf, const SimOp
     d_status.zero(stream);
     d_bar.alloc(1);
     d_bar.zero(stream);
-    red.alloc(4);
+    red.alloc(8);
     red.zero(stream);
     setup_fields();
     setup_species();
@@ -646,7 +646,7 @@ void Sim::run_solve(SolveArgs a)
                 }
             }
             MAG_CK(cudaMemsetAsync(d_bar.p, 0, sizeof(GridBarrier), stream));
-            MAG_CK(cudaMemsetAsync(red.p, 0, 4 * sizeof(double), stream));
+            MAG_CK(cudaMemsetAsync(red.p, 0, 8 * sizeof(double), stream));
         }
     }
     if (a.prof) MAG_CK(cudaMemsetAsync(a.prof, 0, kSolvePhases * sizeof(double), stream));
