@@ -963,20 +963,14 @@ __device__ void solve_prologue(const SolveArgs& a, Team& t, bool& ok)
 {
     const int nx = a.nx, nz = a.nz;
     const unsigned nn = (unsigned)(nx * nz);
-    // 0. start of a step's solve: the linear extrapolation of the last two solutions
-    if (a.u_prev) {
-        const bool valid = *((volatile const int*)a.u_prev_valid) != 0;
-        for (unsigned k = t.tid; k < nn; k += t.nthreads) {
-            if (is_fixed(a.mask[k])) continue;
-            const double u = a.u[k];
-            if (valid) a.u[k] = 2.0 * u - a.u_prev[k];
-            a.u_prev[k] = u;
-        }
-        ok = t.sync();
-        if (t.tid == 0) *a.u_prev_valid = 1;
-    }
-    // 1. right-hand side and Dirichlet values (boundary_solve / boundary_solve_rf)
+    // 0. start of a step's solve: the linear extrapolation of the last two
+    //    solutions on the free nodes (u_prev <- u), and
+    // 1. right-hand side and Dirichlet values (boundary_solve / boundary_solve_rf),
+    // one pass: both are per node
+    const bool extrap = a.u_prev != nullptr;
+    const bool valid = extrap && *((volatile const int*)a.u_prev_valid) != 0;
     const FastDiv dnz((unsigned)nz);
+#pragma unroll 2
     for (unsigned k = t.tid; k < nn; k += t.nthreads) {
         const int i = (int)dnz.div(k);
         const int8_t m = a.mask[k];
@@ -985,6 +979,11 @@ __device__ void solve_prologue(const SolveArgs& a, Team& t, bool& ok)
             a.u[k] = v;
             a.b[k] = v;
         } else {
+            if (extrap) {
+                const double u = a.u[k];
+                if (valid) a.u[k] = 2.0 * u - a.u_prev[k];
+                a.u_prev[k] = u;
+            }
             double rho = 0.0;
             if (a.rho_src == 1) {
                 for (int s = 0; s < a.nsp; ++s) rho += a.rho_weight[s] * (double)a.rho_fixed[s][k];
@@ -997,6 +996,7 @@ __device__ void solve_prologue(const SolveArgs& a, Team& t, bool& ok)
             for (int s = 0; s < a.nsp; ++s) ((unsigned long long*)a.rho_fixed[s])[k] = 0ull;
     }
     ok = t.sync();
+    if (extrap && t.tid == 0) *a.u_prev_valid = 1;  // every block read the flag before the barrier
 }
 
 // the solve's status words (thread 0 of the team)
