@@ -143,6 +143,11 @@ int mag_species(mag_sim* sim, int species, mag_species_info* out);
 int mag_get_field(mag_sim* sim, int which, double* host_out);
 /* Overwrite u, uRF or rho from host doubles (e.g. for a solve of a given rho). */
 int mag_set_field(mag_sim* sim, int which, const double* host_in);
+/* Copy the face field E = -grad u that the particle kernel reads (Field2D::grad,
+ * src/Field2D.hpp, staggered differences; FP32 [V/m]): component 0 = Ex on
+ * (x_sampl+1)*z_sampl faces, 1 = Ez on x_sampl*(z_sampl+1) faces, row-major.
+ * After u is set by hand (mag_set_field) the faces follow at the next solve. */
+int mag_get_face_field(mag_sim* sim, int component, float* host_out);
 
 /* Fields::boundary_solve (src/fields.cpp:278-312): solve for u from the current
  * rho (MAG_RHO) exactly as a self-consistent step does. */

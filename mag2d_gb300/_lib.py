@@ -156,6 +156,7 @@ def lib() -> ctypes.CDLL:
     L.mag_n_species.argtypes = [P]
     L.mag_species.argtypes = [P, ctypes.c_int, ctypes.POINTER(MagSpeciesInfo)]
     L.mag_get_field.argtypes = [P, ctypes.c_int, D]
+    L.mag_get_face_field.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     L.mag_set_field.argtypes = [P, ctypes.c_int, D]
     L.mag_field_solve.argtypes = [P, ctypes.POINTER(MagSolveInfo)]
     L.mag_get_particles.argtypes = [P, ctypes.c_int, ctypes.c_int64, D, D, D, D, D,

@@ -233,6 +233,16 @@ int mag_get_field(mag_sim* sim, int which, double* host_out)
     });
 }
 
+int mag_get_face_field(mag_sim* sim, int component, float* host_out)
+{
+    return guarded([&]() {
+        check_species(sim, 0);
+        if (!host_out || (component != 0 && component != 1)) throw mag::Error(MAG_EINVAL, "face field: component 0 or 1");
+        sim->s->get_faces(component, host_out);
+        return MAG_OK;
+    });
+}
+
 int mag_set_field(mag_sim* sim, int which, const double* host_in)
 {
     return guarded([&]() {

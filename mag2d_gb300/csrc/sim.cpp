@@ -1357,6 +1357,14 @@ SolveStatus Sim::field_solve()
     return solve(false, rho_override ? 2 : 1, false, true);
 }
 
+void Sim::get_faces(int component, float* out)
+{
+    ensure_full_u();
+    const size_t n = component == 0 ? (size_t)(nx + 1) * nz : (size_t)nx * (nz + 1);
+    MAG_CK(cudaStreamSynchronize(stream));
+    MAG_CK(cudaMemcpy(out, component == 0 ? Exf.p : Ezf.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+}
+
 void Sim::get_field(int which, double* out)
 {
     const size_t nn = (size_t)nx * nz;

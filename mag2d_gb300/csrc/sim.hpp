@@ -236,6 +236,8 @@ public:
     bool sort_due = true;
 
     void get_field(int which, double* out);
+
+    void get_faces(int component, float* out);  // Exf (0) or Ezf (1)
     void set_field(int which, const double* in);
     SolveStatus field_solve();
     void get_particles(int s, int64_t cap, double* x, double* z, double* vx, double* vy, double* vz, uint32_t* id,

@@ -62,6 +62,17 @@ class Fields:
     def voltage(self) -> np.ndarray:
         return self._get(MAG_VOLTAGE)
 
+    @property
+    def faces(self) -> tuple[np.ndarray, np.ndarray]:
+        """The FP32 face field the particle kernel reads: Ex ((nx+1, nz)) and Ez ((nx, nz+1))."""
+        nx, nz = self._pic.shape
+        ex = np.zeros((nx + 1, nz), dtype=np.float32)
+        ez = np.zeros((nx, nz + 1), dtype=np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        check(lib().mag_get_face_field(self._pic.h, 0, ex.ctypes.data_as(fp)))
+        check(lib().mag_get_face_field(self._pic.h, 1, ez.ctypes.data_as(fp)))
+        return ex, ez
+
     def set_rho(self, rho: np.ndarray) -> None:
         rho = np.ascontiguousarray(rho, dtype=np.float64)
         check(lib().mag_set_field(self._pic.h, MAG_RHO, _dp(rho)))

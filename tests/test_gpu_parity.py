@@ -107,6 +107,14 @@ def test_inverse_solve_matches_multigrid_in_a_run(m, tmp_path):
     assert np.array_equal(us["inv"], us["inv2"])
 
 
+def _faces_of(u, dx, dz):
+    """Field2D::grad's staggered faces of u with the end faces repeated, FP32 (faces_pass)."""
+    dx_, dz_ = -(u[1:] - u[:-1]) * (1.0 / dx), -(u[:, 1:] - u[:, :-1]) * (1.0 / dz)
+    ex = np.concatenate([dx_[:1], dx_, dx_[-1:]], axis=0).astype(np.float32)
+    ez = np.concatenate([dz_[:, :1], dz_, dz_[:, -1:]], axis=1).astype(np.float32)
+    return ex, ez
+
+
 def _direct_solve(A, b):
     spl = pytest.importorskip("scipy.sparse.linalg")
     lu = spl.splu(A.tocsc())
@@ -142,6 +150,10 @@ def test_poisson_multiblock_matches_direct_solve(m, tmp_path):
         err = np.abs(u_gpu - u_ref).max() / np.abs(u_ref).max()
         assert info["status"] == 0 and info["levels"] > 3, info
         assert err <= 1e-9, (trial, err, info)
+        # the face field the particles read, written by the pass that confirms convergence
+        ex, ez = pic.field.faces
+        fx, fz = _faces_of(u_gpu, pic.dx, pic.dz)
+        assert np.array_equal(ex, fx) and np.array_equal(ez, fz)
     pic.close()
 
 
@@ -166,6 +178,9 @@ def test_poisson_large_grid_residual(m, tmp_path):
     res = np.abs(r / A.diagonal()).max() / np.abs(u).max()
     assert info["status"] == 0, info
     assert res <= 1e-10, (res, info)
+    ex, ez = pic.field.faces
+    fx, fz = _faces_of(u.reshape(nx, nz), pic.dx, pic.dz)
+    assert np.array_equal(ex, fx) and np.array_equal(ez, fz)
     pic.close()
 
 
