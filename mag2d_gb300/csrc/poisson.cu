@@ -608,7 +608,7 @@ struct TileShared {
     uint8_t* f;  // 1: outside the grid, or a fixed node of the fine level
 };
 
-__device__ __forceinline__ TileShared tile_shared(const TileRegion& T, int l)
+__device__ __forceinline__ TileShared tile_shared(const TileRegion& T, bool staged)
 {
     extern __shared__ __align__(16) unsigned char tile_smem[];
     const int n = T.rh * T.rw;
@@ -617,7 +617,7 @@ __device__ __forceinline__ TileShared tile_shared(const TileRegion& T, int l)
     S.r = S.e + n;
     S.cf = S.r + n;
     S.dg = S.cf + 9 * n;
-    S.f = reinterpret_cast<uint8_t*>(l > 0 ? S.dg + n : S.cf);
+    S.f = reinterpret_cast<uint8_t*>(staged ? S.dg + n : S.cf);
     return S;
 }
 
@@ -637,7 +637,7 @@ __device__ void tile_load(const SolveArgs& a, int l, const TileRegion& T, const 
         S.r[q] = in ? L.r[k] : 0.f;
         S.e[q] = (in && load_e) ? L.e[k] : 0.f;
         S.f[q] = (!in || (l == 0 && is_fixed(a.mask[k]))) ? 1 : 0;
-        if (l > 0) {
+        if (l > 0 && L.staged) {
 #pragma unroll
             for (int p = 0; p < 9; ++p) S.cf[p * n + q] = in ? __ldg(&L.coef[p * nn + k]) : 0.f;
             S.dg[q] = in ? __ldg(&L.inv_diag[k]) : 0.f;
@@ -683,6 +683,9 @@ __device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const 
             const int p = li * T.rw + lj;
             if (S.f[p]) continue;
             const int i = T.ri + li, j = T.rj + lj;
+            // the operator row from the staged planes or from the level's own
+            const float* cf = L.staged ? S.cf + p : L.coef + ((size_t)i * L.nz + j);
+            const size_t cs = L.staged ? (size_t)nr : (size_t)L.nx * L.nz;
             float off = 0.f;
 #pragma unroll
             for (int di = -1; di <= 1; ++di) {
@@ -691,10 +694,11 @@ __device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const 
                 for (int dj = -1; dj <= 1; ++dj) {
                     if (j + dj < 0 || j + dj >= L.nz) continue;
                     if (di == 0 && dj == 0) continue;
-                    off += S.cf[((di + 1) * 3 + (dj + 1)) * nr + p] * S.e[p + di * T.rw + dj];
+                    off += cf[((di + 1) * 3 + (dj + 1)) * cs] * S.e[p + di * T.rw + dj];
                 }
             }
-            S.e[p] = (S.r[p] - off) * S.dg[p];
+            const float dg = L.staged ? S.dg[p] : __ldg(&L.inv_diag[(size_t)i * L.nz + j]);
+            S.e[p] = (S.r[p] - off) * dg;
         }
     }
 }
@@ -723,6 +727,8 @@ __device__ void tile_residual(const SolveArgs& a, int l, const TileRegion& T, co
             acc -= k2 * S.e[q - 1];
             acc -= k2 * S.e[q + 1];
         } else {
+            const float* cf = L.staged ? S.cf + q : L.coef + ((size_t)i * L.nz + j);
+            const size_t cs = L.staged ? (size_t)n : (size_t)L.nx * L.nz;
             float ae = 0.f;
 #pragma unroll
             for (int di = -1; di <= 1; ++di) {
@@ -730,7 +736,7 @@ __device__ void tile_residual(const SolveArgs& a, int l, const TileRegion& T, co
 #pragma unroll
                 for (int dj = -1; dj <= 1; ++dj) {
                     if (j + dj < 0 || j + dj >= L.nz) continue;
-                    ae += S.cf[((di + 1) * 3 + (dj + 1)) * n + q] * S.e[q + di * T.rw + dj];
+                    ae += cf[((di + 1) * 3 + (dj + 1)) * cs] * S.e[q + di * T.rw + dj];
                 }
             }
             acc = S.r[q] - ae;
@@ -749,7 +755,7 @@ __device__ void tile_down(const SolveArgs& a, int l)
     const int ncolors = l == 0 ? 2 : 4;
     for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
-        const TileShared S = tile_shared(T, l);
+        const TileShared S = tile_shared(T, l > 0 && L.staged);
         tile_load(a, l, T, S, false);
         __syncthreads();
         int pass = 0;
@@ -805,7 +811,7 @@ __device__ void tile_up(const SolveArgs& a, int l, int res_slot)
     const int ncolors = l == 0 ? 2 : 4;
     for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
-        const TileShared S = tile_shared(T, l);
+        const TileShared S = tile_shared(T, l > 0 && L.staged);
         tile_load(a, l, T, S, true);
         __syncthreads();
         // e += P e_coarse on every region node of the grid (prolong_level)

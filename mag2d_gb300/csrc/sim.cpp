@@ -610,11 +610,24 @@ void Sim::run_solve(SolveArgs a)
             const bool fits = ls > 0 && ls < lv.nlev && 2 * std::max(a.nu1, a.nu2) <= kTileHalo - 2;
             lv.ti.assign(lv.nlev, 0);
             lv.tj.assign(lv.nlev, 0);
+            lv.staged.assign(lv.nlev, 0);
             lv.tile_smem = 0;
             if (fits && base_blocks > 1) {
                 size_t smem = 0;
                 for (int l = 0; l < ls; ++l) {
-                    const int bytes = l == 0 ? kTileNodeBytes : kTileNodeBytesGalerkin;
+                    // a Galerkin level stages its operator with the tile when that
+                    // still gives every block one tile; a larger level reads it from
+                    // global memory and takes tiles of the fine level's size instead
+                    // (fewer tile rounds, fewer halo nodes)
+                    int bytes = kTileNodeBytes;
+                    if (l > 0) {
+                        int ti, tj;
+                        choose_tile(lv.nx[l], lv.nz[l], base_blocks, kTileHalo, smem_max / kTileNodeBytesGalerkin, ti,
+                                    tj);
+                        const long long ntiles = (long long)((lv.nx[l] + ti - 1) / ti) * ((lv.nz[l] + tj - 1) / tj);
+                        lv.staged[l] = ntiles <= base_blocks ? 1 : 0;
+                        if (lv.staged[l]) bytes = kTileNodeBytesGalerkin;
+                    }
                     choose_tile(lv.nx[l], lv.nz[l], base_blocks, kTileHalo, smem_max / bytes, lv.ti[l], lv.tj[l]);
                     smem = std::max(smem, (size_t)(lv.ti[l] + 2 * kTileHalo) * (lv.tj[l] + 2 * kTileHalo) * bytes);
                 }
@@ -643,6 +656,7 @@ void Sim::run_solve(SolveArgs a)
                 for (int l = 0; l < ls; ++l) {
                     a.lev[l].ti = lv.ti[l];
                     a.lev[l].tj = lv.tj[l];
+                    a.lev[l].staged = lv.staged[l];
                 }
             }
             MAG_CK(cudaMemsetAsync(d_bar.p, 0, sizeof(GridBarrier), stream));

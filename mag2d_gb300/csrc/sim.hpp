@@ -133,6 +133,7 @@ struct SolverLevels {
     double k2 = 1.0;
     // multi-block solves: tile phases of the levels above the single-block ones
     std::vector<int> ti, tj;     // tile interiors per level (empty: not yet chosen)
+    std::vector<int> staged;     // Galerkin levels: 1 = tiles stage the operator, 0 = read from global memory
     size_t tile_smem = 0;        // dynamic shared memory of the launch (0: tile phases off)
     bool coarse_staged = false;  // block 0's levels fit the dynamic shared memory
     // the all-FP64 multigrid (SimOptions::multigrid_fp64): the same levels in FP64
