@@ -386,7 +386,10 @@ template <> struct Vec<4> {
     static __device__ __forceinline__ float& at(F& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
 };
 
-template <int VEC> constexpr int push_min_blocks() { return VEC == 4 ? 2 : VEC == 2 ? 3 : 4; }
+// blocks of 256 per SM the register budget is set for: the 4-slot kernel fits
+// 63 registers without spills, and 4 blocks (32 warps) issue faster than 3 at
+// 80 registers (1e8 electrons: 1.57 against 1.61 ms; 5 blocks spill)
+template <int VEC> constexpr int push_min_blocks() { return VEC == 4 ? 4 : VEC == 2 ? 3 : 4; }
 
 // Persistent grid-stride kernel over groups of VEC consecutive slots: every
 // load of a group (x, z, vx, vy, vz and, with collisions, id) is issued before
