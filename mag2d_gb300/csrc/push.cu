@@ -390,6 +390,8 @@ template <> struct Vec<4> {
 // 63 registers without spills, and 4 blocks (32 warps) issue faster than 3 at
 // 80 registers (1e8 electrons: 1.57 against 1.61 ms; 5 blocks spill)
 template <int VEC> constexpr int push_min_blocks() { return VEC == 4 ? 4 : VEC == 2 ? 3 : 4; }
+// the batched kernel keeps the earlier budget (its 4-slot variant would spill at 64 registers)
+template <int VEC> constexpr int batch_min_blocks() { return VEC == 4 ? 2 : VEC == 2 ? 3 : 4; }
 
 // Persistent grid-stride kernel over groups of VEC consecutive slots: every
 // load of a group (x, z, vx, vy, vz and, with collisions, id) is issued before
@@ -627,7 +629,7 @@ __global__ void __launch_bounds__(256, 3) k_push_fused(const __grid_constant__ P
 constexpr int kBatchIters = 4;
 
 template <int COORD, int EMODE, bool BFIELD, int VEC>
-__global__ void __launch_bounds__(256, push_min_blocks<VEC>())
+__global__ void __launch_bounds__(256, batch_min_blocks<VEC>())
     k_push_batch(const PushArgs* __restrict__ args, const unsigned* __restrict__ chunk_off, int nitems)
 {
     using V = Vec<VEC>;
