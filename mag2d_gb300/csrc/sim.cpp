@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iomanip>
@@ -1502,13 +1503,17 @@ void Sim::set_particles(int s, int64_t n, const double* x, const double* z, cons
     S.scrambled = cell_order_broken(x, z, n);
     upload_slots(s);
     init_ttd(s, 0, n);
-    sort_due = true;
+    // particles read back from a sorted run keep the order the particle
+    // kernel's deposit tiles rely on: only scrambled ones are sorted at once
+    if (S.scrambled) sort_due = true;
 }
 
 // Whether host particles come in no cell order: eight windows of 512
 // consecutive particles spread over the arrays, scrambled when more than a
-// quarter of the neighbour pairs step back in cell index.  (Particles read back
-// from a sorted species step back only where one crossed a cell edge since.)
+// quarter of the neighbour pairs lie more than four grid rows apart.
+// (Particles read back from a sorted run have moved a cell or two since:
+// their neighbours stay within a few cells, while random order puts them a
+// third of the grid apart.)
 bool Sim::cell_order_broken(const double* x, const double* z, int64_t n) const
 {
     if (n < 2) return false;
@@ -1517,18 +1522,19 @@ bool Sim::cell_order_broken(const double* x, const double* z, int64_t n) const
     };
     auto cell = [&](int64_t k) { return index((x[k] - x0) / dx, nx - 2) * (nz - 1) + index((z[k] - z0) / dz, nz - 2); };
     const int64_t w = std::min<int64_t>(512, n);
-    int64_t pairs = 0, back = 0;
+    const int64_t far = 4 * (int64_t)(nz - 1);
+    int64_t pairs = 0, apart = 0;
     for (int k = 0; k < 8; ++k) {
         const int64_t first = (n - w) * k / 8;
         int64_t prev = cell(first);
         for (int64_t q = first + 1; q < first + w; ++q) {
             const int64_t c = cell(q);
-            back += c < prev;
+            apart += std::llabs(c - prev) > far;
             ++pairs;
             prev = c;
         }
     }
-    return 4 * back > pairs;
+    return 4 * apart > pairs;
 }
 
 // Pic::print_trace (src/pic.cpp:446-451): TrackedParticle::print of every
