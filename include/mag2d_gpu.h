@@ -248,8 +248,8 @@ int mag_config_species(const char* config_path, const char* species_conf_path, i
  * Working memory is one static device array of 4 MiB that every GPU loading the
  * library holds until exit; grids above 257 x 257 nodes are rejected with
  * MAG_EINVAL.  The first call on a device looks up the array's device address
- * with that device current and keeps it for the process, so make it before any
- * stream capture; the kept address does not survive cudaDeviceReset.  All
+ * with that device current and keeps it for the process; the kept address
+ * does not survive cudaDeviceReset.  All
  * calls share the array and it keeps the last call's contents: calls that
  * overlap on the GPU race. */
 int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, double dz, double macroparticle_factor,

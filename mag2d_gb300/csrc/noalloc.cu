@@ -16,8 +16,8 @@
 //     of the grid must fit kNoAllocScratchBytes; larger grids are rejected;
 //   * the first call on a device looks up the device address of the array
 //     (cudaGetSymbolAddress) with that device current and keeps it for the
-//     process; make that first call before any stream capture.  The kept
-//     address does not survive cudaDeviceReset of that device;
+//     process.  The kept address does not survive cudaDeviceReset of that
+//     device;
 //   * with info == NULL the call returns once the work is queued and reports
 //     nothing about the solve (convergence or a barrier timeout stays in the
 //     array and the next call clears it); voltage_host is copied
