@@ -39,10 +39,10 @@ __device__ __forceinline__ int key_of(uint32_t x, uint32_t z, const SortArgs& a)
     return (i >> a.si) * a.nzk + (j >> a.sj);
 }
 
-// Runs of consecutive lanes with the same cell (c < 0: no particle): the
+// Runs of consecutive lanes with the same key (c < 0: no particle): the
 // lane's run head and, for a head, the run's length.  Particles sorted a few
-// steps ago arrive in such runs; a cell that occurs in two runs of a warp is
-// simply counted twice.
+// steps ago arrive in such runs; a key that occurs in two runs of a warp is
+// simply looked up twice.
 struct LaneRun {
     int head, len;
     bool is_head;
