@@ -112,6 +112,7 @@ __device__ __forceinline__ bool is_fixed(int8_t m) { return m == 0 || m == 1; }
 struct FastDiv {
     unsigned d, mp;
     int l;
+    __device__ FastDiv() : d(1), mp(0), l(0) {}
     __device__ explicit FastDiv(unsigned dd) : d(dd)
     {
         l = dd > 1 ? 32 - __clz(dd - 1) : 0;  // ceil(log2 d)
@@ -606,6 +607,10 @@ struct TileShared {
     float* cf;   // Galerkin levels: the 9 operator planes of the region (plane p of node q at p * n + q)
     float* dg;   // Galerkin levels: inverse diagonal
     uint8_t* f;  // 1: outside the grid, or a fixed node of the fine level
+    // divisions of the tile's loops, set up once per tile (the set-up itself
+    // is a 64-bit division): by the region width, by its half (colour passes)
+    // and by the interior width
+    FastDiv dw, dh, dj;
 };
 
 __device__ __forceinline__ TileShared tile_shared(const TileRegion& T, bool staged)
@@ -618,6 +623,9 @@ __device__ __forceinline__ TileShared tile_shared(const TileRegion& T, bool stag
     S.cf = S.r + n;
     S.dg = S.cf + 9 * n;
     S.f = reinterpret_cast<uint8_t*>(staged ? S.dg + n : S.cf);
+    S.dw = FastDiv((unsigned)T.rw);
+    S.dh = FastDiv((unsigned)((T.rw + 1) / 2));
+    S.dj = FastDiv((unsigned)T.nj);
     return S;
 }
 
@@ -627,7 +635,7 @@ __device__ void tile_load(const SolveArgs& a, int l, const TileRegion& T, const 
 {
     const MGLevelDev& L = a.lev[l];
     const int n = T.rh * T.rw;
-    const FastDiv dw((unsigned)T.rw);
+    const FastDiv& dw = S.dw;
     const size_t nn = (size_t)L.nx * L.nz;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
         const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
@@ -654,7 +662,7 @@ __device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const 
         const float k2 = (float)a.k2;
         const int hw = (T.rw + 1) / 2;
         const int n = T.rh * hw;
-        const FastDiv dh((unsigned)hw);
+        const FastDiv& dh = S.dh;
         for (int q = threadIdx.x; q < n; q += blockDim.x) {
             const int li = (int)dh.div((unsigned)q);
             const int lj = 2 * (q - li * hw) + ((color + T.ri + T.rj + li) & 1);
@@ -674,7 +682,7 @@ __device__ void tile_pass(const SolveArgs& a, int l, const TileRegion& T, const 
         const int hh = (T.rh + 1) / 2, hw = (T.rw + 1) / 2;
         const int n = hh * hw;
         const int nr = T.rh * T.rw;
-        const FastDiv dh((unsigned)hw);
+        const FastDiv& dh = S.dh;
         for (int q = threadIdx.x; q < n; q += blockDim.x) {
             const int a2 = (int)dh.div((unsigned)q);
             const int li = 2 * a2 + ((ci + T.ri) & 1);
@@ -708,7 +716,7 @@ __device__ void tile_residual(const SolveArgs& a, int l, const TileRegion& T, co
 {
     const MGLevelDev& L = a.lev[l];
     const int n = T.rh * T.rw;
-    const FastDiv dw((unsigned)T.rw);
+    const FastDiv& dw = S.dw;
     const float* __restrict__ st = a.st32;
     const float k2 = (float)a.k2;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
@@ -766,7 +774,7 @@ __device__ void tile_down(const SolveArgs& a, int l)
             }
         // the tile's correction back to the level (read again by the up phase)
         for (int q = threadIdx.x; q < T.ni * T.nj; q += blockDim.x) {
-            const int ii = q / T.nj, jj = q - ii * T.nj;
+            const int ii = (int)S.dj.div((unsigned)q), jj = q - ii * T.nj;
             L.e[(size_t)(T.i0 + ii) * L.nz + T.j0 + jj] = S.e[(ii + kTileHalo) * T.rw + jj + kTileHalo];
         }
         tile_residual(a, l, T, S, kTileHalo - 1 - pass);
@@ -777,8 +785,10 @@ __device__ void tile_down(const SolveArgs& a, int l)
         const int J0 = (T.j0 + sz - 1) / sz, J1 = (T.j0 + T.nj - 1) / sz;
         const int cw = J1 - J0 + 1, nc = (I1 - I0 + 1) * cw;
         auto get = [&](int i, int j) { return S.r[(i - T.ri) * T.rw + (j - T.rj)]; };
+        const FastDiv dcw((unsigned)cw);
         for (int q = threadIdx.x; q < nc; q += blockDim.x) {
-            const int I = I0 + q / cw, J = J0 + q % cw;
+            const int qi = (int)dcw.div((unsigned)q);
+            const int I = I0 + qi, J = J0 + (q - qi * cw);
             const size_t K = (size_t)I * C.nz + J;
             C.r[K] = restrict_node(I, J, L.cmode, L.nx, L.nz, get);
             C.e[K] = 0.f;
@@ -816,7 +826,7 @@ __device__ void tile_up(const SolveArgs& a, int l, int res_slot)
         __syncthreads();
         // e += P e_coarse on every region node of the grid (prolong_level)
         const int n = T.rh * T.rw;
-        const FastDiv dw((unsigned)T.rw);
+        const FastDiv& dw = S.dw;
         for (int q = threadIdx.x; q < n; q += blockDim.x) {
             if (S.f[q]) continue;
             const int li = (int)dw.div((unsigned)q), lj = q - li * T.rw;
@@ -832,7 +842,7 @@ __device__ void tile_up(const SolveArgs& a, int l, int res_slot)
         float lres = 0.f;
         unsigned lumax_hi = 0u;
         for (int q = threadIdx.x; q < T.ni * T.nj; q += blockDim.x) {
-            const int ii = q / T.nj, jj = q - ii * T.nj;
+            const int ii = (int)S.dj.div((unsigned)q), jj = q - ii * T.nj;
             const int p = (ii + kTileHalo) * T.rw + jj + kTileHalo;
             const size_t k = (size_t)(T.i0 + ii) * L.nz + T.j0 + jj;
             if (l > 0) {
