@@ -347,8 +347,30 @@ struct GridBarrier {
     unsigned int pad[2];
 };
 
+// Magic numbers of an unsigned division by a divisor fixed for a whole pass
+// (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, figure 4.1): n / d = (t + ((n - t) >> 1)) >> (l - 1)
+// with t = umulhi(m, n), exact for every 32-bit n.  Setting them up takes a
+// 64-bit division, so the host does it once per level.
+struct DivMagic {
+    unsigned d, m;
+    int l;
+};
+__host__ __device__ inline DivMagic div_magic(unsigned d)
+{
+    DivMagic r{d, 0u, 0};
+    if (d > 1) {
+        int l = 0;
+        while (l < 32 && (1ull << l) < d) ++l;  // ceil(log2 d)
+        r.l = l;
+        r.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+    return r;
+}
+
 struct MGLevelDev {
     int nx, nz;
+    DivMagic dz, dhz;       // divisions by nz and by (nz + 1) / 2
     float* e;               // correction
     float* r;               // right-hand side of the correction equation
     float* t;               // residual scratch

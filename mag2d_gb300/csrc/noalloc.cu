@@ -236,6 +236,8 @@ extern "C" int mag_poisson_solve_noalloc(int coord, int nx, int nz, double dx, d
     for (int l = 0; l < nlev; ++l) {
         a.lev[l].nx = lnx[l];
         a.lev[l].nz = lnz[l];
+        a.lev[l].dz = div_magic((unsigned)lnz[l]);
+        a.lev[l].dhz = div_magic((unsigned)((lnz[l] + 1) / 2));
         a.lev[l].e = (float*)(base + o_e[l]);
         a.lev[l].r = (float*)(base + o_r[l]);
         a.lev[l].t = (float*)(base + o_t[l]);

@@ -118,6 +118,7 @@ struct FastDiv {
         l = dd > 1 ? 32 - __clz(dd - 1) : 0;  // ceil(log2 d)
         mp = (unsigned)(((1ull << 32) * ((1ull << l) - dd)) / dd + 1);
     }
+    __device__ explicit FastDiv(const DivMagic& m) : d(m.d), mp(m.m), l(m.l) {}
     __device__ __forceinline__ unsigned div(unsigned n) const
     {
         if (d == 1) return n;
@@ -214,7 +215,7 @@ __device__ void smooth_fine(const SolveArgs& a, Team& t, int sweeps, bool revers
     const float* __restrict__ st = a.st32;
     const float k2 = (float)a.k2;
     const unsigned n = (unsigned)(nx * hz);
-    const FastDiv dh((unsigned)hz);
+    const FastDiv dh(L.dhz);
     for (int s = 0; s < sweeps && ok; ++s)
         for (int cc = 0; cc < 2 && ok; ++cc) {
             const int color = reverse ? 1 - cc : cc;
@@ -273,7 +274,7 @@ __device__ void smooth_coarse(const SolveArgs& a, Team& t, int l, int sweeps, bo
     const float* __restrict__ coef = L.coef;
     const float* __restrict__ idg = L.inv_diag;
     const unsigned n = (unsigned)(hx * hz);
-    const FastDiv dh((unsigned)hz);
+    const FastDiv dh(L.dhz);
     for (int s = 0; s < sweeps && ok; ++s)
         for (int cc = 0; cc < 4 && ok; ++cc) {
             const int color = reverse ? 3 - cc : cc;
@@ -299,7 +300,7 @@ __device__ void residual_level(const SolveArgs& a, Team& t, int l, float* __rest
     const float* __restrict__ e = L.e;
     const float* __restrict__ r = L.r;
     const unsigned n = (unsigned)(nx * nz);
-    const FastDiv dz((unsigned)nz);
+    const FastDiv dz(L.dz);
     if (l == 0) {
         const int8_t* __restrict__ mask = a.mask;
         const float* __restrict__ st = a.st32;
@@ -383,7 +384,7 @@ __device__ void restrict_level(const SolveArgs& a, Team& t, int l, const float* 
     float* __restrict__ cr = C.r;
     float* __restrict__ ce = C.e;
     const unsigned n = (unsigned)(C.nx * C.nz);
-    const FastDiv dz((unsigned)C.nz);
+    const FastDiv dz(C.dz);
     const int fnz = F.nz;
     auto get = [&](int i, int j) { return tl[(size_t)i * fnz + j]; };
 #pragma unroll 2
@@ -402,7 +403,7 @@ __device__ void prolong_level(const SolveArgs& a, Team& t, int l)
     const float* __restrict__ ec = C.e;
     float* __restrict__ fe = F.e;
     const unsigned n = (unsigned)(F.nx * F.nz);
-    const FastDiv dz((unsigned)F.nz);
+    const FastDiv dz(F.dz);
 #pragma unroll 4
     for (unsigned q = t.tid; q < n; q += t.nthreads) {
         if (l == 0 && is_fixed(a.mask[q])) continue;
@@ -985,7 +986,7 @@ __device__ void solve_prologue(const SolveArgs& a, Team& t, bool& ok)
     // one pass: both are per node
     const bool extrap = a.u_prev != nullptr;
     const bool valid = extrap && *((volatile const int*)a.u_prev_valid) != 0;
-    const FastDiv dnz((unsigned)nz);
+    const FastDiv dnz(a.lev[0].dz);
 #pragma unroll 2
     for (unsigned k = t.tid; k < nn; k += t.nthreads) {
         const int i = (int)dnz.div(k);
@@ -1036,7 +1037,7 @@ __device__ void solve_body(const SolveArgs& a, Team& t)
     const unsigned long long t_start = Team::now();
     t.t_mark = t_start;
     solve_prologue(a, t, ok);
-    const FastDiv dnz((unsigned)nz);
+    const FastDiv dnz(a.lev[0].dz);
     t.mark(kPhaseStart);
     // 2. FP64 residual refinement around the FP32 multigrid
     int it = 0;

@@ -707,6 +707,8 @@ SolveArgs Sim::solve_args(bool rf_solve, int rho_src, bool clear_rho)
     for (int l = 0; l < lv.nlev; ++l) {
         a.lev[l].nx = lv.nx[l];
         a.lev[l].nz = lv.nz[l];
+        a.lev[l].dz = div_magic((unsigned)lv.nz[l]);
+        a.lev[l].dhz = div_magic((unsigned)((lv.nz[l] + 1) / 2));
         a.lev[l].e = lv.e[l].p;
         a.lev[l].r = lv.r[l].p;
         a.lev[l].t = lv.t[l].p;
