@@ -377,6 +377,9 @@ struct MGLevelDev {
     const float* coef;      // 9 planes of nx*nz (levels >= 1), plane k = (di+1)*3 + (dj+1)
     const float* inv_diag;  // levels >= 1
     int ti, tj;             // multi-block solves: interior size of this level's tiles (0: not tiled)
+    // divisions of a tile's loops, for the interior tiles [0] and the last
+    // column of tiles [1]: by the region width, by its half, by the interior width
+    DivMagic tw[2], th[2], tn[2];
     int staged;             // Galerkin levels of a tiled solve: 1 = tiles stage the operator in shared memory,
                             // 0 = the passes read it from global memory (larger tiles)
     int cmode;              // coarsening to the next level: 0 both directions, 1 x only, 2 z only

@@ -614,7 +614,7 @@ struct TileShared {
     FastDiv dw, dh, dj;
 };
 
-__device__ __forceinline__ TileShared tile_shared(const TileRegion& T, bool staged)
+__device__ __forceinline__ TileShared tile_shared(const TileRegion& T, const MGLevelDev& L, bool staged)
 {
     extern __shared__ __align__(16) unsigned char tile_smem[];
     const int n = T.rh * T.rw;
@@ -624,9 +624,10 @@ __device__ __forceinline__ TileShared tile_shared(const TileRegion& T, bool stag
     S.cf = S.r + n;
     S.dg = S.cf + 9 * n;
     S.f = reinterpret_cast<uint8_t*>(staged ? S.dg + n : S.cf);
-    S.dw = FastDiv((unsigned)T.rw);
-    S.dh = FastDiv((unsigned)((T.rw + 1) / 2));
-    S.dj = FastDiv((unsigned)T.nj);
+    const int c = T.nj == L.tj ? 0 : 1;  // the last column of tiles may be narrower
+    S.dw = FastDiv(L.tw[c]);
+    S.dh = FastDiv(L.th[c]);
+    S.dj = FastDiv(L.tn[c]);
     return S;
 }
 
@@ -764,7 +765,7 @@ __device__ void tile_down(const SolveArgs& a, int l)
     const int ncolors = l == 0 ? 2 : 4;
     for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
-        const TileShared S = tile_shared(T, l > 0 && L.staged);
+        const TileShared S = tile_shared(T, L, l > 0 && L.staged);
         tile_load(a, l, T, S, false);
         __syncthreads();
         int pass = 0;
@@ -822,7 +823,7 @@ __device__ void tile_up(const SolveArgs& a, int l, int res_slot)
     const int ncolors = l == 0 ? 2 : 4;
     for (int tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
         const TileRegion T = tile_region(tt, L.nx, L.nz, L.ti, L.tj);
-        const TileShared S = tile_shared(T, l > 0 && L.staged);
+        const TileShared S = tile_shared(T, L, l > 0 && L.staged);
         tile_load(a, l, T, S, true);
         __syncthreads();
         // e += P e_coarse on every region node of the grid (prolong_level)

@@ -658,6 +658,13 @@ void Sim::run_solve(SolveArgs a)
                     a.lev[l].ti = lv.ti[l];
                     a.lev[l].tj = lv.tj[l];
                     a.lev[l].staged = lv.staged[l];
+                    const int tj = lv.tj[l], last = lv.nz[l] - (lv.nz[l] + tj - 1) / tj * tj + tj;
+                    const int w[2] = {tj, last};
+                    for (int c = 0; c < 2; ++c) {
+                        a.lev[l].tw[c] = div_magic((unsigned)(w[c] + 2 * kTileHalo));
+                        a.lev[l].th[c] = div_magic((unsigned)((w[c] + 2 * kTileHalo + 1) / 2));
+                        a.lev[l].tn[c] = div_magic((unsigned)w[c]);
+                    }
                 }
             }
             MAG_CK(cudaMemsetAsync(d_bar.p, 0, sizeof(GridBarrier), stream));
